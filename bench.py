@@ -1,0 +1,453 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 3D backpropagation.
+
+Metric: backprop voxel-angle updates/s (A * Nx * Ny * Nx per reconstruction)
+on one GB300, FP32 GPU arithmetic against the FP64 oracle, with the rel-L2
+error stated.
+
+Workload (one step = one full reconstruction): ``backpropagate_3d`` with
+A=200 angles uniform in [0, 2 pi), a 256x256 complex64 sinogram of a seeded
+random-ellipsoid phantom (3-12 ellipsoids, semi-axes 8-60 px, n in
+[1.335, 1.36], nm=1.333, res=3 px/wavelength, Rytov data a + i*phi),
+padfac 1.75 (512x512 padded FFTs), intp_order=2, output 256^3 complex64.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value   device-resident throughput (sinogram already in HBM; the prepared
+        plan's kernels timed with CUDA events on their stream, L2 flushed
+        between steps by a 256 MiB write outside the timed events)
+e2e     the same metric through the public API ``backpropagate_3d`` with a
+        pinned host sinogram in and a host volume out (H2D + D2H inside)
+roofline  the dominant kernel stage, timed live with CUDA events around
+        each of its launches, against MEASURED_PEAKS.json's HBM bandwidth
+cpu_baseline  the FP64 oracle port on this host's cores, on a bounded
+        sample of the same workload (a few angles)
+With --gpus N > 1 (torchrun), every rank runs an independent replica of the
+workload (the path has no exchange step); value sums the ranks' updates
+over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "tests", "golden")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = ("backprop voxel-angle updates/s on 1 GB300, FP32 vs FP64 plain, "
+          "at stated rel-L2")
+UNIT = "voxel-angle updates/s"
+WORKLOAD = dict(A=200, n=256, padfac=1.75, intp_order=2, res=3.0, nm=1.333,
+                lD=0.0, seed=2024, count_range=(3, 12), semi_range=(8, 60))
+WORKLOAD_NAME = ("backpropagate_3d: A=200 x 256x256 complex64 sinogram "
+                 "(ellipsoid phantom) -> 256^3 complex64, padfac 1.75 "
+                 "(512^2 FFTs), intp_order 2")
+CPU_SAMPLE_ANGLES = 4
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the CPU oracle sample (and the rel-L2 check)")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="profiling case: the workload's plane and volume "
+                         "size with 8 angles and the save_memory workspace, "
+                         "two executions, nothing else")
+    return ap.parse_args()
+
+
+def make_workload():
+    from sino_gen import ellipsoid_phantom_sinogram
+    w = WORKLOAD
+    sino, angles = ellipsoid_phantom_sinogram(
+        w["n"], w["A"], seed=w["seed"], count_range=w["count_range"],
+        semi_range=w["semi_range"], res=w["res"], nm=w["nm"])
+    return sino.astype(np.complex64), angles
+
+
+def updates(A, n):
+    return float(A) * n * n * n
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu),
+                 "--query-gpu=" + self.FIELDS, "--format=csv,noheader",
+                 "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(s):
+            try:
+                return float(s.split()[0])
+            except (ValueError, IndexError):
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap")
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(stage):
+    """Per-launch DRAM bytes of `stage` from the committed ncu summary, or
+    None."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            parts = [p.strip() for p in line.strip().strip("|").split("|")]
+            if len(parts) >= 2 and parts[0] == stage:
+                try:
+                    return float(parts[1])
+                except ValueError:
+                    return None
+    return None
+
+
+# --------------------------------------------------------------- CPU side
+def cpu_sample(sino, angles, subset):
+    """Time the FP64 oracle on a sub-problem of `subset` angles with all host
+    threads; return (seconds, volume, cores)."""
+    from oracle import odt_oracle
+    cores = os.cpu_count() or 1
+    w = WORKLOAD
+    s = sino[subset].astype(np.complex128)
+    a = angles[subset]
+    # one-time setup (the propagator table) outside the timed sample
+    cache = {}
+    odt_oracle.backpropagate_3d(s[:1], a[:1], w["res"], w["nm"],
+                                lD=w["lD"], padfac=w["padfac"],
+                                intp_order=w["intp_order"], nthreads=cores,
+                                fft_workers=cores, angle_subset=[],
+                                weight_angles=False, cache=cache)
+    t0 = time.perf_counter()
+    vol = odt_oracle.backpropagate_3d(s, a, w["res"], w["nm"], lD=w["lD"],
+                                      padfac=w["padfac"],
+                                      intp_order=w["intp_order"],
+                                      nthreads=cores, fft_workers=cores,
+                                      cache=cache)
+    return time.perf_counter() - t0, vol, cores
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm's CPU implementation (the
+    FP64 oracle port; the reference is pure Python) on this host's cores.
+    One step = one angle of the workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import odt_oracle
+    sino, angles = make_workload()
+    w = WORKLOAD
+    cores = os.cpu_count() or 1
+    s = sino.astype(np.complex128)
+    times = []
+    # the propagator table is per-call setup in the reference, amortised
+    # over its 200 angles; it is built in the first warm-up step here
+    cache = {}
+    for it in range(args.warmup + args.steps):
+        a = it % w["A"]
+        t0 = time.perf_counter()
+        odt_oracle.backpropagate_3d(s, angles, w["res"], w["nm"],
+                                    lD=w["lD"], padfac=w["padfac"],
+                                    intp_order=w["intp_order"],
+                                    nthreads=cores, fft_workers=cores,
+                                    angle_subset=[a], cache=cache)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+    step = statistics.mean(times)
+    value = updates(1, w["n"]) / step
+    sample = ("one angle of the workload per step (256^3 updates), FP64, "
+              "scipy.fft + OpenMP spline resampling")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME, "sample": "1 angle per step"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------- GPU side
+def run_ours(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    from odtbrain_gb300 import build as native_build
+    native_build.build()
+    import odtbrain_gb300 as odt
+    from odtbrain_gb300._alg3d import Backprop3D
+
+    w = WORKLOAD
+    sino, angles = make_workload()
+    A, n = w["A"], w["n"]
+    U = updates(A, n)
+    host = torch.from_numpy(sino).pin_memory()
+    dsino = host.to(dev)
+    rec = Backprop3D(tuple(sino.shape), angles, w["res"], w["nm"], lD=w["lD"],
+                     padfac=w["padfac"], intp_order=w["intp_order"],
+                     input_dtype="complex64", device=dev)
+    vol = torch.empty(rec.volume_shape(), device=dev, dtype=torch.complex64)
+    flush = torch.empty(L2_FLUSH_BYTES, device=dev, dtype=torch.uint8)
+    for _ in range(max(args.warmup, 1)):
+        rec(dsino, out=vol)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    stream = torch.cuda.current_stream(dev)
+    ev = [(torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        rec(dsino, out=vol, check=False)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    rec.check()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = U * world / (ms_per_step / 1e3)
+
+    # save_memory path (smaller angle batches), same result
+    rec_sm = Backprop3D(tuple(sino.shape), angles, w["res"], w["nm"],
+                        lD=w["lD"], padfac=w["padfac"],
+                        intp_order=w["intp_order"], save_memory=True,
+                        input_dtype="complex64", device=dev)
+    vol_sm = rec_sm(dsino)
+    torch.cuda.synchronize()
+    sm_ev = (torch.cuda.Event(enable_timing=True),
+             torch.cuda.Event(enable_timing=True))
+    flush.zero_()
+    sm_ev[0].record(stream)
+    rec_sm(dsino, out=vol_sm, check=False)
+    sm_ev[1].record(stream)
+    torch.cuda.synchronize()
+    sm_ms = sm_ev[0].elapsed_time(sm_ev[1])
+    sm_same = bool(torch.equal(vol_sm, vol))
+    del rec_sm, vol_sm
+
+    # per-stage live timing (event pair around every launch)
+    flush.zero_()
+    stages = rec.timed(dsino, out=vol)
+    dom = max(stages, key=lambda k: stages[k]["ms"])
+    ds = stages[dom]
+    per_launch_bytes = ds["bytes"] / ds["launches"]
+    per_launch_s = ds["ms"] / ds["launches"] / 1e3
+    peak, peak_kind = measured_peaks()
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    traffic = profile_traffic(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "traffic": traffic,
+                "algorithmic_bytes_per_launch": per_launch_bytes,
+                "launch_ms": per_launch_s * 1e3}
+    stage_summary = {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
+                         "share": round(v["ms"] / sum(x["ms"] for x in
+                                                      stages.values()), 4),
+                         "GB_per_s": (v["bytes"] / (v["ms"] / 1e3) / 1e9
+                                      if v["ms"] > 0 else None)}
+                     for k, v in stages.items()}
+
+    # end to end through the public API, host buffers
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 5))
+    kw = dict(lD=w["lD"], padfac=w["padfac"], intp_order=w["intp_order"],
+              dtype=np.float32)
+    host_np = host.numpy()
+    out = odt.backpropagate_3d(host_np, angles, w["res"], w["nm"], **kw)
+    e2e_t = []
+    barrier()
+    for _ in range(e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = odt.backpropagate_3d(host_np, angles, w["res"], w["nm"], **kw)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_t)
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": U * world / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(host.numel() * host.element_size()),
+           "d2h_bytes_per_step": int(out.nbytes),
+           "ms_per_step": e2e_s * 1e3}
+
+    line = None
+    if rank == 0:
+        cpu = None
+        accuracy = None
+        if not args.no_cpu_baseline:
+            subset = list(range(0, A, A // CPU_SAMPLE_ANGLES))[
+                :CPU_SAMPLE_ANGLES]
+            t_cpu, ref, cores = cpu_sample(sino, angles, subset)
+            cpu = {"value": updates(len(subset), n) / t_cpu, "unit": UNIT,
+                   "cores": cores, "kind": "port",
+                   "sample": "%d of the %d angles as a %d-angle problem "
+                             "(%d x 256^3 updates), FP64 oracle, %.1f s"
+                             % (len(subset), A, len(subset), len(subset),
+                                t_cpu)}
+            sub = Backprop3D((len(subset), n, n), angles[subset], w["res"],
+                             w["nm"], lD=w["lD"], padfac=w["padfac"],
+                             intp_order=w["intp_order"],
+                             input_dtype="complex64", device=dev)
+            got = sub(dsino[subset].contiguous()).cpu().numpy()
+            rel = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+            mx = float(np.abs(got - ref).max() / np.abs(ref).max())
+            accuracy = {"rel_l2": rel, "max_abs_rel": mx,
+                        "vs": "FP64 oracle, same %d-angle sub-problem"
+                        % len(subset)}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 (complex64)", "data": "synthetic",
+            "config": {"workload": WORKLOAD_NAME, "A": A, "n": n,
+                       "padded_fft": 512, "intp_order": w["intp_order"],
+                       "save_memory": False,
+                       "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "e2e": e2e,
+            "gpu_launches": rec.launches_per_call * args.steps,
+            "roofline": roofline,
+            "stages": stage_summary,
+            "save_memory_ms_per_step": sm_ms,
+            "save_memory_identical": sm_same,
+            "accuracy": accuracy,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "step_ms": [round(x, 3) for x in step_ms],
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_ncu_case():
+    import torch
+    from odtbrain_gb300 import build as native_build
+    native_build.build()
+    from odtbrain_gb300._alg3d import Backprop3D
+    w = WORKLOAD
+    sino, angles = make_workload()
+    sino, angles = sino[:8].copy(), angles[:8].copy()
+    dev = torch.device("cuda", 0)
+    rec = Backprop3D(tuple(sino.shape), angles, w["res"], w["nm"],
+                     lD=w["lD"], padfac=w["padfac"],
+                     intp_order=w["intp_order"], save_memory=True,
+                     input_dtype="complex64", device=dev)
+    d = torch.from_numpy(sino).to(dev)
+    for _ in range(2):
+        vol = rec(d)
+    torch.cuda.synchronize()
+    print("ncu case done: %d launches per execution, volume %s" %
+          (rec.launches_per_call, tuple(vol.shape)))
+
+
+def main():
+    args = parse_args()
+    if args.ncu_case:
+        run_ncu_case()
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+/*
+ * odtbrain_gb300 -- C ABI of the GB300 (sm_103a) 3D filtered backpropagation.
+ *
+ * The library replaces the compute of two reference entry points:
+ *
+ *   odtbrain.backpropagate_3d         odtbrain/_alg3d_bpp.py:84-555
+ *   odtbrain.backpropagate_3d_tilted  odtbrain/_alg3d_bppt.py:374-949
+ *
+ * The reference is pure Python (NumPy + pyFFTW + numexpr + scipy.ndimage +
+ * multiprocessing); it has no foreign-function interface of its own.  The
+ * entry points below are what a binding of that Python path binds: the host
+ * computes the FP64 constants exactly as the reference does (angle weights,
+ * filter, propagator phase, rotation matrices and offsets) and hands plain
+ * pointers to this library, which runs the per-angle pipeline on the GPU:
+ *
+ *   (a) pad + weight + forward 2D FFT + filter    _alg3d_bpp.py:493-509
+ *   (b) per-plane propagator + inverse FFT + crop _alg3d_bpp.py:514-528
+ *   (c) spline rotation + accumulation            _alg3d_bpp.py:532-546,
+ *                                                 _alg3d_bppt.py:904-944
+ *
+ * All functions return an odt_status; none of them throws.  Device pointers
+ * are raw CUDA device addresses; `stream` is a cudaStream_t passed as void*.
+ * Execution is stream-ordered and does not synchronise the host, except
+ * odt_bpp3d_read_status which waits for the stream.
+ */
+#ifndef ODTBRAIN_GB300_H
+#define ODTBRAIN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum odt_status {
+    ODT_OK = 0,
+    ODT_ERR_INVALID_ARGUMENT = 1, /* maps to ValueError on the Python side   */
+    ODT_ERR_UNSUPPORTED = 2,      /* maps to NotImplementedError             */
+    ODT_ERR_CUDA = 3,             /* a CUDA runtime call failed              */
+    ODT_ERR_OUT_OF_MEMORY = 4,    /* plan tables could not be allocated      */
+    ODT_ERR_DEVICE_CHECK = 5      /* a kernel's own bounds check tripped     */
+} odt_status;
+
+enum odt_pad_mode {
+    ODT_PAD_NONE = 0,  /* padding=(False, False)                 */
+    ODT_PAD_EDGE = 1,  /* padval="edge": np.pad(mode="edge")     */
+    ODT_PAD_RAMP = 2   /* padval=float: np.pad(mode="linear_ramp") */
+};
+
+enum odt_geometry {
+    /* scipy.ndimage.rotate of every (z, x) plane about the y axis,
+     * _alg3d_bpp.py:68-81; 6 doubles per angle: m00 m01 m10 m11 off0 off1 */
+    ODT_GEOM_Y_AXIS = 0,
+    /* scipy.ndimage.affine_transform of the (x, -y, z) volume,
+     * _alg3d_bppt.py:904-944; 12 doubles per angle: 3x3 matrix row-major,
+     * then the offset */
+    ODT_GEOM_AFFINE3D = 1
+};
+
+enum odt_input_dtype { ODT_INPUT_C64 = 0, ODT_INPUT_C128 = 1 };
+
+typedef struct odt_bpp3d_desc {
+    int32_t num_angles;          /* A                                        */
+    int32_t ny, nx;              /* sinogram plane; volume is (nx, ny, nx)  */
+    int32_t pad_ny, pad_nx;      /* padded FFT sizes lNy, lNx               */
+    int32_t pad_y_left;          /* padyl, _alg3d_bpp.py:300                */
+    int32_t pad_x_left;          /* padxl, _alg3d_bpp.py:302                */
+    int32_t pad_mode;            /* enum odt_pad_mode                       */
+    double padval_re, padval_im; /* linear-ramp end value                   */
+    int32_t intp_order;          /* spline order 0..3                       */
+    int32_t geometry;            /* enum odt_geometry                       */
+    int32_t onlyreal;            /* output float32 real part only           */
+    int32_t input_dtype;         /* enum odt_input_dtype                    */
+    /* Host arrays of pad_ny*pad_nx entries, row-major [ky][kx] in FFT order:
+     * filter: complex128 (interleaved re, im) =
+     *   prefactor [* filterabs] / (lNx*lNy)      _alg3d_bpp.py:389-399, 509
+     * kz_phase: km*(M-1), the propagator phase per unit z  :419-437 */
+    const double *filter;
+    const double *kz_phase;
+    uint64_t workspace_limit;    /* bytes of scratch the plan may use; 0 =
+                                    library default                         */
+} odt_bpp3d_desc;
+
+typedef struct odt_bpp3d_plan odt_bpp3d_plan;
+
+/* Build a plan (device tables for the filter, the propagator and the FFT
+ * twiddles).  Replaces the per-call setup of _alg3d_bpp.py:237-487. */
+odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc,
+                                 odt_bpp3d_plan **plan);
+
+/* Bytes of device scratch odt_bpp3d_execute needs. */
+odt_status odt_bpp3d_workspace_size(const odt_bpp3d_plan *plan,
+                                    uint64_t *bytes);
+
+/* Number of angles the plan processes per pass of the rotation kernel. */
+odt_status odt_bpp3d_angle_batch(const odt_bpp3d_plan *plan, int32_t *batch);
+
+/* Run the backpropagation (the loop of _alg3d_bpp.py:492-549).
+ *   sino      device, (A, ny, nx) complex64 or complex128 (desc.input_dtype)
+ *   weights   device, A doubles (angle weights, util.py:4-67) or NULL
+ *   geometry  device, A*6 (Y_AXIS) or A*12 (AFFINE3D) doubles
+ *   volume    device, (nx, ny, nx) complex64, or float32 when onlyreal;
+ *             fully overwritten
+ *   workspace device, odt_bpp3d_workspace_size bytes, 256-byte aligned */
+odt_status odt_bpp3d_execute(const odt_bpp3d_plan *plan, const void *sino,
+                             const double *weights, const double *geometry,
+                             void *volume, void *workspace, void *stream);
+
+/* Per-stage record of one execution, for measurement. */
+enum odt_stage {
+    ODT_STAGE_ROWS_FORWARD = 0,      /* (a) pad, weight, forward FFT along x */
+    ODT_STAGE_COLUMNS_PROPAGATE = 1, /* (b) FFT along y, filter, propagator,
+                                        backward FFT along y               */
+    ODT_STAGE_ROWS_INVERSE = 2,      /* (b) backward FFT along x, crop      */
+    ODT_STAGE_ROTATE = 3,            /* (c) spline resampling + accumulation */
+    ODT_NUM_STAGES = 4
+};
+typedef struct odt_stage_timing {
+    double ms[ODT_NUM_STAGES];        /* summed CUDA-event time per stage */
+    int64_t launches[ODT_NUM_STAGES]; /* kernel launches per stage        */
+    double bytes[ODT_NUM_STAGES];     /* algorithmic HBM bytes per stage:
+                                         (a) sinogram read + spectrum write,
+                                         (b) spectrum read / slab write,
+                                         (c) slab read + volume write      */
+} odt_stage_timing;
+
+/* odt_bpp3d_execute with a CUDA event pair around every kernel launch;
+ * waits for `stream` and fills `timing`.  No counterpart in the reference
+ * (measurement only). */
+odt_status odt_bpp3d_execute_timed(const odt_bpp3d_plan *plan,
+                                   const void *sino, const double *weights,
+                                   const double *geometry, void *volume,
+                                   void *workspace, void *stream,
+                                   odt_stage_timing *timing);
+
+/* Number of kernel launches one odt_bpp3d_execute makes. */
+odt_status odt_bpp3d_launch_count(const odt_bpp3d_plan *plan,
+                                  int64_t *launches);
+
+/* Wait for `stream`, then return ODT_ERR_DEVICE_CHECK if any kernel of this
+ * plan recorded a failed internal check since the last call (the status word
+ * is cleared). */
+odt_status odt_bpp3d_read_status(const odt_bpp3d_plan *plan, void *stream);
+
+odt_status odt_bpp3d_plan_destroy(odt_bpp3d_plan *plan);
+
+/* Human-readable text of a status, and detail of the last host-side error
+ * of the calling thread. */
+const char *odt_status_string(odt_status status);
+const char *odt_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ODTBRAIN_GB300_H */

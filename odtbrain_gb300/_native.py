@@ -1,0 +1,192 @@
+"""ctypes binding of the C ABI in ``include/odtbrain_gb300.h``.
+
+The shared library is built in-tree by ``odtbrain_gb300.build`` and loaded
+from ``odtbrain_gb300/_lib``.  There is no CPU fallback: if the library is
+missing, :func:`lib` raises.
+"""
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+ODT_OK = 0
+ODT_ERR_INVALID_ARGUMENT = 1
+ODT_ERR_UNSUPPORTED = 2
+ODT_ERR_CUDA = 3
+ODT_ERR_OUT_OF_MEMORY = 4
+ODT_ERR_DEVICE_CHECK = 5
+
+ODT_PAD_NONE, ODT_PAD_EDGE, ODT_PAD_RAMP = 0, 1, 2
+ODT_GEOM_Y_AXIS, ODT_GEOM_AFFINE3D = 0, 1
+ODT_INPUT_C64, ODT_INPUT_C128 = 0, 1
+
+# every symbol include/odtbrain_gb300.h declares
+EXPORTED_SYMBOLS = (
+    "odt_bpp3d_plan_create",
+    "odt_bpp3d_workspace_size",
+    "odt_bpp3d_angle_batch",
+    "odt_bpp3d_execute",
+    "odt_bpp3d_execute_timed",
+    "odt_bpp3d_launch_count",
+    "odt_bpp3d_read_status",
+    "odt_bpp3d_plan_destroy",
+    "odt_status_string",
+    "odt_last_error",
+)
+
+
+class OdtError(RuntimeError):
+    """A non-OK status returned by the native library."""
+
+    def __init__(self, status, msg):
+        super().__init__(msg)
+        self.status = status
+
+
+class Bpp3dDesc(ctypes.Structure):
+    _fields_ = [
+        ("num_angles", ctypes.c_int32),
+        ("ny", ctypes.c_int32),
+        ("nx", ctypes.c_int32),
+        ("pad_ny", ctypes.c_int32),
+        ("pad_nx", ctypes.c_int32),
+        ("pad_y_left", ctypes.c_int32),
+        ("pad_x_left", ctypes.c_int32),
+        ("pad_mode", ctypes.c_int32),
+        ("padval_re", ctypes.c_double),
+        ("padval_im", ctypes.c_double),
+        ("intp_order", ctypes.c_int32),
+        ("geometry", ctypes.c_int32),
+        ("onlyreal", ctypes.c_int32),
+        ("input_dtype", ctypes.c_int32),
+        ("filter", ctypes.POINTER(ctypes.c_double)),
+        ("kz_phase", ctypes.POINTER(ctypes.c_double)),
+        ("workspace_limit", ctypes.c_uint64),
+    ]
+
+
+STAGE_NAMES = ("rows_forward", "columns_propagate", "rows_inverse",
+               "rotate")
+
+
+class StageTiming(ctypes.Structure):
+    _fields_ = [
+        ("ms", ctypes.c_double * 4),
+        ("launches", ctypes.c_int64 * 4),
+        ("bytes", ctypes.c_double * 4),
+    ]
+
+    def as_dict(self):
+        return {name: {"ms": self.ms[i], "launches": int(self.launches[i]),
+                       "bytes": self.bytes[i]}
+                for i, name in enumerate(STAGE_NAMES)}
+
+
+_LIB = None
+_LOCK = threading.Lock()
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib():
+    """Load (once) and return the native library; raises if it is absent."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = _build.LIB
+        if not os.path.exists(path):
+            raise RuntimeError(
+                "odtbrain_gb300 CUDA library not built (%s missing); run "
+                "`python -m odtbrain_gb300.build` or "
+                "`python -c 'import __graft_entry__ as g; g.build()'`" % path)
+        L = ctypes.CDLL(path)
+        vp = ctypes.c_void_p
+        L.odt_bpp3d_plan_create.argtypes = [ctypes.POINTER(Bpp3dDesc),
+                                            ctypes.POINTER(vp)]
+        L.odt_bpp3d_workspace_size.argtypes = [
+            vp, ctypes.POINTER(ctypes.c_uint64)]
+        L.odt_bpp3d_angle_batch.argtypes = [vp,
+                                            ctypes.POINTER(ctypes.c_int32)]
+        L.odt_bpp3d_execute.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.odt_bpp3d_execute_timed.argtypes = [vp, vp, vp, vp, vp, vp, vp,
+                                              ctypes.POINTER(StageTiming)]
+        L.odt_bpp3d_launch_count.argtypes = [vp,
+                                             ctypes.POINTER(ctypes.c_int64)]
+        L.odt_bpp3d_read_status.argtypes = [vp, vp]
+        L.odt_bpp3d_plan_destroy.argtypes = [vp]
+        for name in ("odt_bpp3d_plan_create", "odt_bpp3d_workspace_size",
+                     "odt_bpp3d_angle_batch", "odt_bpp3d_execute",
+                     "odt_bpp3d_execute_timed", "odt_bpp3d_launch_count",
+                     "odt_bpp3d_read_status", "odt_bpp3d_plan_destroy"):
+            getattr(L, name).restype = ctypes.c_int
+        L.odt_status_string.argtypes = [ctypes.c_int]
+        L.odt_status_string.restype = ctypes.c_char_p
+        L.odt_last_error.argtypes = []
+        L.odt_last_error.restype = ctypes.c_char_p
+        _LIB = L
+        return L
+
+
+def check(status):
+    """Raise the Python exception the reference would raise for a status."""
+    if status == ODT_OK:
+        return
+    L = lib()
+    detail = L.odt_last_error().decode(errors="replace")
+    text = "%s: %s" % (L.odt_status_string(status).decode(), detail)
+    if status == ODT_ERR_INVALID_ARGUMENT:
+        raise ValueError(text)
+    if status == ODT_ERR_UNSUPPORTED:
+        raise NotImplementedError(text)
+    if status == ODT_ERR_OUT_OF_MEMORY:
+        raise MemoryError(text)
+    raise OdtError(status, text)
+
+
+class Plan:
+    """Owns an ``odt_bpp3d_plan``."""
+
+    def __init__(self, desc):
+        L = lib()
+        handle = ctypes.c_void_p()
+        check(L.odt_bpp3d_plan_create(ctypes.byref(desc),
+                                      ctypes.byref(handle)))
+        self._h = handle
+        ws = ctypes.c_uint64()
+        check(L.odt_bpp3d_workspace_size(self._h, ctypes.byref(ws)))
+        self.workspace_bytes = int(ws.value)
+        b = ctypes.c_int32()
+        check(L.odt_bpp3d_angle_batch(self._h, ctypes.byref(b)))
+        self.angle_batch = int(b.value)
+        n = ctypes.c_int64()
+        check(L.odt_bpp3d_launch_count(self._h, ctypes.byref(n)))
+        self.launches_per_execute = int(n.value)
+
+    def execute(self, sino_ptr, weights_ptr, geometry_ptr, volume_ptr,
+                workspace_ptr, stream_handle):
+        check(lib().odt_bpp3d_execute(self._h, sino_ptr, weights_ptr,
+                                      geometry_ptr, volume_ptr,
+                                      workspace_ptr, stream_handle))
+
+    def execute_timed(self, sino_ptr, weights_ptr, geometry_ptr, volume_ptr,
+                      workspace_ptr, stream_handle):
+        t = StageTiming()
+        check(lib().odt_bpp3d_execute_timed(
+            self._h, sino_ptr, weights_ptr, geometry_ptr, volume_ptr,
+            workspace_ptr, stream_handle, ctypes.byref(t)))
+        return t.as_dict()
+
+    def read_status(self, stream_handle):
+        check(lib().odt_bpp3d_read_status(self._h, stream_handle))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _LIB is not None:
+            _LIB.odt_bpp3d_plan_destroy(h)
+            self._h = None

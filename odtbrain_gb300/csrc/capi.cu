@@ -1,0 +1,523 @@
+// C ABI of odtbrain_gb300 (declared in include/odtbrain_gb300.h).
+//
+// Plan creation turns the FP64 host constants of the reference
+// (odtbrain/_alg3d_bpp.py:317-437; _alg3d_bppt.py:680-820) into the FP32
+// device tables the stage kernels read, and sizes the angle batches.
+// Execution runs, per batch of angles, the filter stages into coefficient
+// slabs and then the resampling/accumulation stage.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/odtbrain_gb300.h"
+#include "odt_internal.cuh"
+
+using odt::FilterTables;
+using odt::RotParams;
+using odt::StageParams;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+odt_status fail(odt_status st, const std::string &msg)
+{
+    g_last_error = msg;
+    return st;
+}
+
+odt_status cuda_fail(cudaError_t e, const char *where)
+{
+    return fail(ODT_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+constexpr uint64_t kDefaultWorkspace = 8ull << 30;    // 8 GiB of slabs etc.
+constexpr uint64_t kPlaneBudget = 64ull << 20;         // column-stage output kept L2-sized
+constexpr size_t kAlign = 256;
+
+size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+// Spline pole and transfer function Bhat(w) of the sampled B-spline
+// (order 2: [1 6 1]/8, order 3: [1 4 1]/6).
+double spline_pole(int order) { return order == 2 ? std::sqrt(8.0) - 3.0 : std::sqrt(3.0) - 2.0; }
+double spline_bhat(int order, double w)
+{
+    return order == 2 ? (6.0 + 2.0 * std::cos(w)) / 8.0 : (4.0 + 2.0 * std::cos(w)) / 6.0;
+}
+
+// Coefficients of the boundary solve for a cropped line of length n: with
+// d0 = u[-1] - u[1] and d1 = u[n] - u[n-2], the homogeneous correction
+// A z^k + B z^(n-1-k) has A = ca*d0 + cb*d1 and B = ca*d1 + cb*d0.
+void boundary_solve(double z, int n, double *ca, double *cb)
+{
+    const double a = z - 1.0 / z;
+    const double b = std::pow(z, n - 2) - std::pow(z, n);
+    const double det = a * a - b * b;
+    *ca = a / det;
+    *cb = -b / det;
+}
+
+double fftfreq_rad(int k, int n)
+{
+    // 2*pi*numpy.fft.fftfreq(n)[k]
+    const int half = (n - 1) / 2;
+    const int m = k <= half ? k : k - n;
+    return 2.0 * M_PI * (double)m / (double)n;
+}
+
+}  // namespace
+
+struct odt_bpp3d_plan {
+    odt_bpp3d_desc d;
+    int nz;
+    int batch;       // angles per batch
+    int jobs;        // (angle, plane) jobs per column/row launch
+    size_t off_rowspec, off_T, off_slab, off_comp, ws_bytes;
+    double bx_ca, bx_cb, by_ca, by_cb;
+    // device tables (one allocation)
+    void *d_tables;
+    FilterTables tab;
+    int *d_status;
+};
+
+namespace {
+
+StageParams stage_params(const odt_bpp3d_plan *p)
+{
+    StageParams P;
+    const odt_bpp3d_desc &d = p->d;
+    P.A = d.num_angles;
+    P.ny = d.ny;
+    P.nx = d.nx;
+    P.nz = p->nz;
+    P.lNy = d.pad_ny;
+    P.lNx = d.pad_nx;
+    P.padyl = d.pad_y_left;
+    P.padxl = d.pad_x_left;
+    P.pad_mode = d.pad_mode;
+    P.padval = make_float2((float)d.padval_re, (float)d.padval_im);
+    P.order = d.intp_order;
+    P.tilted = d.geometry == ODT_GEOM_AFFINE3D;
+    P.in_c128 = d.input_dtype == ODT_INPUT_C128;
+    P.bx_ca = (float)p->bx_ca;
+    P.bx_cb = (float)p->bx_cb;
+    P.by_ca = (float)p->by_ca;
+    P.by_cb = (float)p->by_cb;
+    P.tab = p->tab;
+    P.status = p->d_status;
+    return P;
+}
+
+odt_status validate(const odt_bpp3d_desc *d)
+{
+    if (!d)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "descriptor is NULL");
+    if (d->num_angles < 1 || d->ny < 1 || d->nx < 2)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "need num_angles >= 1, ny >= 1, nx >= 2");
+    if (d->pad_ny < d->ny || d->pad_nx < d->nx || d->pad_y_left < 0 || d->pad_x_left < 0 ||
+        d->pad_y_left + d->ny > d->pad_ny || d->pad_x_left + d->nx > d->pad_nx)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "inconsistent padding geometry");
+    if (d->pad_mode < ODT_PAD_NONE || d->pad_mode > ODT_PAD_RAMP)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "unknown pad_mode");
+    if (d->pad_mode == ODT_PAD_NONE && (d->pad_ny != d->ny || d->pad_nx != d->nx))
+        return fail(ODT_ERR_INVALID_ARGUMENT, "pad_mode NONE needs unpadded sizes");
+    if (d->geometry != ODT_GEOM_Y_AXIS && d->geometry != ODT_GEOM_AFFINE3D)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "unknown geometry");
+    if (d->input_dtype != ODT_INPUT_C64 && d->input_dtype != ODT_INPUT_C128)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "unknown input dtype");
+    if (d->intp_order < 0 || d->intp_order > 5)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "intp_order must be in 0..5");
+    if (d->intp_order > 3)
+        return fail(ODT_ERR_UNSUPPORTED, "spline orders 4 and 5 are not implemented on the GPU");
+    if (d->geometry == ODT_GEOM_AFFINE3D && d->intp_order >= 2 && d->ny < 2)
+        return fail(ODT_ERR_UNSUPPORTED, "3D spline prefilter needs ny >= 2");
+    if (!odt::line_size_supported(d->pad_nx) || !odt::line_size_supported(d->pad_ny))
+        return fail(ODT_ERR_UNSUPPORTED,
+                    "FFT length must be a power of two in [64, 4096] or any length <= 1024");
+    if (!d->filter || !d->kz_phase)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "filter and kz_phase tables are required");
+    return ODT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *odt_status_string(odt_status s)
+{
+    switch (s) {
+    case ODT_OK: return "ok";
+    case ODT_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case ODT_ERR_UNSUPPORTED: return "unsupported";
+    case ODT_ERR_CUDA: return "CUDA error";
+    case ODT_ERR_OUT_OF_MEMORY: return "out of memory";
+    case ODT_ERR_DEVICE_CHECK: return "device-side check failed";
+    }
+    return "unknown status";
+}
+
+const char *odt_last_error(void) { return g_last_error.c_str(); }
+
+odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **out)
+{
+    if (!out)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "plan output pointer is NULL");
+    *out = nullptr;
+    odt_status st = validate(desc);
+    if (st != ODT_OK)
+        return st;
+    odt_bpp3d_plan *p = new (std::nothrow) odt_bpp3d_plan();
+    if (!p)
+        return fail(ODT_ERR_OUT_OF_MEMORY, "host allocation failed");
+    p->d = *desc;
+    p->d.filter = nullptr;
+    p->d.kz_phase = nullptr;
+    const odt_bpp3d_desc &d = p->d;
+    const int lNy = d.pad_ny, lNx = d.pad_nx, nz = d.nx;
+    p->nz = nz;
+    const int order = d.intp_order;
+    const bool pf = order >= 2;
+    const bool tilted = d.geometry == ODT_GEOM_AFFINE3D;
+    const size_t K = (size_t)lNy * lNx;
+
+    // ---- FP64 host tables -> FP32 device tables
+    std::vector<float2> G(K), W(K), S(K), AL(K), BE(K), twx(lNx), twy(lNy);
+    std::vector<float> zp(odt::ZPOW_N, 0.f);
+    const double z1 = pf ? spline_pole(order) : 0.0;
+    double za_ca = 0, za_cb = 0;
+    if (pf) {
+        boundary_solve(z1, nz, &za_ca, &za_cb);
+        boundary_solve(z1, d.nx, &p->bx_ca, &p->bx_cb);
+        if (d.ny >= 2)
+            boundary_solve(z1, d.ny, &p->by_ca, &p->by_cb);
+        double zz = 1.0;
+        for (int m = 0; m < odt::ZPOW_N; ++m) {
+            zp[m] = (float)zz;
+            zz *= z1;
+        }
+    }
+    const double z_first = 0.0 - 0.5 * nz, z_last = (double)(nz - 1) - 0.5 * nz;
+    for (int ky = 0; ky < lNy; ++ky) {
+        const double iby = (pf && tilted) ? 1.0 / spline_bhat(order, fftfreq_rad(ky, lNy)) : 1.0;
+        for (int kx = 0; kx < lNx; ++kx) {
+            const size_t k = (size_t)ky * lNx + kx;
+            const double ibx = pf ? 1.0 / spline_bhat(order, fftfreq_rad(kx, lNx)) : 1.0;
+            const double w = desc->kz_phase[k];
+            const double ibw = pf ? 1.0 / spline_bhat(order, w) : 1.0;
+            const double sc = ibx * iby * ibw;
+            G[k] = make_float2((float)(desc->filter[2 * k] * sc), (float)(desc->filter[2 * k + 1] * sc));
+            const float whi = (float)w;
+            W[k] = make_float2(whi, (float)(w - (double)whi));
+            S[k] = make_float2((float)std::cos(w), (float)std::sin(w));
+            if (pf) {
+                const std::complex<double> I(0.0, 1.0);
+                const std::complex<double> e0 = std::exp(I * (w * z_first));
+                const std::complex<double> en = std::exp(I * (w * z_last));
+                const std::complex<double> d0 = e0 * (-2.0 * std::sin(w)) * I;
+                const std::complex<double> d1 = en * (2.0 * std::sin(w)) * I;
+                const std::complex<double> al = za_ca * d0 + za_cb * d1;
+                const std::complex<double> be = za_ca * d1 + za_cb * d0;
+                AL[k] = make_float2((float)al.real(), (float)al.imag());
+                BE[k] = make_float2((float)be.real(), (float)be.imag());
+            } else {
+                AL[k] = make_float2(0.f, 0.f);
+                BE[k] = make_float2(0.f, 0.f);
+            }
+        }
+    }
+    for (int m = 0; m < lNx; ++m)
+        twx[m] = make_float2((float)std::cos(-2.0 * M_PI * m / lNx), (float)std::sin(-2.0 * M_PI * m / lNx));
+    for (int m = 0; m < lNy; ++m)
+        twy[m] = make_float2((float)std::cos(-2.0 * M_PI * m / lNy), (float)std::sin(-2.0 * M_PI * m / lNy));
+
+    size_t o = 0;
+    const size_t oG = o; o = align_up(o + K * 8);
+    const size_t oW = o; o = align_up(o + K * 8);
+    const size_t oS = o; o = align_up(o + K * 8);
+    const size_t oA = o; o = align_up(o + K * 8);
+    const size_t oB = o; o = align_up(o + K * 8);
+    const size_t oTx = o; o = align_up(o + (size_t)lNx * 8);
+    const size_t oTy = o; o = align_up(o + (size_t)lNy * 8);
+    const size_t oZ = o; o = align_up(o + odt::ZPOW_N * 4);
+    const size_t oSt = o; o = align_up(o + 16);
+    cudaError_t e = cudaMalloc(&p->d_tables, o);
+    if (e != cudaSuccess) {
+        delete p;
+        return e == cudaErrorMemoryAllocation ? fail(ODT_ERR_OUT_OF_MEMORY, "cudaMalloc of plan tables failed")
+                                              : cuda_fail(e, "cudaMalloc");
+    }
+    char *base = (char *)p->d_tables;
+    struct Up { size_t off; const void *src; size_t n; } ups[] = {
+        {oG, G.data(), K * 8}, {oW, W.data(), K * 8}, {oS, S.data(), K * 8}, {oA, AL.data(), K * 8},
+        {oB, BE.data(), K * 8}, {oTx, twx.data(), (size_t)lNx * 8}, {oTy, twy.data(), (size_t)lNy * 8},
+        {oZ, zp.data(), odt::ZPOW_N * 4}};
+    for (const Up &u : ups) {
+        e = cudaMemcpy(base + u.off, u.src, u.n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(p->d_tables);
+            delete p;
+            return cuda_fail(e, "cudaMemcpy of plan tables");
+        }
+    }
+    e = cudaMemset(base + oSt, 0, 16);
+    if (e != cudaSuccess) {
+        cudaFree(p->d_tables);
+        delete p;
+        return cuda_fail(e, "cudaMemset");
+    }
+    p->tab.G = (const float2 *)(base + oG);
+    p->tab.wsplit = (const float2 *)(base + oW);
+    p->tab.step = (const float2 *)(base + oS);
+    p->tab.alpha = (const float2 *)(base + oA);
+    p->tab.beta = (const float2 *)(base + oB);
+    p->tab.twx = (const float2 *)(base + oTx);
+    p->tab.twy = (const float2 *)(base + oTy);
+    p->tab.zpow = (const float *)(base + oZ);
+    p->d_status = (int *)(base + oSt);
+
+    // ---- batching
+    const size_t plane_row_bytes = (size_t)d.ny * lNx * 8;           // one job's column-stage output
+    const size_t slab_bytes = (size_t)nz * d.ny * d.nx * 8;          // one angle's coefficient slab
+    const size_t rowspec_bytes = (size_t)lNy * lNx * 8;              // one angle's row spectra
+    const size_t vol_bytes = (size_t)nz * d.ny * d.nx * 8;           // compensation buffer
+    const uint64_t limit = d.workspace_limit ? d.workspace_limit : kDefaultWorkspace;
+    size_t jobs_cap = std::max<size_t>(16, kPlaneBudget / plane_row_bytes);
+    long long batch = (long long)((limit > vol_bytes + jobs_cap * plane_row_bytes)
+                                      ? (limit - vol_bytes - jobs_cap * plane_row_bytes) / (slab_bytes + rowspec_bytes)
+                                      : 1);
+    batch = std::max<long long>(1, std::min<long long>(batch, d.num_angles));
+    p->batch = (int)batch;
+    const size_t total_jobs = (size_t)batch * nz;
+    size_t jobs = std::min(total_jobs, jobs_cap);
+    if (jobs >= 16)
+        jobs = jobs / 16 * 16;
+    p->jobs = (int)jobs;
+    const int nbatches = (d.num_angles + p->batch - 1) / p->batch;
+    size_t w = 0;
+    p->off_rowspec = w; w = align_up(w + (size_t)batch * rowspec_bytes);
+    p->off_T = w; w = align_up(w + jobs * plane_row_bytes);
+    p->off_slab = w; w = align_up(w + (size_t)batch * slab_bytes);
+    p->off_comp = w; w = align_up(w + (nbatches > 1 ? vol_bytes : 0));
+    p->ws_bytes = w;
+
+    StageParams P = stage_params(p);
+    e = odt::configure_kernels(P);
+    if (e != cudaSuccess) {
+        cudaFree(p->d_tables);
+        delete p;
+        return cuda_fail(e, "kernel configuration");
+    }
+    *out = p;
+    return ODT_OK;
+}
+
+odt_status odt_bpp3d_workspace_size(const odt_bpp3d_plan *plan, uint64_t *bytes)
+{
+    if (!plan || !bytes)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *bytes = plan->ws_bytes;
+    return ODT_OK;
+}
+
+odt_status odt_bpp3d_angle_batch(const odt_bpp3d_plan *plan, int32_t *batch)
+{
+    if (!plan || !batch)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *batch = plan->batch;
+    return ODT_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Event pair around one launch, summed into a stage slot after the run.
+struct LaunchTimer {
+    odt_stage_timing *t;
+    cudaStream_t s;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev;
+    explicit LaunchTimer(odt_stage_timing *timing, cudaStream_t stream) : t(timing), s(stream) {}
+    void begin(int stage)
+    {
+        if (!t)
+            return;
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, s);
+        ev.push_back({stage, {a, b}});
+    }
+    void end(double bytes)
+    {
+        if (!t)
+            return;
+        cudaEventRecord(ev.back().second.second, s);
+        t->launches[ev.back().first] += 1;
+        t->bytes[ev.back().first] += bytes;
+    }
+    cudaError_t finish()
+    {
+        if (!t)
+            return cudaSuccess;
+        cudaError_t e = cudaStreamSynchronize(s);
+        for (auto &x : ev) {
+            float ms = 0.f;
+            if (e == cudaSuccess)
+                e = cudaEventElapsedTime(&ms, x.second.first, x.second.second);
+            t->ms[x.first] += ms;
+            cudaEventDestroy(x.second.first);
+            cudaEventDestroy(x.second.second);
+        }
+        ev.clear();
+        return e;
+    }
+};
+
+odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *weights, const double *geometry,
+                    void *volume, void *workspace, void *stream, odt_stage_timing *timing)
+{
+    if (!plan || !sino || !geometry || !volume || (!workspace && plan->ws_bytes))
+        return fail(ODT_ERR_INVALID_ARGUMENT, "NULL pointer argument");
+    if (((uintptr_t)workspace % kAlign) != 0)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    const odt_bpp3d_desc &d = plan->d;
+    cudaStream_t s = (cudaStream_t)stream;
+    StageParams P = stage_params(plan);
+    char *ws = (char *)workspace;
+    float2 *rowspec = (float2 *)(ws + plan->off_rowspec);
+    float2 *T = (float2 *)(ws + plan->off_T);
+    float2 *slab = (float2 *)(ws + plan->off_slab);
+    float2 *comp = (float2 *)(ws + plan->off_comp);
+    const size_t in_elem = d.input_dtype == ODT_INPUT_C128 ? 16 : 8;
+    const int geo_stride = d.geometry == ODT_GEOM_AFFINE3D ? 12 : 6;
+    const int nbatches = (d.num_angles + plan->batch - 1) / plan->batch;
+    const double plane_in = (double)d.ny * d.nx, spec = (double)d.pad_ny * d.pad_nx;
+    const double vol = (double)plan->nz * d.ny * d.nx;
+    const double out_elem = d.onlyreal ? 4.0 : 8.0;
+    if (timing)
+        std::memset(timing, 0, sizeof(*timing));
+    LaunchTimer lt(timing, s);
+    cudaError_t e;
+    for (int b = 0; b < nbatches; ++b) {
+        const int a0 = b * plan->batch;
+        const int nb = std::min(plan->batch, d.num_angles - a0);
+        const char *sino_b = (const char *)sino + (size_t)a0 * d.ny * d.nx * in_elem;
+        lt.begin(ODT_STAGE_ROWS_FORWARD);
+        e = odt::launch_rows_forward(P, sino_b, weights ? weights + a0 : nullptr, nb, rowspec, s);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "rows_forward launch");
+        lt.end(nb * (plane_in * in_elem + spec * 8.0));
+        const int total = nb * plan->nz;
+        for (int q0 = 0; q0 < total; q0 += plan->jobs) {
+            const int qn = std::min(plan->jobs, total - q0);
+            lt.begin(ODT_STAGE_COLUMNS_PROPAGATE);
+            e = odt::launch_columns_propagate(P, rowspec, T, q0, qn, s);
+            if (e != cudaSuccess)
+                return cuda_fail(e, "columns_propagate launch");
+            lt.end((double)qn / plan->nz * spec * 8.0);
+            lt.begin(ODT_STAGE_ROWS_INVERSE);
+            e = odt::launch_rows_inverse(P, T, slab, q0, qn, s);
+            if (e != cudaSuccess)
+                return cuda_fail(e, "rows_inverse launch");
+            lt.end((double)qn * plane_in * 8.0);
+        }
+        RotParams R;
+        R.ny = d.ny;
+        R.nx = d.nx;
+        R.nz = plan->nz;
+        R.nbatch_angles = nb;
+        R.first_pass = b == 0;
+        R.last_pass = b == nbatches - 1;
+        R.onlyreal = d.onlyreal;
+        R.status = plan->d_status;
+        lt.begin(ODT_STAGE_ROTATE);
+        e = odt::launch_rotate(R, d.intp_order, d.geometry == ODT_GEOM_AFFINE3D, slab,
+                               geometry + (size_t)a0 * geo_stride, volume, comp, s);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "rotate launch");
+        double rb = nb * vol * 8.0 + vol * out_elem;
+        if (!R.first_pass)
+            rb += vol * (out_elem + 8.0);
+        if (!R.last_pass)
+            rb += vol * 8.0;
+        lt.end(rb);
+    }
+    e = lt.finish();
+    if (e != cudaSuccess)
+        return cuda_fail(e, "timing");
+    return ODT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+odt_status odt_bpp3d_execute(const odt_bpp3d_plan *plan, const void *sino, const double *weights,
+                             const double *geometry, void *volume, void *workspace, void *stream)
+{
+    return run_plan(plan, sino, weights, geometry, volume, workspace, stream, nullptr);
+}
+
+odt_status odt_bpp3d_execute_timed(const odt_bpp3d_plan *plan, const void *sino, const double *weights,
+                                   const double *geometry, void *volume, void *workspace, void *stream,
+                                   odt_stage_timing *timing)
+{
+    if (!timing)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "timing is NULL");
+    return run_plan(plan, sino, weights, geometry, volume, workspace, stream, timing);
+}
+
+odt_status odt_bpp3d_launch_count(const odt_bpp3d_plan *plan, int64_t *launches)
+{
+    if (!plan || !launches)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "NULL argument");
+    const int A = plan->d.num_angles;
+    const int nbatches = (A + plan->batch - 1) / plan->batch;
+    int64_t n = 0;
+    for (int b = 0; b < nbatches; ++b) {
+        const int nb = std::min(plan->batch, A - b * plan->batch);
+        const int64_t total = (int64_t)nb * plan->nz;
+        n += 2 + 2 * ((total + plan->jobs - 1) / plan->jobs);
+    }
+    *launches = n;
+    return ODT_OK;
+}
+
+odt_status odt_bpp3d_read_status(const odt_bpp3d_plan *plan, void *stream)
+{
+    if (!plan)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "NULL plan");
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, plan->d_status, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "status read");
+    if (h != 0) {
+        cudaMemsetAsync(plan->d_status, 0, sizeof(int), (cudaStream_t)stream);
+        char buf[96];
+        snprintf(buf, sizeof buf, "device check failed (bits 0x%x)", h);
+        return fail(ODT_ERR_DEVICE_CHECK, buf);
+    }
+    return ODT_OK;
+}
+
+odt_status odt_bpp3d_plan_destroy(odt_bpp3d_plan *plan)
+{
+    if (!plan)
+        return ODT_OK;
+    cudaError_t e = cudaFree(plan->d_tables);
+    delete plan;
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaFree");
+    return ODT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,200 @@
+// Line transforms shared by the filter stages of the 3D backpropagation.
+//
+// A "line" is one 1D complex transform (one padded sinogram row, one
+// spectrum column, one propagated row).  A group of TPL threads owns a line;
+// thread j of the group holds the elements at positions j + r*TPL
+// (r < SLOTS) in registers, both before and after the transform, so stage
+// kernels can fuse loads, pointwise filters and cropped stores around it.
+//
+// Pow2Line<N>: radix-8 Stockham autosort FFT (Govindaraju et al., "High
+//   performance discrete Fourier transforms on graphics processors", SC'08),
+//   with a final radix-4 or radix-2 pass for N = 8^a * {2, 4}.  Passes
+//   exchange through two shared-memory buffers used alternately, so each
+//   exchange needs a single barrier.
+// GenericLine: O(N^2) direct DFT for the sizes that are not powers of two
+//   (only reachable with padding=(False, False)); N <= 1024.
+//
+// Sign convention: DIR = -1 is the forward transform exp(-2 pi i n k / N),
+// DIR = +1 the unnormalised backward transform, like FFTW's execute().
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace odt {
+
+__device__ __forceinline__ float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c)  // a*b + c
+{
+    return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+template <int DIR>
+__device__ __forceinline__ float2 mul_i(float2 a)  // a * (DIR * i)
+{
+    return DIR > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+// tw holds exp(-2 pi i m / N); the backward transform uses its conjugate.
+template <int DIR>
+__device__ __forceinline__ float2 twid(const float2 *tw, int m)
+{
+    float2 t = tw[m];
+    return DIR > 0 ? make_float2(t.x, -t.y) : t;
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft2(float2 &a, float2 &b)
+{
+    float2 t = a;
+    a = t + b;
+    b = t - b;
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft4(float2 &x0, float2 &x1, float2 &x2, float2 &x3)
+{
+    float2 a0 = x0 + x2, a1 = x0 - x2, a2 = x1 + x3, a3 = mul_i<DIR>(x1 - x3);
+    x0 = a0 + a2;
+    x2 = a0 - a2;
+    x1 = a1 + a3;
+    x3 = a1 - a3;
+}
+
+template <int DIR>
+__device__ __forceinline__ void dft8(float2 *x)
+{
+    float2 e0 = x[0], e1 = x[2], e2 = x[4], e3 = x[6];
+    float2 o0 = x[1], o1 = x[3], o2 = x[5], o3 = x[7];
+    dft4<DIR>(e0, e1, e2, e3);
+    dft4<DIR>(o0, o1, o2, o3);
+    const float r = 0.70710678118654752440f;
+    // o1 *= (1 + DIR i)/sqrt2 ; o2 *= DIR i ; o3 *= (-1 + DIR i)/sqrt2
+    o1 = make_float2((o1.x - DIR * o1.y) * r, (o1.y + DIR * o1.x) * r);
+    o2 = mul_i<DIR>(o2);
+    o3 = make_float2((-o3.x - DIR * o3.y) * r, (-o3.y + DIR * o3.x) * r);
+    x[0] = e0 + o0;
+    x[4] = e0 - o0;
+    x[1] = e1 + o1;
+    x[5] = e1 - o1;
+    x[2] = e2 + o2;
+    x[6] = e2 - o2;
+    x[3] = e3 + o3;
+    x[7] = e3 - o3;
+}
+
+constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+constexpr int ipow8(int k) { return k == 0 ? 1 : 8 * ipow8(k - 1); }
+
+// Power-of-two line, 64 <= N <= 4096.
+template <int N_>
+struct Pow2Line {
+    static constexpr int N = N_;
+    static constexpr int TPL = N / 8;
+    static constexpr int SLOTS = 8;
+    static constexpr int P8 = ilog2c(N) / 3;
+    static constexpr int TAIL = N / ipow8(P8);  // 1, 2 or 4
+    int n;  // == N, kept for a uniform interface with GenericLine
+    __device__ __forceinline__ int size() const { return N; }
+
+    // v: positions j + r*TPL in, same positions out.  `line[0/1]` point at
+    // element 0 of this line in the two exchange buffers; `es` is the
+    // element stride.  `flip` alternates the buffers across exchanges.
+    template <int DIR>
+    __device__ __forceinline__ void run(float2 (&v)[8], int j, float2 *line0, float2 *line1, int es,
+                                        const float2 *tw, int &flip) const
+    {
+        int Ns = 1;
+#pragma unroll
+        for (int pass = 0; pass < P8; ++pass) {
+            if (pass > 0) {
+                const int jm = j & (Ns - 1);
+                const int stp = jm * (N / (Ns * 8));
+#pragma unroll
+                for (int r = 1; r < 8; ++r)
+                    v[r] = cmul(v[r], twid<DIR>(tw, r * stp));
+            }
+            dft8<DIR>(v);
+            if (pass == P8 - 1 && TAIL == 1)
+                break;
+            float2 *b = flip ? line1 : line0;
+            flip ^= 1;
+            const int idxD = (j / Ns) * Ns * 8 + (j & (Ns - 1));
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                b[(idxD + r * Ns) * es] = v[r];
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                v[r] = b[(j + r * TPL) * es];
+            Ns *= 8;
+        }
+        if (TAIL == 4) {
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+                const int jj = j + g * TPL;
+                float2 x0 = v[g], x1 = v[g + 2], x2 = v[g + 4], x3 = v[g + 6];
+                x1 = cmul(x1, twid<DIR>(tw, jj));
+                x2 = cmul(x2, twid<DIR>(tw, 2 * jj));
+                x3 = cmul(x3, twid<DIR>(tw, 3 * jj));
+                dft4<DIR>(x0, x1, x2, x3);
+                v[g] = x0;
+                v[g + 2] = x1;
+                v[g + 4] = x2;
+                v[g + 6] = x3;
+            }
+        } else if (TAIL == 2) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int jj = j + q * TPL;
+                float2 b = cmul(v[q + 4], twid<DIR>(tw, jj));
+                float2 a = v[q];
+                v[q] = a + b;
+                v[q + 4] = a - b;
+            }
+        }
+    }
+};
+
+// Any N <= TPL*SLOTS: direct DFT through shared memory.
+struct GenericLine {
+    static constexpr int TPL = 64;
+    static constexpr int SLOTS = 16;
+    int n;
+    __device__ __forceinline__ int size() const { return n; }
+
+    template <int DIR>
+    __device__ __forceinline__ void run(float2 (&v)[16], int j, float2 *line0, float2 *line1, int es,
+                                        const float2 *tw, int &flip) const
+    {
+        float2 *b = flip ? line1 : line0;
+        flip ^= 1;
+#pragma unroll
+        for (int r = 0; r < SLOTS; ++r) {
+            const int k = j + r * TPL;
+            if (k < n)
+                b[k * es] = v[r];
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int r = 0; r < SLOTS; ++r) {
+            const int k = j + r * TPL;
+            if (k >= n)
+                break;
+            float2 acc = make_float2(0.f, 0.f);
+            int m = 0;
+            for (int i = 0; i < n; ++i) {
+                acc = cfma(b[i * es], twid<DIR>(tw, m), acc);
+                m += k;
+                if (m >= n)
+                    m -= n;
+            }
+            v[r] = acc;
+        }
+    }
+};
+
+}  // namespace odt

@@ -1,0 +1,65 @@
+// Internal declarations shared by the stage kernels, the rotation kernels
+// and the C-ABI layer.  Nothing here is part of the public interface.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace odt {
+
+// Error bits recorded by kernels in the plan's device status word.
+enum : int {
+    DEVCHK_BOX_OVERFLOW = 1,   // a rotation footprint did not fit its tile
+    DEVCHK_BAD_CONFIG = 2      // a kernel was launched with an unsupported shape
+};
+
+// Number of boundary-correction terms of the B-spline prefilter that are
+// applied; the pole satisfies |z|^24 < 2e-14, below FP32 resolution.
+constexpr int ZPOW_N = 24;
+
+struct FilterTables {
+    const float2 *G;      // [lNy*lNx] filter * prefilter particular factors
+    const float2 *wsplit; // [lNy*lNx] propagator phase km*(M-1): (hi, lo)
+    const float2 *step;   // [lNy*lNx] exp(i*km*(M-1))
+    const float2 *alpha;  // [lNy*lNx] z-prefilter boundary term at p = 0
+    const float2 *beta;   // [lNy*lNx] z-prefilter boundary term at p = nz-1
+    const float2 *twx;    // [lNx] exp(-2 pi i m / lNx)
+    const float2 *twy;    // [lNy] exp(-2 pi i m / lNy)
+    const float *zpow;    // [ZPOW_N] pole^m
+};
+
+struct StageParams {
+    int A, ny, nx, nz, lNy, lNx, padyl, padxl;
+    int pad_mode;
+    float2 padval;
+    int order;        // spline order; >= 2 means the prefilter is folded in
+    int tilted;       // 1: slabs for the 3D affine path ([a][z][y][x] and a
+                      //    y-prefilter); 0: y-axis path ([a][y][z][x])
+    int in_c128;      // input sinogram is complex128
+    float bx_ca, bx_cb;  // x-prefilter boundary solve (n = nx)
+    float by_ca, by_cb;  // y-prefilter boundary solve (n = ny)
+    FilterTables tab;
+    int *status;
+};
+
+struct RotParams {
+    int ny, nx, nz;
+    int nbatch_angles;
+    int first_pass;   // this launch starts the sum (overwrite)
+    int last_pass;    // this launch ends the sum (drop the compensation)
+    int onlyreal;
+    int *status;
+};
+
+// Launchers (stream-ordered; return cudaGetLastError()).
+cudaError_t launch_rows_forward(const StageParams &P, const void *sino_batch, const double *weights_batch,
+                                int nb, float2 *rowspec, cudaStream_t s);
+cudaError_t launch_columns_propagate(const StageParams &P, const float2 *rowspec, float2 *T, int q0, int qn,
+                                     cudaStream_t s);
+cudaError_t launch_rows_inverse(const StageParams &P, const float2 *T, float2 *slab, int q0, int qn,
+                                cudaStream_t s);
+cudaError_t launch_rotate(const RotParams &R, int order, int tilted, const float2 *slab, const double *geo,
+                          void *volume, float2 *comp, cudaStream_t s);
+cudaError_t configure_kernels(const StageParams &P);
+bool line_size_supported(int n);
+
+}  // namespace odt

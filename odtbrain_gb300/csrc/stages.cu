@@ -1,0 +1,478 @@
+// Filter stages (a) and (b) of the 3D backpropagation on sm_103a.
+//
+// Reference loop body (odtbrain/_alg3d_bpp.py:492-528, _alg3d_bppt.py:
+// 865-898), per angle:
+//   pad -> forward 2D FFT -> *prefactor/(lNx*lNy) -> for every z plane p:
+//   *exp(i km (M-1) z_p) -> unnormalised backward 2D FFT -> crop.
+//
+// GB300 decomposition (three kernels, all lines in registers):
+//   rows_forward       padded+weighted rows, forward FFT along x
+//   columns_propagate  forward FFT along y, filter multiply, then for a run
+//                      of z planes: propagator (exact anchor + complex
+//                      recurrence), backward FFT along y, crop in y
+//   rows_inverse       backward FFT along x, crop in x -> coefficient slab
+//
+// The B-spline prefilter that scipy.ndimage applies before resampling
+// (mirror boundaries, along z and x of every plane; along all three axes on
+// the tilted path) is folded into these stages exactly: each Fourier
+// component exp(i k n) of a cropped line has the prefiltered form
+// exp(i k n)/Bhat(k) + A z^n + B z^(N-1-n) (z the spline pole, Bhat the
+// sampled B-spline's transfer function), where A and B follow from the two
+// mirror conditions.  So the spectrum is divided by Bhat along every
+// prefiltered axis (folded into the filter table G), z gets per-frequency
+// boundary terms (alpha, beta tables), and x (and y) get per-line boundary
+// terms computed from four samples just outside the crop.
+#include <type_traits>
+
+#include "odt_fft.cuh"
+#include "odt_internal.cuh"
+
+namespace odt {
+
+// exp(i * w * z) with w held as (hi, lo) floats and z a small half-integer:
+// exact product hi*z via FMA, Cody-Waite reduction by 2*pi, then sincosf.
+__device__ __forceinline__ float2 expi_phase(float2 w, float z)
+{
+    const float ph = w.x * z;
+    const float err = fmaf(w.x, z, -ph);
+    const float lo = fmaf(w.y, z, err);
+    const float k = rintf(ph * 0.15915494309189535f);
+    float r = fmaf(-k, 6.28125f, ph);
+    r = fmaf(-k, 1.9353071795864769253e-3f, r);
+    r += lo;
+    float s, c;
+    sincosf(r, &s, &c);
+    return make_float2(c, s);
+}
+
+__device__ __forceinline__ float2 load_sino(const void *sino, int in_c128, size_t idx, double w)
+{
+    if (in_c128) {
+        const double2 v = reinterpret_cast<const double2 *>(sino)[idx];
+        return make_float2((float)(v.x * w), (float)(v.y * w));
+    }
+    const float2 v = reinterpret_cast<const float2 *>(sino)[idx];
+    const float wf = (float)w;
+    return make_float2(v.x * wf, v.y * wf);
+}
+
+// np.pad linear_ramp value at ramp position i of `width` (i = 0 is the
+// outer edge): end + (edge - end) * i / width  (numpy linspace, endpoint
+// False).
+__device__ __forceinline__ float2 ramp(float2 edge, float2 end, int i, int width)
+{
+    const float t = (float)i / (float)width;
+    return make_float2(fmaf(edge.x - end.x, t, end.x), fmaf(edge.y - end.y, t, end.y));
+}
+
+// Padded, weighted sample (y, x) of the padded plane of angle row `arow`
+// (odtbrain/_alg3d_bpp.py:493-506: np.pad pads y first, then x).
+__device__ float2 padded_sample(const StageParams &P, const void *sino, size_t arow, double w, int y, int x)
+{
+    const int ny = P.ny, nx = P.nx;
+    if (P.pad_mode == 0)
+        return load_sino(sino, P.in_c128, arow + (size_t)y * nx + x, w);
+    const int ys = y - P.padyl, xs = x - P.padxl;
+    if (P.pad_mode == 1) {
+        const int yc = min(max(ys, 0), ny - 1), xc = min(max(xs, 0), nx - 1);
+        return load_sino(sino, P.in_c128, arow + (size_t)yc * nx + xc, w);
+    }
+    const int padyr = P.lNy - ny - P.padyl, padxr = P.lNx - nx - P.padxl;
+    auto colval = [&](int xc) -> float2 {
+        if (ys >= 0 && ys < ny)
+            return load_sino(sino, P.in_c128, arow + (size_t)ys * nx + xc, w);
+        if (ys < 0)
+            return ramp(load_sino(sino, P.in_c128, arow + xc, w), P.padval, y, P.padyl);
+        const int jdx = ys - ny;
+        return ramp(load_sino(sino, P.in_c128, arow + (size_t)(ny - 1) * nx + xc, w), P.padval,
+                    padyr - 1 - jdx, padyr);
+    };
+    if (xs >= 0 && xs < nx)
+        return colval(xs);
+    if (xs < 0)
+        return ramp(colval(0), P.padval, x, P.padxl);
+    return ramp(colval(nx - 1), P.padval, padxr - 1 - (xs - nx), padxr);
+}
+
+template <class L>
+__device__ __forceinline__ void copy_twiddles(float2 *dst, const float2 *src, int n)
+{
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        dst[i] = src[i];
+}
+
+// ---------------------------------------------------------------------------
+// (a) rows: pad + weight + forward FFT along x.
+// rowspec[a][y][kx], a in the batch, y over the padded height.
+template <class L, int LPC>
+__global__ void __launch_bounds__(LPC * L::TPL) k_rows_forward(StageParams P, L line, const void *sino,
+                                                               const double *weights, int nb, float2 *rowspec)
+{
+    extern __shared__ float2 smem[];
+    const int n = line.size();
+    float2 *buf0 = smem, *buf1 = smem + LPC * n, *tw = smem + 2 * LPC * n;
+    copy_twiddles<L>(tw, P.tab.twx, n);
+    const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
+    const long long lid = (long long)blockIdx.x * LPC + l;
+    const long long nlines = (long long)nb * P.lNy;
+    const bool valid = lid < nlines;
+    const int a = valid ? (int)(lid / P.lNy) : 0;
+    const int y = valid ? (int)(lid % P.lNy) : 0;
+    const double w = weights ? weights[a] : 1.0;
+    const size_t arow = (size_t)a * P.ny * P.nx;
+    float2 v[L::SLOTS];
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int x = j + r * L::TPL;
+        v[r] = (valid && x < n) ? padded_sample(P, sino, arow, w, y, x) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    int flip = 0;
+    line.template run<-1>(v, j, buf0 + l * n, buf1 + l * n, 1, tw, flip);
+    if (!valid)
+        return;
+    float2 *dst = rowspec + (size_t)lid * n;
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int x = j + r * L::TPL;
+        if (x < n)
+            dst[x] = v[r];
+    }
+}
+
+// Select v[pos / TPL] of the thread holding position `pos` without dynamic
+// register indexing; returns true when this thread holds it.
+template <class L>
+__device__ __forceinline__ bool held(const float2 (&v)[L::SLOTS], int j, int pos, float2 &out)
+{
+    if (pos % L::TPL != j)
+        return false;
+    const int rr = pos / L::TPL;
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r)
+        if (r == rr)
+            out = v[r];
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// (b1) columns: forward FFT along y, filter, then for z planes p of jobs
+// q in [q0, q0+qn) (q = a*nz + p): propagator, backward FFT along y, crop.
+// T[(q-q0)][y][kx], y over the cropped height.
+template <class L, int KX>
+__global__ void __launch_bounds__(KX * L::TPL) k_columns_propagate(StageParams P, L line, const float2 *rowspec,
+                                                                   float2 *T, int q0, int qn, int ppc)
+{
+    extern __shared__ float2 smem[];
+    const int n = line.size();  // lNy
+    float2 *buf0 = smem, *buf1 = smem + KX * n, *tw = smem + 2 * KX * n;
+    float2 *edge = tw + n;  // [KX][4]
+    copy_twiddles<L>(tw, P.tab.twy, n);
+    const int c = threadIdx.x % KX, j = threadIdx.x / KX;
+    const int kx = blockIdx.x * KX + c;
+    const bool colok = kx < P.lNx;
+    const int lNx = P.lNx, nz = P.nz, ny = P.ny, padyl = P.padyl;
+    const int qb = q0 + blockIdx.y * ppc;
+    const int qe = min(q0 + qn, qb + ppc);
+    const bool pf = P.order >= 2;
+    const bool yfix = pf && P.tilted;
+    // y-prefilter edge positions (u at y0-1, y0+1, y1-1, y1+1)
+    const int e0 = (padyl - 1 + n) % n, e1 = (padyl + 1) % n;
+    const int e2 = (padyl + ny - 2 + n) % n, e3 = (padyl + ny) % n;
+    __syncthreads();
+
+    float2 Gs[L::SLOTS], E[L::SLOTS], st[L::SLOTS];
+    int flip = 0;
+    int cur_a = -1;
+    for (int q = qb; q < qe; ++q) {
+        const int a = q / nz, p = q % nz;
+        const float zp = (float)p - 0.5f * (float)nz;
+        if (a != cur_a) {
+            float2 v[L::SLOTS];
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int ky = j + r * L::TPL;
+                v[r] = (colok && ky < n) ? rowspec[((size_t)a * n + ky) * lNx + kx] : make_float2(0.f, 0.f);
+            }
+            line.template run<-1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int ky = j + r * L::TPL;
+                if (colok && ky < n) {
+                    const size_t k = (size_t)ky * lNx + kx;
+                    Gs[r] = cmul(v[r], P.tab.G[k]);
+                    E[r] = expi_phase(P.tab.wsplit[k], zp);
+                    st[r] = P.tab.step[k];
+                } else {
+                    Gs[r] = make_float2(0.f, 0.f);
+                    E[r] = make_float2(0.f, 0.f);
+                    st[r] = make_float2(0.f, 0.f);
+                }
+            }
+            cur_a = a;
+        }
+        float2 v[L::SLOTS];
+        const bool lowb = pf && p < ZPOW_N;
+        const bool highb = pf && (nz - 1 - p) < ZPOW_N;
+        const float zl = lowb ? P.tab.zpow[p] : 0.f;
+        const float zh = highb ? P.tab.zpow[nz - 1 - p] : 0.f;
+#pragma unroll
+        for (int r = 0; r < L::SLOTS; ++r) {
+            float2 e = E[r];
+            if (lowb || highb) {
+                const int ky = j + r * L::TPL;
+                if (colok && ky < n) {
+                    const size_t k = (size_t)ky * lNx + kx;
+                    if (lowb) {
+                        const float2 al = P.tab.alpha[k];
+                        e = make_float2(fmaf(al.x, zl, e.x), fmaf(al.y, zl, e.y));
+                    }
+                    if (highb) {
+                        const float2 be = P.tab.beta[k];
+                        e = make_float2(fmaf(be.x, zh, e.x), fmaf(be.y, zh, e.y));
+                    }
+                }
+            }
+            v[r] = cmul(Gs[r], e);
+            E[r] = cmul(E[r], st[r]);
+        }
+        line.template run<1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+        float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
+        if (yfix) {
+            float2 t;
+            if (held<L>(v, j, e0, t)) edge[c * 4 + 0] = t;
+            if (held<L>(v, j, e1, t)) edge[c * 4 + 1] = t;
+            if (held<L>(v, j, e2, t)) edge[c * 4 + 2] = t;
+            if (held<L>(v, j, e3, t)) edge[c * 4 + 3] = t;
+            __syncthreads();
+            const float2 d0 = edge[c * 4 + 0] - edge[c * 4 + 1];
+            const float2 d1 = edge[c * 4 + 3] - edge[c * 4 + 2];
+            Acoef = make_float2(P.by_ca * d0.x + P.by_cb * d1.x, P.by_ca * d0.y + P.by_cb * d1.y);
+            Bcoef = make_float2(P.by_ca * d1.x + P.by_cb * d0.x, P.by_ca * d1.y + P.by_cb * d0.y);
+        }
+        if (colok) {
+            float2 *dst = T + (size_t)(q - q0) * ny * lNx + kx;
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int yy = j + r * L::TPL - padyl;
+                if (yy >= 0 && yy < ny) {
+                    float2 o = v[r];
+                    if (yfix) {
+                        if (yy < ZPOW_N) {
+                            const float zz = P.tab.zpow[yy];
+                            o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
+                        }
+                        if (ny - 1 - yy < ZPOW_N) {
+                            const float zz = P.tab.zpow[ny - 1 - yy];
+                            o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
+                        }
+                    }
+                    dst[(size_t)yy * lNx] = o;
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// (b2) rows: backward FFT along x, x-prefilter boundary terms, crop -> slab.
+template <class L, int LPC>
+__global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L line, const float2 *T,
+                                                               float2 *slab, int q0, int qn)
+{
+    extern __shared__ float2 smem[];
+    const int n = line.size();  // lNx
+    float2 *buf0 = smem, *buf1 = smem + LPC * n, *tw = smem + 2 * LPC * n;
+    float2 *edge = tw + n;  // [LPC][4]
+    copy_twiddles<L>(tw, P.tab.twx, n);
+    const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
+    const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl;
+    const long long rid = (long long)blockIdx.x * LPC + l;
+    const bool valid = rid < (long long)qn * ny;
+    float2 v[L::SLOTS];
+    const float2 *src = T + (size_t)(valid ? rid : 0) * n;
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int x = j + r * L::TPL;
+        v[r] = (valid && x < n) ? src[x] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    int flip = 0;
+    line.template run<1>(v, j, buf0 + l * n, buf1 + l * n, 1, tw, flip);
+    const bool pf = P.order >= 2;
+    float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
+    if (pf) {
+        const int e0 = (padxl - 1 + n) % n, e1 = (padxl + 1) % n;
+        const int e2 = (padxl + nx - 2 + n) % n, e3 = (padxl + nx) % n;
+        float2 t;
+        if (held<L>(v, j, e0, t)) edge[l * 4 + 0] = t;
+        if (held<L>(v, j, e1, t)) edge[l * 4 + 1] = t;
+        if (held<L>(v, j, e2, t)) edge[l * 4 + 2] = t;
+        if (held<L>(v, j, e3, t)) edge[l * 4 + 3] = t;
+        __syncthreads();
+        const float2 d0 = edge[l * 4 + 0] - edge[l * 4 + 1];
+        const float2 d1 = edge[l * 4 + 3] - edge[l * 4 + 2];
+        Acoef = make_float2(P.bx_ca * d0.x + P.bx_cb * d1.x, P.bx_ca * d0.y + P.bx_cb * d1.y);
+        Bcoef = make_float2(P.bx_ca * d1.x + P.bx_cb * d0.x, P.bx_ca * d1.y + P.bx_cb * d0.y);
+    }
+    if (!valid)
+        return;
+    const int qq = q0 + (int)(rid / ny);
+    const int y = (int)(rid % ny);
+    const int a = qq / nz, p = qq % nz;
+    size_t base;
+    if (P.tilted)
+        base = (((size_t)a * nz + p) * ny + y) * nx;
+    else
+        base = (((size_t)a * ny + y) * nz + p) * nx;
+    float2 *dst = slab + base;
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int xx = j + r * L::TPL - padxl;
+        if (xx >= 0 && xx < nx) {
+            float2 o = v[r];
+            if (pf) {
+                if (xx < ZPOW_N) {
+                    const float zz = P.tab.zpow[xx];
+                    o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
+                }
+                if (nx - 1 - xx < ZPOW_N) {
+                    const float zz = P.tab.zpow[nx - 1 - xx];
+                    o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
+                }
+            }
+            dst[xx] = o;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Dispatch on the line length.
+template <class L>
+struct Cfg {
+    static constexpr int LPC = (L::TPL >= 256) ? 1 : 256 / L::TPL;
+    static constexpr int KX = (L::TPL >= 512) ? 1 : ((512 / L::TPL) > 16 ? 16 : 512 / L::TPL);
+};
+template <>
+struct Cfg<GenericLine> {
+    static constexpr int LPC = 4;
+    static constexpr int KX = 4;
+};
+
+template <class L>
+static size_t smem_rows(int n) { return (size_t)(2 * Cfg<L>::LPC * n + n + 4 * Cfg<L>::LPC) * sizeof(float2); }
+template <class L>
+static size_t smem_cols(int n) { return (size_t)(2 * Cfg<L>::KX * n + n + 4 * Cfg<L>::KX) * sizeof(float2); }
+
+constexpr int kPlanesPerColumnBlock = 16;
+
+template <class L>
+static cudaError_t rows_forward_impl(const StageParams &P, L line, const void *sino, const double *w, int nb,
+                                     float2 *out, cudaStream_t s)
+{
+    constexpr int LPC = Cfg<L>::LPC;
+    const long long lines = (long long)nb * P.lNy;
+    const unsigned grid = (unsigned)((lines + LPC - 1) / LPC);
+    k_rows_forward<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, sino, w, nb, out);
+    return cudaGetLastError();
+}
+
+template <class L>
+static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rowspec, float2 *T, int q0, int qn,
+                                cudaStream_t s)
+{
+    constexpr int KX = Cfg<L>::KX;
+    dim3 grid((P.lNx + KX - 1) / KX, (qn + kPlanesPerColumnBlock - 1) / kPlanesPerColumnBlock);
+    k_columns_propagate<L, KX><<<grid, KX * L::TPL, smem_cols<L>(line.n), s>>>(P, line, rowspec, T, q0, qn,
+                                                                             kPlanesPerColumnBlock);
+    return cudaGetLastError();
+}
+
+template <class L>
+static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 *T, float2 *slab, int q0, int qn,
+                                     cudaStream_t s)
+{
+    constexpr int LPC = Cfg<L>::LPC;
+    const long long lines = (long long)qn * P.ny;
+    const unsigned grid = (unsigned)((lines + LPC - 1) / LPC);
+    k_rows_inverse<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, slab, q0, qn);
+    return cudaGetLastError();
+}
+
+// The attribute is per kernel and process-wide, so it is always set to the
+// largest size the instantiation can need (the generic line serves every
+// length up to its maximum).
+template <class L>
+static cudaError_t set_smem_attrs(int n)
+{
+    if (std::is_same<L, GenericLine>::value)
+        n = GenericLine::TPL * GenericLine::SLOTS;
+    cudaError_t e;
+    e = cudaFuncSetAttribute(k_rows_forward<L, Cfg<L>::LPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_rows<L>(n));
+    if (e != cudaSuccess)
+        return e;
+    e = cudaFuncSetAttribute(k_rows_inverse<L, Cfg<L>::LPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_rows<L>(n));
+    if (e != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_cols<L>(n));
+}
+
+// Calls fn(line) with the line type for length n.
+template <class F>
+static cudaError_t with_line(int n, F &&fn)
+{
+    switch (n) {
+    case 64: return fn(Pow2Line<64>{64});
+    case 128: return fn(Pow2Line<128>{128});
+    case 256: return fn(Pow2Line<256>{256});
+    case 512: return fn(Pow2Line<512>{512});
+    case 1024: return fn(Pow2Line<1024>{1024});
+    case 2048: return fn(Pow2Line<2048>{2048});
+    case 4096: return fn(Pow2Line<4096>{4096});
+    default:
+        if (n >= 1 && n <= GenericLine::TPL * GenericLine::SLOTS)
+            return fn(GenericLine{n});
+        return cudaErrorInvalidValue;
+    }
+}
+
+bool line_size_supported(int n)
+{
+    switch (n) {
+    case 64: case 128: case 256: case 512: case 1024: case 2048: case 4096: return true;
+    default: return n >= 1 && n <= GenericLine::TPL * GenericLine::SLOTS;
+    }
+}
+
+cudaError_t configure_kernels(const StageParams &P)
+{
+    cudaError_t e = with_line(P.lNx, [&](auto line) { return set_smem_attrs<decltype(line)>(line.n); });
+    if (e != cudaSuccess)
+        return e;
+    return with_line(P.lNy, [&](auto line) { return set_smem_attrs<decltype(line)>(line.n); });
+}
+
+cudaError_t launch_rows_forward(const StageParams &P, const void *sino_batch, const double *weights_batch, int nb,
+                                float2 *rowspec, cudaStream_t s)
+{
+    return with_line(P.lNx, [&](auto line) {
+        return rows_forward_impl(P, line, sino_batch, weights_batch, nb, rowspec, s);
+    });
+}
+
+cudaError_t launch_columns_propagate(const StageParams &P, const float2 *rowspec, float2 *T, int q0, int qn,
+                                     cudaStream_t s)
+{
+    return with_line(P.lNy, [&](auto line) { return columns_impl(P, line, rowspec, T, q0, qn, s); });
+}
+
+cudaError_t launch_rows_inverse(const StageParams &P, const float2 *T, float2 *slab, int q0, int qn,
+                                cudaStream_t s)
+{
+    return with_line(P.lNx, [&](auto line) { return rows_inverse_impl(P, line, T, slab, q0, qn, s); });
+}
+
+}  // namespace odt

@@ -1,0 +1,145 @@
+"""Generate the golden fixtures in ``tests/golden/`` from the unmodified
+ODTbrain reference.
+
+Run where the reference source tree is mounted (default /root/reference, or
+$ODT_REFERENCE_ROOT):
+
+    python tests/golden/make_golden.py
+
+Writes
+  reference_zips.npz   the reference's own golden vectors for the 3D path
+                       (tests/data/alg3d_bpp__test_3d_backprop_phase.zip,
+                       ..._nopadreal.zip, ..._mprotate.zip), parsed
+  reference_cases.npz  inputs and FP64 outputs of backpropagate_3d /
+                       backpropagate_3d_tilted for small cases, produced by
+                       the reference itself (through the import shims of
+                       refshim.py: scipy.fft for FFTW, NumPy for numexpr)
+  reference_geometry.npz  FP64 host geometry of the reference (angle weights,
+                       sphere points, rotation matrices, offsets) for
+                       bit-exact comparison
+The input sinogram generator below restates the reference's test helper
+(tests/common_methods.py:63-184) so that the GPU tests can regenerate the
+same inputs without the reference tree.
+"""
+import io
+import json
+import os
+import sys
+import zipfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(HERE))
+
+import refshim  # noqa: E402
+from sino_gen import gauss_sino_3d, gauss_sino_3d_tilted, parameter_sets  # noqa: E402,E501
+
+
+def _read_zip(path):
+    with zipfile.ZipFile(path) as z:
+        return np.loadtxt(io.BytesIO(z.read("data.txt")))
+
+
+def main():
+    odt = refshim.load_reference()
+    from odtbrain import _alg3d_bppt as bppt
+    root = refshim.REFERENCE_ROOT
+    data = os.path.join(root, "tests", "data")
+    zips = {}
+    for name in ("test_3d_backprop_phase", "test_3d_backprop_nopadreal",
+                 "test_3d_mprotate"):
+        zips[name] = _read_zip(os.path.join(data,
+                                            "alg3d_bpp__%s.zip" % name))
+    np.savez_compressed(os.path.join(HERE, "reference_zips.npz"), **zips)
+
+    cases = {}
+
+    def add(name, fn, sino, angles, **kw):
+        out = fn(sino, angles, **kw)
+        cases[name + "__sino"] = sino
+        cases[name + "__angles"] = np.asarray(angles)
+        cases[name + "__out"] = out
+        clean = {}
+        for k, v in kw.items():
+            if k == "dtype":
+                continue  # every case runs at the reference default, float64
+            if isinstance(v, (list, tuple)) and k == "tilted_axis":
+                v = [float(t) for t in v]
+            elif isinstance(v, np.floating):
+                v = float(v)
+            clean[k] = v
+        cases[name + "__kw"] = np.array(json.dumps(clean))
+
+    sino, angles = gauss_sino_3d()
+    p1, p2 = parameter_sets(2)
+    add("bpp_ramp0_p2", odt.backpropagate_3d, sino, angles, padval=0,
+        dtype=float, **p2)
+    add("bpp_edge_p1", odt.backpropagate_3d, sino, angles, padval="edge",
+        dtype=float, **p1)
+    s2, a2 = gauss_sino_3d(A=7, Nx=17, Ny=13, max_phase=3.0,
+                          ampl_range=(0.8, 1.1))
+    add("bpp_rect_order3", odt.backpropagate_3d, s2, a2, padval="edge",
+        intp_order=3, dtype=float, **p1)
+    add("bpp_rect_nopad", odt.backpropagate_3d, s2, a2,
+        padding=(False, False), dtype=float, **p2)
+    add("bppt_default_p2", odt.backpropagate_3d_tilted, sino, angles,
+        padval=0, dtype=float, **p2)
+    st, at = gauss_sino_3d_tilted(A=11, tilt_plane=0.3)
+    ax = [np.sin(0.3), np.cos(0.3), 0.15]
+    add("bppt_axis_order2", odt.backpropagate_3d_tilted, st, at,
+        tilted_axis=ax, padval="edge", dtype=float, **p1)
+    add("bppt_axis_order1", odt.backpropagate_3d_tilted, st, at,
+        tilted_axis=ax, intp_order=1, padval=0, dtype=float, **p1)
+    add("bppt_yz_onlyreal", odt.backpropagate_3d_tilted, s2, a2,
+        tilted_axis=[0, np.cos(0.2), np.sin(0.2)], onlyreal=True,
+        dtype=float, **p2)
+    pts = bppt.sphere_points_from_angles_and_tilt(
+        at, np.array([0, np.cos(0.4), np.sin(0.4)]))
+    add("bppt_points3", odt.backpropagate_3d_tilted, st, pts,
+        tilted_axis=[0, np.cos(0.4), np.sin(0.4)], weight_angles=False,
+        dtype=float, **p1)
+    np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **cases)
+
+    geo = {}
+    rng = np.random.default_rng(3)
+    angle_sets = {
+        "uniform": np.linspace(0, 2 * np.pi, 200, endpoint=False),
+        "wedge": np.linspace(0, np.deg2rad(120), 40),
+        "random": np.sort(rng.uniform(-1, 7, 37)),
+        "dupes": np.concatenate([np.zeros(3), np.linspace(0, np.pi, 9)]),
+    }
+    for k, a in angle_sets.items():
+        geo["weights_%s__angles" % k] = a
+        geo["weights_%s__w" % k] = odt.util.compute_angle_weights_1d(a)
+    for i, axis in enumerate(([0, np.cos(.2), np.sin(.2)], [0.3, 1, 0.1],
+                              [0, 1, 0], [1, 0.1, 0.2])):
+        a = np.linspace(0, 2 * np.pi, 23, endpoint=False)
+        raw_axis = np.asarray(axis, dtype=float)
+        axis = bppt.norm_vec(raw_axis)
+        angz = np.arctan2(axis[0], axis[1])
+        rotmat = np.array([[np.cos(angz), -np.sin(angz), 0],
+                           [np.sin(angz), np.cos(angz), 0],
+                           [0, 0, 1]])
+        axis_yz = bppt.norm_vec(np.dot(rotmat, axis))
+        pts = bppt.sphere_points_from_angles_and_tilt(a, axis_yz)
+        rpts = bppt.rotate_points_to_axis(points=pts, axis=axis_yz)
+        shape = (30, 24, 30)
+        c = 0.5 * np.array(shape) - .5
+        mats = []
+        for pnt in rpts:
+            _d, dinv = bppt.rotation_matrix_from_point_planerot(
+                pnt, plane_angle=angz, ret_inv=True)
+            mats.append(np.concatenate([dinv.reshape(-1),
+                                        c - np.dot(dinv, c)]))
+        geo["tilt%d__axis" % i] = raw_axis
+        geo["tilt%d__angles" % i] = a
+        geo["tilt%d__points" % i] = pts
+        geo["tilt%d__geo" % i] = np.array(mats)
+    np.savez_compressed(os.path.join(HERE, "reference_geometry.npz"), **geo)
+    print("wrote fixtures to", HERE)
+
+
+if __name__ == "__main__":
+    main()

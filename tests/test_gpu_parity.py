@@ -1,0 +1,266 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the FP64
+oracle, the reference's golden vectors and fixtures made by the unmodified
+reference.
+
+Tolerances (FP32 GPU arithmetic vs FP64 reference), written per test:
+  * relative L2 error  <= 1e-5   (the stated target), and
+  * max |error| <= 1e-5 * max|reference| (single worst voxel).
+"""
+import multiprocessing as mp
+
+import numpy as np
+import pytest
+
+from conftest import reference_cases
+from oracle import odt_oracle as O
+from sino_gen import (cutout, ellipsoid_phantom_sinogram, gauss_sino_3d,
+                      gauss_sino_3d_tilted, parameter_sets)
+
+pytestmark = pytest.mark.gpu
+
+REL_L2 = 1e-5
+MAX_REL = 1e-5
+
+
+def errs(got, ref):
+    got = np.asarray(got)
+    ref = np.asarray(ref)
+    rel = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-300)
+    mx = np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300)
+    return rel, mx
+
+
+def assert_close(got, ref, rel_l2=REL_L2, max_rel=MAX_REL, what=""):
+    assert got.shape == ref.shape, (what, got.shape, ref.shape)
+    rel, mx = errs(got, ref)
+    assert rel <= rel_l2 and mx <= max_rel, \
+        "%s rel-L2 %.3e (<= %.1e), max %.3e (<= %.1e)" % (
+            what, rel, rel_l2, mx, max_rel)
+
+
+@pytest.fixture(scope="module")
+def odt(cuda_ready):
+    import odtbrain_gb300
+    return odtbrain_gb300
+
+
+def test_golden_backprop_phase(odt, golden):
+    """test_alg3d_bpp.py:30-42: padval=0 (linear ramp), complex result."""
+    sino, angles = gauss_sino_3d()
+    r = [cutout(odt.backpropagate_3d(sino, angles, padval=0, dtype=float,
+                                     **p)) for p in parameter_sets(2)]
+    data = np.array(r).flatten().view(float)
+    ref = golden["reference_zips"]["test_3d_backprop_phase"]
+    assert_close(data, ref, what="phase")
+    # the reference's own FP32-vs-FP64 bound (test_alg3d_bpp.py:101-113)
+    assert np.allclose(data, ref, atol=6e-7 * 4, rtol=0)
+
+
+def test_golden_backprop_nopadreal(odt, golden):
+    """test_alg3d_bpp.py:45-62: no padding (22-point DFTs), real part."""
+    sino, angles = gauss_sino_3d()
+    r = [cutout(odt.backpropagate_3d(sino, angles, padding=(False, False),
+                                     dtype=float, onlyreal=True, **p))
+         for p in parameter_sets(2)]
+    data = np.array(r).flatten().view(float)
+    ref = golden["reference_zips"]["test_3d_backprop_nopadreal"]
+    assert_close(data, ref, what="nopadreal")
+
+
+def test_reference_cases(odt, golden):
+    for name, sino, angles, kw, out in reference_cases(golden):
+        fn = (odt.backpropagate_3d_tilted if name.startswith("bppt")
+              else odt.backpropagate_3d)
+        got = fn(sino, angles, **kw)
+        assert got.dtype == out.dtype, name
+        assert_close(got, out, what=name)
+
+
+@pytest.mark.parametrize("order", [0, 1, 2, 3])
+@pytest.mark.parametrize("kind", ["y", "tilted"])
+def test_orders_vs_oracle(odt, order, kind):
+    rng = np.random.default_rng(order * 7 + (kind == "y"))
+    A, ny, nx = 10, 18, 20
+    sino = (rng.normal(0, .1, (A, ny, nx))
+            + 1j * rng.normal(0, .5, (A, ny, nx)))
+    angles = np.sort(rng.uniform(0, 2 * np.pi, A))
+    kw = dict(res=3.0, nm=1.333, intp_order=order, padval="edge")
+    if kind == "y":
+        ref = O.backpropagate_3d(sino, angles, **kw)
+        got = odt.backpropagate_3d(sino, angles, **kw)
+    else:
+        ax = [0.1, 1.0, 0.25]
+        ref = O.backpropagate_3d_tilted(sino, angles, tilted_axis=ax, **kw)
+        got = odt.backpropagate_3d_tilted(sino, angles, tilted_axis=ax, **kw)
+    # order 0 is nearest-neighbour: a voxel's value jumps where its
+    # coordinate crosses a half-integer; FP32 filtering does not move
+    # coordinates (FP64 geometry), so the bound stays the same
+    assert_close(got, ref, what="order %d %s" % (order, kind))
+
+
+@pytest.mark.parametrize("shape,padding,padval", [
+    ((6, 16, 16), (True, True), "edge"),      # padded to 64
+    ((5, 64, 64), (False, False), "edge"),    # 64-point Stockham, unpadded
+    ((5, 30, 24), (False, False), "edge"),    # generic DFT both axes
+    ((4, 70, 40), (True, True), 0.5),         # 128 x 128 padded, ramp
+    ((4, 9, 37), (True, True), 2j * np.pi),   # complex ramp end value
+])
+def test_padding_and_sizes(odt, shape, padding, padval):
+    rng = np.random.default_rng(sum(shape))
+    A, ny, nx = shape
+    sino = np.exp(1j * rng.normal(0, .4, shape) + rng.normal(0, .05, shape))
+    # distinct modulo pi: symmetric sets make the angle weights 0/0, in the
+    # reference as here
+    angles = np.sort(rng.uniform(0, 2 * np.pi, A))
+    kw = dict(res=2.5, nm=1.335, lD=1.5, padding=padding, padval=padval)
+    ref = O.backpropagate_3d(sino, angles, **kw)
+    got = odt.backpropagate_3d(sino, angles, **kw)
+    assert_close(got, ref, what=str(shape))
+
+
+def test_onlyreal_matches_real_part(odt):
+    """test_alg3d_bpp.py:77-98."""
+    sino, angles = gauss_sino_3d(Nx=10, Ny=10)
+    for p in parameter_sets(2):
+        c = odt.backpropagate_3d(sino, angles, padval=0, dtype=float, **p)
+        r = odt.backpropagate_3d(sino, angles, padval=0, dtype=float,
+                                 onlyreal=True, **p)
+        assert r.dtype == np.float64
+        assert np.allclose(c.real, r, rtol=0, atol=1e-7 * np.abs(c).max())
+
+
+def test_float32_dtype(odt):
+    sino, angles = gauss_sino_3d()
+    p = parameter_sets(1)[0]
+    f32 = odt.backpropagate_3d(sino, angles, padval=0, dtype=np.float32, **p)
+    f64 = odt.backpropagate_3d(sino, angles, padval=0, dtype=float, **p)
+    assert f32.dtype == np.complex64 and f64.dtype == np.complex128
+    assert np.array_equal(f32.astype(np.complex128), f64)
+
+
+@pytest.mark.parametrize("fn", ["backpropagate_3d", "backpropagate_3d_tilted"])
+def test_save_memory_and_copy(odt, fn):
+    """test_save_memory.py and test_copy.py: identical results."""
+    sino, angles = gauss_sino_3d(Nx=10, Ny=10)
+    p = parameter_sets(1)[0]
+    f = getattr(odt, fn)
+    a = f(sino, angles, padval=0, save_memory=False, **p)
+    b = f(sino, angles, padval=0, save_memory=True, **p)
+    assert np.array_equal(a, b)
+    s2 = sino.copy()
+    c = f(s2, angles, padval=0, copy=False, **p)
+    assert np.allclose(a, c, rtol=1e-6, atol=1e-7 * np.abs(a).max())
+    # copy=False overwrote the caller's array with the weighted sinogram
+    from odtbrain_gb300.util import compute_angle_weights_1d
+    w = compute_angle_weights_1d(angles).reshape(-1, 1, 1)
+    assert np.allclose(s2, sino * w)
+
+
+@pytest.mark.parametrize("fn", ["backpropagate_3d", "backpropagate_3d_tilted"])
+def test_even_weights(odt, fn):
+    """test_weighting.py: uniform angles give weights 1."""
+    sino, angles = gauss_sino_3d()
+    p = parameter_sets(1)[0]
+    f = getattr(odt, fn)
+    a = f(sino, angles, weight_angles=False, **p)
+    b = f(sino, angles, weight_angles=True, **p)
+    assert np.allclose(a, b, rtol=0, atol=1e-6 * np.abs(a).max())
+
+
+@pytest.mark.parametrize("fn", ["backpropagate_3d", "backpropagate_3d_tilted"])
+def test_counters(odt, fn):
+    """test_counters.py:63-90."""
+    sino, angles = gauss_sino_3d(Nx=10, Ny=10)
+    p = parameter_sets(1)[0]
+    jmc = mp.Value("i", 0)
+    jmm = mp.Value("i", 0)
+    getattr(odt, fn)(sino, angles, padval=0, count=jmc, max_count=jmm, **p)
+    assert jmc.value == jmm.value
+    assert jmc.value != 0
+
+
+def test_tilted_default_axis_equals_plain(odt):
+    """test_alg3d_bppt.py:10-50."""
+    sino, angles = gauss_sino_3d()
+    for p in parameter_sets(2):
+        for pv in (0, "edge"):
+            a = odt.backpropagate_3d(sino, angles, padval=pv, **p)
+            b = odt.backpropagate_3d_tilted(sino, angles, padval=pv, **p)
+            assert np.allclose(a, b, rtol=0, atol=2e-6 * np.abs(a).max())
+
+
+def test_tilted_plane_rotation_soft(odt):
+    """test_alg3d_bppt.py:53-86 (the reference's soft tolerance)."""
+    p = parameter_sets(1)[0]
+    results = []
+    for angz in [1.1, 0.0, 0.234, 2.80922, -.29, 9.87]:
+        sino, angles = gauss_sino_3d_tilted(tilt_plane=angz, A=21)
+        axis = np.dot(np.array([[np.cos(angz), -np.sin(angz), 0],
+                                [np.sin(angz), np.cos(angz), 0],
+                                [0, 0, 1]]), [0, 1, 0])
+        f = odt.backpropagate_3d_tilted(sino, angles, padval="edge",
+                                        tilted_axis=axis,
+                                        padding=(False, False), **p)
+        results.append(cutout(f).flatten().view(float))
+    for ii in range(len(results)):
+        assert np.allclose(results[ii], results[ii - 1], atol=.2, rtol=.2)
+
+
+def test_multibatch_kahan(odt, monkeypatch):
+    """A workspace too small for all angles forces several batches; the
+    compensation carried across launches keeps the result unchanged."""
+    from odtbrain_gb300 import _alg3d
+    sino, angles = ellipsoid_phantom_sinogram(48, 40, seed=4,
+                                              count_range=(2, 4),
+                                              semi_range=(4, 12))
+    kw = dict(res=3.0, nm=1.333, dtype=np.float32)
+    one = odt.backpropagate_3d(sino, angles, **kw)
+    monkeypatch.setattr(_alg3d, "_WS_DEFAULT", 8 << 20)
+    _alg3d._PLAN_CACHE.clear()
+    many = odt.backpropagate_3d(sino, angles, **kw)
+    _alg3d._PLAN_CACHE.clear()
+    ref = O.backpropagate_3d(sino, angles, res=3.0, nm=1.333)
+    assert_close(many, ref, what="multibatch")
+    assert_close(one, ref, what="single batch")
+
+
+def test_torch_tensors_in_and_out(odt):
+    import torch
+    sino, angles = gauss_sino_3d()
+    p = parameter_sets(1)[0]
+    ref = odt.backpropagate_3d(sino, angles, dtype=np.float32, **p)
+    t = torch.from_numpy(sino.astype(np.complex64)).cuda()
+    out = odt.backpropagate_3d(t, torch.from_numpy(angles), dtype=np.float32,
+                               **p)
+    assert isinstance(out, torch.Tensor) and out.is_cuda
+    assert out.dtype == torch.complex64
+    assert np.allclose(out.cpu().numpy(), ref, rtol=0,
+                       atol=1e-6 * np.abs(ref).max())
+
+
+def test_c2_shape_subset_vs_oracle(odt):
+    """256^2 -> 512^2 padded, 256^3 volume (the benchmark's plane and volume
+    size) with 3 angles; the oracle runs on the host cores."""
+    sino, angles = ellipsoid_phantom_sinogram(
+        256, 3, seed=11, count_range=(3, 12), semi_range=(8, 60),
+        angles=np.array([0.3, 1.9, 4.4]))
+    kw = dict(res=3.0, nm=1.333)
+    got = odt.backpropagate_3d(sino.astype(np.complex64), angles,
+                               dtype=np.float32, **kw)
+    ref = O.backpropagate_3d(sino, angles, fft_workers=-1, **kw)
+    assert_close(got, ref, what="256^3")
+
+
+def test_c3_shape_subset_vs_oracle(odt):
+    """Tilted axis 0.2 rad toward z, 200^2 -> 512^2, 200^3 volume, 2
+    angles."""
+    ax = (0, np.cos(0.2), np.sin(0.2))
+    sino, angles = ellipsoid_phantom_sinogram(
+        200, 2, seed=12, count_range=(3, 12), semi_range=(8, 50), axis=ax,
+        angles=np.array([0.0, 2.5]))
+    # two angles give 0/0 angle weights (as in the reference): weights off
+    kw = dict(res=3.0, nm=1.333, tilted_axis=ax, weight_angles=False)
+    got = odt.backpropagate_3d_tilted(sino.astype(np.complex64), angles,
+                                      dtype=np.float32, **kw)
+    ref = O.backpropagate_3d_tilted(sino, angles, fft_workers=-1, **kw)
+    assert_close(got, ref, what="200^3 tilted")

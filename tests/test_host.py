@@ -1,0 +1,192 @@
+"""CPU tests of the host side: FP64 geometry bit-identical to the
+reference's, input validation and error types, and the C ABI library (it
+loads and exports every symbol include/odtbrain_gb300.h declares; its
+argument checks run without a GPU)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import odtbrain_gb300 as odt
+from odtbrain_gb300 import _geometry as geom
+from odtbrain_gb300 import _native, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_weights_bit_identical(golden):
+    g = golden["reference_geometry"]
+    keys = [k for k in g if k.startswith("weights_") and
+            k.endswith("__angles")]
+    assert keys
+    for k in keys:
+        stem = k[:-len("__angles")]
+        assert np.array_equal(geom.compute_angle_weights_1d(g[k]),
+                              g[stem + "__w"]), stem
+
+
+def test_tilted_geometry_bit_identical(golden):
+    g = golden["reference_geometry"]
+    for i in range(4):
+        axis = g["tilt%d__axis" % i]
+        angles = g["tilt%d__angles" % i]
+        axis_n = geom.norm_vec(axis)
+        angz = np.arctan2(axis_n[0], axis_n[1])
+        rotmat = np.array([[np.cos(angz), -np.sin(angz), 0],
+                           [np.sin(angz), np.cos(angz), 0], [0, 0, 1]])
+        axis_yz = geom.norm_vec(np.dot(rotmat, axis_n))
+        pts = geom.sphere_points_from_angles_and_tilt(angles, axis_yz)
+        assert np.array_equal(pts, g["tilt%d__points" % i])
+        _w, mats, _ax = geom.tilted_geometry(angles, axis, False,
+                                             (30, 24, 30))
+        assert np.array_equal(mats, g["tilt%d__geo" % i]), i
+
+
+def test_sphere_points_known_answers():
+    """test_spherecoords_from_angles_and_axis.py:8-30."""
+    angles = np.array([0, np.pi / 2, np.pi])
+    axes = [[1, 0, 0], [0, 1, 0], [0, 0, 1], [0, 1, 1], [1, 0, 1], [1, 1, 1]]
+    s2 = 1 / np.sqrt(2)
+    correct = np.array([[[1, 0, 0], [1, 0, 0], [1, 0, 0]],
+                        [[0, 0, 1], [1, 0, 0], [0, 0, -1]],
+                        [[0, 0, 1], [0, 0, 1], [0, 0, 1]],
+                        [[0, 0, 1], [s2, .5, .5], [0, 1, 0]],
+                        [[s2, 0, s2], [s2, 0, s2], [s2, 0, s2]],
+                        [[s2, 0, s2],
+                         [0.87965281125489458, s2 / 3 * 2,
+                          0.063156230327168605],
+                         [s2 / 3, s2 / 3 * 4, s2 / 3]]])
+    res = [geom.sphere_points_from_angles_and_tilt(angles, ax)
+           for ax in axes]
+    assert np.allclose(correct, np.array(res))
+
+
+def test_rotation_matrices_known_answers():
+    """test_rotation_matrices.py:8-102."""
+    sq2 = np.sqrt(2)
+    rot = geom.rotate_points_to_axis(points=[[1, 2, 3]], axis=[1, 2, 3])
+    assert rot[0][0] < 1e-14 and rot[0][2] < 1e-14
+    rot = geom.rotate_points_to_axis(points=[[0, 0, 1], [1, 0, 0], [1, 1, 0]],
+                                     axis=[0, 1, 1])
+    assert np.allclose(rot[0], [0, 1 / sq2, 1 / sq2])
+    assert np.allclose(rot[1], [1, 0, 0])
+    assert np.allclose(rot[2], [1, 1 / sq2, -1 / sq2])
+    rot = geom.rotate_points_to_axis(points=[[0, 0, 1], [1, 0, 0],
+                                             [0, -1, 0]], axis=[1, 0, 1])
+    assert np.allclose(rot[0], [-.5, 1 / sq2, .5])
+    assert np.allclose(rot[1], [.5, 1 / sq2, -.5])
+    assert np.allclose(rot[2], [1 / sq2, 0, 1 / sq2])
+    rot = geom.rotate_points_to_axis(points=[[0, 0, 1], [1, 0, 0],
+                                             [1, -1, 0]], axis=[0, -1, 0])
+    assert np.allclose(rot[0], [0, 0, -1])
+    m1 = geom.rotation_matrix_from_point([0, 0, 1])
+    assert np.allclose(np.dot(m1, [1, 2, 3]), [1, 2, 3])
+    m2 = geom.rotation_matrix_from_point([0, 1, 1])
+    assert np.allclose(np.dot(m2, [0, 0, 1]), [0, 1 / sq2, 1 / sq2])
+    m3 = geom.rotation_matrix_from_point([-1, 1, 0])
+    assert np.allclose(np.dot(m3, [1, 0, 0]), [0, 0, -1])
+    assert np.allclose(np.dot(m3, [0, 1 / sq2, -1 / sq2]), [-1, 0, 0])
+
+
+def test_rotation_y_geometry_matches_scipy_construction():
+    from scipy import special
+    angles = np.linspace(0, 2 * np.pi, 200, endpoint=False)
+    g = geom.rotation_y_geometry(angles, 256, 256)
+    for i in (0, 50, 77, 199):
+        deg = -np.rad2deg(angles[i])
+        c, s = special.cosdg(deg), special.sindg(deg)
+        R = np.array([[c, s], [-s, c]])
+        shp = np.asarray((256, 256))
+        off = (shp - 1) / 2 - R @ ((shp - 1) / 2)
+        assert np.array_equal(g[i, :4], R.reshape(-1))
+        assert np.array_equal(g[i, 4:], off)
+
+
+def test_padding_geometry():
+    g = geom.padding_geometry(256, 256, (True, True), 1.75)
+    assert (g["lNx"], g["lNy"], g["padxl"], g["padyl"]) == (512, 512, 128,
+                                                            128)
+    g = geom.padding_geometry(200, 200, (True, True), 1.75)
+    assert (g["lNx"], g["padxl"], g["padxr"]) == (512, 156, 156)
+    g = geom.padding_geometry(22, 22, (True, True), 1.75)
+    assert g["lNx"] == 64
+    g = geom.padding_geometry(128, 128, (True, True), 1.75)
+    assert g["lNx"] == 256
+    g = geom.padding_geometry(22, 17, (False, False), 1.75)
+    assert (g["lNx"], g["lNy"]) == (17, 22)
+
+
+@pytest.mark.parametrize("kwargs,exc", [
+    (dict(padding=(True,)), ValueError),
+    (dict(padding=(1, 1)), ValueError),
+    (dict(padding=(True, False)), ValueError),
+    (dict(coords=np.zeros((3, 4))), NotImplementedError),
+    (dict(num_cores=10 ** 6), ValueError),
+    (dict(dtype=np.int32), ValueError),
+])
+@pytest.mark.parametrize("fn", ["backpropagate_3d", "backpropagate_3d_tilted"])
+def test_validation_errors(fn, kwargs, exc):
+    sino = np.ones((4, 8, 8), dtype=complex)
+    angles = np.linspace(0, np.pi, 4)
+    with pytest.raises(exc):
+        getattr(odt, fn)(sino, angles, 3.0, 1.333, **kwargs)
+
+
+def test_shape_errors():
+    with pytest.raises(ValueError):
+        odt.backpropagate_3d(np.ones((4, 8), complex), np.zeros(4), 3, 1.3)
+    with pytest.raises(ValueError):
+        odt.backpropagate_3d(np.ones((4, 8, 8), complex), np.zeros(3), 3,
+                             1.3)
+    with pytest.raises(ValueError):
+        odt.backpropagate_3d_tilted(np.ones((4, 8, 8), complex),
+                                    np.zeros((4, 2)), 3, 1.3)
+
+
+def _header_symbols():
+    text = open(os.path.join(ROOT, "include", "odtbrain_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(odt_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def native_lib():
+    build.build()
+    return _native.lib()
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    declared = _header_symbols()
+    assert set(declared) == set(_native.EXPORTED_SYMBOLS)
+    for name in declared:
+        assert hasattr(native_lib, name), name
+
+
+def test_plan_create_argument_checks(native_lib):
+    """Validation happens before any CUDA call, so it runs on CPU."""
+    d = _native.Bpp3dDesc()
+    d.num_angles, d.ny, d.nx = 4, 16, 16
+    d.pad_ny = d.pad_nx = 64
+    d.pad_y_left = d.pad_x_left = 24
+    d.pad_mode = _native.ODT_PAD_EDGE
+    d.intp_order = 4
+    filt = np.zeros(64 * 64 * 2)
+    ph = np.zeros(64 * 64)
+    d.filter = filt.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.kz_phase = ph.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    h = ctypes.c_void_p()
+    st = native_lib.odt_bpp3d_plan_create(ctypes.byref(d), ctypes.byref(h))
+    assert st == _native.ODT_ERR_UNSUPPORTED
+    with pytest.raises(NotImplementedError):
+        _native.check(st)
+    d.intp_order = 2
+    d.pad_x_left = 60
+    st = native_lib.odt_bpp3d_plan_create(ctypes.byref(d), ctypes.byref(h))
+    assert st == _native.ODT_ERR_INVALID_ARGUMENT
+    assert b"padding" in native_lib.odt_last_error()
+    d.pad_x_left = 24
+    d.pad_nx = 3000  # neither a supported power of two nor <= 1024
+    st = native_lib.odt_bpp3d_plan_create(ctypes.byref(d), ctypes.byref(h))
+    assert st == _native.ODT_ERR_UNSUPPORTED
+    assert native_lib.odt_status_string(5) == b"device-side check failed"
