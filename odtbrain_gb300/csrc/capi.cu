@@ -79,8 +79,9 @@ struct odt_bpp3d_plan {
     int nz;
     int batch;       // angles per batch
     int jobs;        // (angle, plane) jobs per column/row launch
-    size_t off_rowspec, off_T, off_slab, off_comp, ws_bytes;
+    size_t off_rowspec, off_T, off_Tab, off_slab, off_comp, off_rot, ws_bytes;
     double bx_ca, bx_cb, by_ca, by_cb;
+    int kx_zero_lo, kx_zero_hi;  // all-zero spectrum columns [lo, hi)
     // device tables (one allocation)
     void *d_tables;
     FilterTables tab;
@@ -106,6 +107,8 @@ StageParams stage_params(const odt_bpp3d_plan *p)
     P.order = d.intp_order;
     P.tilted = d.geometry == ODT_GEOM_AFFINE3D;
     P.in_c128 = d.input_dtype == ODT_INPUT_C128;
+    P.kx_zero_lo = p->kx_zero_lo;
+    P.kx_zero_hi = p->kx_zero_hi;
     P.bx_ca = (float)p->bx_ca;
     P.bx_cb = (float)p->bx_cb;
     P.by_ca = (float)p->by_ca;
@@ -232,6 +235,28 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
             }
         }
     }
+    // largest run of all-zero filter columns around the Nyquist column
+    // (outside the |k| < km disc): neither computed nor read
+    {
+        auto zero_col = [&](int kx) {
+            for (int ky = 0; ky < lNy; ++ky) {
+                const size_t k = (size_t)ky * lNx + kx;
+                if (desc->filter[2 * k] != 0.0 || desc->filter[2 * k + 1] != 0.0)
+                    return false;
+            }
+            return true;
+        };
+        int lo = lNx / 2, hi = lNx / 2;
+        if (zero_col(lNx / 2)) {
+            hi = lNx / 2 + 1;
+            while (lo > 0 && zero_col(lo - 1))
+                --lo;
+            while (hi < lNx && zero_col(hi))
+                ++hi;
+        }
+        p->kx_zero_lo = lo;
+        p->kx_zero_hi = hi;
+    }
     for (int m = 0; m < lNx; ++m)
         twx[m] = make_float2((float)std::cos(-2.0 * M_PI * m / lNx), (float)std::sin(-2.0 * M_PI * m / lNx));
     for (int m = 0; m < lNy; ++m)
@@ -282,30 +307,65 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     p->tab.zpow = (const float *)(base + oZ);
     p->d_status = (int *)(base + oSt);
 
-    // ---- batching
+    // ---- batching: the largest angle batch (and column-stage chunk) whose
+    // workspace fits the limit
     const size_t plane_row_bytes = (size_t)d.ny * lNx * 8;           // one job's column-stage output
     const size_t slab_bytes = (size_t)nz * d.ny * d.nx * 8;          // one angle's coefficient slab
     const size_t rowspec_bytes = (size_t)lNy * lNx * 8;              // one angle's row spectra
+    const size_t tab_bytes = pf ? (size_t)2 * d.ny * lNx * 8 : 0;    // one angle's z-boundary rows
     const size_t vol_bytes = (size_t)nz * d.ny * d.nx * 8;           // compensation buffer
     const uint64_t limit = d.workspace_limit ? d.workspace_limit : kDefaultWorkspace;
-    size_t jobs_cap = std::max<size_t>(16, kPlaneBudget / plane_row_bytes);
-    long long batch = (long long)((limit > vol_bytes + jobs_cap * plane_row_bytes)
-                                      ? (limit - vol_bytes - jobs_cap * plane_row_bytes) / (slab_bytes + rowspec_bytes)
-                                      : 1);
-    batch = std::max<long long>(1, std::min<long long>(batch, d.num_angles));
-    p->batch = (int)batch;
-    const size_t total_jobs = (size_t)batch * nz;
-    size_t jobs = std::min(total_jobs, jobs_cap);
-    if (jobs >= 16)
-        jobs = jobs / 16 * 16;
-    p->jobs = (int)jobs;
-    const int nbatches = (d.num_angles + p->batch - 1) / p->batch;
-    size_t w = 0;
-    p->off_rowspec = w; w = align_up(w + (size_t)batch * rowspec_bytes);
-    p->off_T = w; w = align_up(w + jobs * plane_row_bytes);
-    p->off_slab = w; w = align_up(w + (size_t)batch * slab_bytes);
-    p->off_comp = w; w = align_up(w + (nbatches > 1 ? vol_bytes : 0));
-    p->ws_bytes = w;
+    const size_t jobs_cap = std::max<size_t>(16, kPlaneBudget / plane_row_bytes);
+    auto layout = [&](int batch, size_t jobs, bool commit) -> size_t {
+        const int nbatches = (d.num_angles + batch - 1) / batch;
+        size_t w = 0;
+        const size_t o_rowspec = w; w = align_up(w + (size_t)batch * rowspec_bytes);
+        const size_t o_T = w; w = align_up(w + jobs * plane_row_bytes);
+        const size_t o_Tab = w; w = align_up(w + (size_t)batch * tab_bytes);
+        const size_t o_slab = w; w = align_up(w + (size_t)batch * slab_bytes);
+        const size_t o_comp = w; w = align_up(w + (nbatches > 1 ? vol_bytes : 0));
+        const size_t o_rot = w;
+        w = align_up(w + odt::rotate_scratch_bytes(batch, d.ny, d.nx, nz, tilted ? 1 : 0));
+        if (commit) {
+            p->batch = batch;
+            p->jobs = (int)jobs;
+            p->off_rowspec = o_rowspec;
+            p->off_T = o_T;
+            p->off_Tab = o_Tab;
+            p->off_slab = o_slab;
+            p->off_comp = o_comp;
+            p->off_rot = o_rot;
+            p->ws_bytes = w;
+        }
+        return w;
+    };
+    auto jobs_for = [&](int batch) {
+        size_t jobs = std::min((size_t)batch * nz, jobs_cap);
+        return jobs >= 16 ? jobs / 16 * 16 : jobs;
+    };
+    int best = 0;
+    for (int lo = 1, hi = d.num_angles; lo <= hi;) {  // ws grows with the batch
+        const int mid = lo + (hi - lo) / 2;
+        if (layout(mid, jobs_for(mid), false) <= limit) {
+            best = mid;
+            lo = mid + 1;
+        } else {
+            hi = mid - 1;
+        }
+    }
+    // a single batch needs no compensation buffer, so it can fit when a
+    // slightly smaller batch does not
+    if (best < d.num_angles && layout(d.num_angles, jobs_for(d.num_angles), false) <= limit)
+        best = d.num_angles;
+    if (best > 0) {
+        layout(best, jobs_for(best), true);
+    } else {
+        // one angle per batch; shrink the column-stage chunk toward the limit
+        size_t jobs = jobs_for(1);
+        while (jobs > 1 && layout(1, jobs, false) > limit)
+            jobs = jobs > 16 ? jobs - 16 : jobs - 1;
+        layout(1, jobs, true);
+    }
 
     StageParams P = stage_params(p);
     e = odt::configure_kernels(P);
@@ -393,8 +453,10 @@ odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *
     char *ws = (char *)workspace;
     float2 *rowspec = (float2 *)(ws + plan->off_rowspec);
     float2 *T = (float2 *)(ws + plan->off_T);
+    float2 *Tab = (float2 *)(ws + plan->off_Tab);
     float2 *slab = (float2 *)(ws + plan->off_slab);
     float2 *comp = (float2 *)(ws + plan->off_comp);
+    void *rot_scratch = ws + plan->off_rot;
     const size_t in_elem = d.input_dtype == ODT_INPUT_C128 ? 16 : 8;
     const int geo_stride = d.geometry == ODT_GEOM_AFFINE3D ? 12 : 6;
     const int nbatches = (d.num_angles + plan->batch - 1) / plan->batch;
@@ -414,6 +476,13 @@ odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *
         if (e != cudaSuccess)
             return cuda_fail(e, "rows_forward launch");
         lt.end(nb * (plane_in * in_elem + spec * 8.0));
+        if (d.intp_order >= 2) {
+            lt.begin(ODT_STAGE_COLUMNS_PROPAGATE);
+            e = odt::launch_columns_boundary(P, rowspec, Tab, nb, s);
+            if (e != cudaSuccess)
+                return cuda_fail(e, "columns_boundary launch");
+            lt.end(0.0);
+        }
         const int total = nb * plan->nz;
         for (int q0 = 0; q0 < total; q0 += plan->jobs) {
             const int qn = std::min(plan->jobs, total - q0);
@@ -423,7 +492,7 @@ odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *
                 return cuda_fail(e, "columns_propagate launch");
             lt.end((double)qn / plan->nz * spec * 8.0);
             lt.begin(ODT_STAGE_ROWS_INVERSE);
-            e = odt::launch_rows_inverse(P, T, slab, q0, qn, s);
+            e = odt::launch_rows_inverse(P, T, Tab, slab, q0, qn, s);
             if (e != cudaSuccess)
                 return cuda_fail(e, "rows_inverse launch");
             lt.end((double)qn * plane_in * 8.0);
@@ -439,7 +508,7 @@ odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *
         R.status = plan->d_status;
         lt.begin(ODT_STAGE_ROTATE);
         e = odt::launch_rotate(R, d.intp_order, d.geometry == ODT_GEOM_AFFINE3D, slab,
-                               geometry + (size_t)a0 * geo_stride, volume, comp, s);
+                               geometry + (size_t)a0 * geo_stride, volume, comp, rot_scratch, s);
         if (e != cudaSuccess)
             return cuda_fail(e, "rotate launch");
         double rb = nb * vol * 8.0 + vol * out_elem;
@@ -485,6 +554,10 @@ odt_status odt_bpp3d_launch_count(const odt_bpp3d_plan *plan, int64_t *launches)
         const int nb = std::min(plan->batch, A - b * plan->batch);
         const int64_t total = (int64_t)nb * plan->nz;
         n += 2 + 2 * ((total + plan->jobs - 1) / plan->jobs);
+        if (plan->d.intp_order >= 2)
+            n += 1;  // z-prefilter boundary columns
+        if (plan->d.geometry == ODT_GEOM_Y_AXIS)
+            n += 1;  // per-(angle, tile) geometry setup
     }
     *launches = n;
     return ODT_OK;

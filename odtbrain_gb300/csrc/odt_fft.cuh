@@ -87,6 +87,15 @@ __device__ __forceinline__ void dft8(float2 *x)
 }
 
 constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+
+// Exchange-buffer slot of line position p: bits 3..6 are XORed into bits
+// 0..3.  This permutes each 128-position block, and makes every access
+// pattern of the Stockham passes (unit-stride reads, stride-8 and stride-64
+// writes) hit distinct banks within a half-warp, for element strides 1, 2,
+// 4, 8 and 16 (the row and column buffer layouts).
+__device__ __forceinline__ int xslot(int p) { return p ^ ((p >> 3) & 15); }
+// Slots a line of n positions occupies in an exchange buffer.
+__host__ __device__ constexpr int xslots(int n) { return n; }
 constexpr int ipow8(int k) { return k == 0 ? 1 : 8 * ipow8(k - 1); }
 
 // Power-of-two line, 64 <= N <= 4096.
@@ -125,11 +134,11 @@ struct Pow2Line {
             const int idxD = (j / Ns) * Ns * 8 + (j & (Ns - 1));
 #pragma unroll
             for (int r = 0; r < 8; ++r)
-                b[(idxD + r * Ns) * es] = v[r];
+                b[xslot(idxD + r * Ns) * es] = v[r];
             __syncthreads();
 #pragma unroll
             for (int r = 0; r < 8; ++r)
-                v[r] = b[(j + r * TPL) * es];
+                v[r] = b[xslot(j + r * TPL) * es];
             Ns *= 8;
         }
         if (TAIL == 4) {
@@ -159,7 +168,7 @@ struct Pow2Line {
     }
 };
 
-// Any N <= TPL*SLOTS: direct DFT through shared memory.
+// Any N <= TPL*SLOTS: direct DFT through shared memory (unpadded slots).
 struct GenericLine {
     static constexpr int TPL = 64;
     static constexpr int SLOTS = 16;

@@ -35,6 +35,8 @@ struct StageParams {
     int tilted;       // 1: slabs for the 3D affine path ([a][z][y][x] and a
                       //    y-prefilter); 0: y-axis path ([a][y][z][x])
     int in_c128;      // input sinogram is complex128
+    int kx_zero_lo, kx_zero_hi;  // spectrum columns in [lo, hi) are all zero
+                                 // (outside the |k| < km disc)
     float bx_ca, bx_cb;  // x-prefilter boundary solve (n = nx)
     float by_ca, by_cb;  // y-prefilter boundary solve (n = ny)
     FilterTables tab;
@@ -55,10 +57,16 @@ cudaError_t launch_rows_forward(const StageParams &P, const void *sino_batch, co
                                 int nb, float2 *rowspec, cudaStream_t s);
 cudaError_t launch_columns_propagate(const StageParams &P, const float2 *rowspec, float2 *T, int q0, int qn,
                                      cudaStream_t s);
-cudaError_t launch_rows_inverse(const StageParams &P, const float2 *T, float2 *slab, int q0, int qn,
-                                cudaStream_t s);
+// z-prefilter boundary columns of a batch (order >= 2): Tab[a][2][ny][lNx].
+cudaError_t launch_columns_boundary(const StageParams &P, const float2 *rowspec, float2 *Tab, int nb,
+                                    cudaStream_t s);
+cudaError_t launch_rows_inverse(const StageParams &P, const float2 *T, const float2 *Tab, float2 *slab, int q0,
+                                int qn, cudaStream_t s);
+// Scratch (device bytes) the rotation stage needs for a batch: per-(angle,
+// tile) geometry records of the y-axis path.
+size_t rotate_scratch_bytes(int nbatch_angles, int ny, int nx, int nz, int tilted);
 cudaError_t launch_rotate(const RotParams &R, int order, int tilted, const float2 *slab, const double *geo,
-                          void *volume, float2 *comp, cudaStream_t s);
+                          void *volume, float2 *comp, void *scratch, cudaStream_t s);
 cudaError_t configure_kernels(const StageParams &P);
 bool line_size_supported(int n);
 

@@ -197,83 +197,157 @@ __device__ __forceinline__ void store_sum(const RotParams &R, void *volume, floa
 // ---------------------------------------------------------------------------
 // y-axis path: every (z, x) plane at fixed y is rotated; the slab layout is
 // [a][y][z][x] so that a plane is contiguous.
+//
+// Work split: a CTA owns a 32 (z) x 32 (x) output tile of one y plane and
+// loops over the batch's angles.  The footprint of the rotated tile
+// (<= 52 x 52 coefficients for orders <= 3) is staged in shared memory with
+// cp.async, double-buffered so that the next angle's footprint streams in
+// while the current one is interpolated.  Everything that depends only on
+// (angle, tile) -- the footprint box, the FP32 coordinate split, whether
+// the tile needs bounds checks and mirrored taps -- is computed once per
+// launch by k_rotate_y_setup and read back as a 64-byte record.
 constexpr int RY_T = 32;       // output tile is 32 (z) x 32 (x)
 constexpr int RY_BOX = 52;     // footprint of a rotated tile + taps + margin
 constexpr int RY_BP = 53;      // shared-memory row pitch (float2)
+constexpr int RY_KAHAN = 8;    // angles summed plainly between Kahan steps
+
+struct __align__(16) TileGeo {
+    AxisCoord z, x;            // coordinates at the tile origin
+    short box_z0, box_x0;      // footprint origin
+    short box_zn, box_xn;      // footprint size; box_zn == 0: no output of
+                               // the tile is inside for this angle
+    int interior;              // all taps in range: no checks, no mirroring
+    int pad;
+};
+static_assert(sizeof(TileGeo) == 64, "TileGeo is one 64-byte record");
+
+template <int ORDER>
+__global__ void k_rotate_y_setup(RotParams R, const double *__restrict__ geo, TileGeo *__restrict__ tiles)
+{
+    const int ntz = (R.nz + RY_T - 1) / RY_T, ntx = (R.nx + RY_T - 1) / RY_T;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= R.nbatch_angles * ntz * ntx)
+        return;
+    const int a = id / (ntz * ntx), t = id % (ntz * ntx);
+    const int oz0 = (t / ntx) * RY_T, ox0 = (t % ntx) * RY_T;
+    const int nz = R.nz, nx = R.nx;
+    const double *g = geo + 6 * (size_t)a;
+    const double m00 = g[0], m01 = g[1], m10 = g[2], m11 = g[3], f0 = g[4], f1 = g[5];
+    const int ozB = min(oz0 + RY_T - 1, nz - 1), oxB = min(ox0 + RY_T - 1, nx - 1);
+    double czmin = DBL_MAX, czmax = -DBL_MAX, cxmin = DBL_MAX, cxmax = -DBL_MAX;
+    for (int k = 0; k < 4; ++k) {
+        const double oz = (k & 1) ? ozB : oz0, oxx = (k & 2) ? oxB : ox0;
+        const double cz = (f0 + m00 * oz) + m01 * oxx, cx = (f1 + m10 * oz) + m11 * oxx;
+        czmin = fmin(czmin, cz);
+        czmax = fmax(czmax, cz);
+        cxmin = fmin(cxmin, cx);
+        cxmax = fmax(cxmax, cx);
+    }
+    TileGeo tg;
+    tg.z = make_axis((f0 + m00 * (double)oz0) + m01 * (double)ox0, m00, m01);
+    tg.x = make_axis((f1 + m10 * (double)oz0) + m11 * (double)ox0, m10, m11);
+    tg.box_z0 = tg.box_x0 = tg.box_zn = tg.box_xn = 0;
+    tg.interior = 0;
+    tg.pad = 0;
+    if (!(czmax < -0.01 || czmin > nz - 1 + 0.01 || cxmax < -0.01 || cxmin > nx - 1 + 0.01)) {
+        long long zlo = tap_start_d<ORDER>(czmin) - 1, zhi = tap_start_d<ORDER>(czmax) + ORDER + 1;
+        long long xlo = tap_start_d<ORDER>(cxmin) - 1, xhi = tap_start_d<ORDER>(cxmax) + ORDER + 1;
+        zlo = zlo < 0 ? 0 : zlo;
+        xlo = xlo < 0 ? 0 : xlo;
+        zhi = zhi > nz - 1 ? nz - 1 : zhi;
+        xhi = xhi > nx - 1 ? nx - 1 : xhi;
+        const long long zn = zhi - zlo + 1, xn = xhi - xlo + 1;
+        if (zn > RY_BOX || xn > RY_BOX) {
+            atomicOr(R.status, DEVCHK_BOX_OVERFLOW);
+        } else if (zn > 0 && xn > 0) {
+            tg.box_z0 = (short)zlo;
+            tg.box_x0 = (short)xlo;
+            tg.box_zn = (short)zn;
+            tg.box_xn = (short)xn;
+            // every output of the tile well inside and every tap of every
+            // output within [0, n-1]: no checks and no mirroring needed
+            tg.interior = (czmin >= 2.0 && czmax <= nz - 3.0 && cxmin >= 2.0 && cxmax <= nx - 3.0 &&
+                           ozB == oz0 + RY_T - 1 && oxB == ox0 + RY_T - 1)
+                              ? 1
+                              : 0;
+        }
+    }
+    tiles[id] = tg;
+}
+
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// Issue the footprint copy of one (angle, tile) into `buf`.
+__device__ __forceinline__ void stage_box(const TileGeo &tg, const float2 *plane, int nx, float2 *buf)
+{
+    const int zn = tg.box_zn, xn = tg.box_xn;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int zi = ty; zi < zn; zi += 8) {
+        const float2 *row = plane + (size_t)(tg.box_z0 + zi) * nx + tg.box_x0;
+        for (int xi = tx; xi < xn; xi += 32)
+            cp_async8(buf + zi * RY_BP + xi, row + xi);
+    }
+}
+
+__device__ __forceinline__ TileGeo load_tile(const TileGeo *p)
+{
+    TileGeo t;
+    const int4 *s = reinterpret_cast<const int4 *>(p);
+    int4 *d = reinterpret_cast<int4 *>(&t);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        d[k] = __ldg(s + k);
+    return t;
+}
 
 template <int ORDER, bool ONLYREAL>
-__global__ void __launch_bounds__(256) k_rotate_y(RotParams R, const float2 *__restrict__ slab,
-                                                  const double *__restrict__ geo, void *volume, float2 *comp)
+__global__ void __launch_bounds__(256, 3) k_rotate_y(RotParams R, const float2 *__restrict__ slab,
+                                                     const double *__restrict__ geo,
+                                                     const TileGeo *__restrict__ tiles, void *volume,
+                                                     float2 *comp)
 {
-    __shared__ float2 box[RY_BOX * RY_BP];
-    __shared__ double sg[6];
-    __shared__ AxisCoord sax[2];  // z, x coordinates at the tile origin
-    __shared__ int si[4];         // box z0, box x0, box nz (<=0: skip), box nx
+    __shared__ float2 box[2][RY_BOX * RY_BP];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int ntx = (R.nx + RY_T - 1) / RY_T, ntz = (R.nz + RY_T - 1) / RY_T;
+    const int tile = blockIdx.y * ntx + blockIdx.x;
     const int ox0 = blockIdx.x * RY_T, oz0 = blockIdx.y * RY_T, y = blockIdx.z;
     const int nx = R.nx, nz = R.nz, ny = R.ny;
     const int ox = ox0 + tx;
-    float2 s[4], cp[4];
+    const int nb = R.nbatch_angles;
+    const size_t plane_stride = (size_t)nz * nx;
+    float2 s[4], cp[4], part[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         s[q] = make_float2(0.f, 0.f);
         cp[q] = make_float2(0.f, 0.f);
+        part[q] = make_float2(0.f, 0.f);
     }
-    for (int a = 0; a < R.nbatch_angles; ++a) {
-        if (threadIdx.x == 0) {
-            const double *g = geo + 6 * (size_t)a;
-            const double m00 = g[0], m01 = g[1], m10 = g[2], m11 = g[3], f0 = g[4], f1 = g[5];
-            for (int k = 0; k < 6; ++k)
-                sg[k] = g[k];
-            const int ozB = min(oz0 + RY_T - 1, nz - 1), oxB = min(ox0 + RY_T - 1, nx - 1);
-            double czmin = DBL_MAX, czmax = -DBL_MAX, cxmin = DBL_MAX, cxmax = -DBL_MAX;
-            for (int k = 0; k < 4; ++k) {
-                const double oz = (k & 1) ? ozB : oz0, oxx = (k & 2) ? oxB : ox0;
-                const double cz = (f0 + m00 * oz) + m01 * oxx, cx = (f1 + m10 * oz) + m11 * oxx;
-                czmin = fmin(czmin, cz);
-                czmax = fmax(czmax, cz);
-                cxmin = fmin(cxmin, cx);
-                cxmax = fmax(cxmax, cx);
-            }
-            int zn = 0, xn = 0, z0 = 0, x0 = 0;
-            if (!(czmax < -0.01 || czmin > nz - 1 + 0.01 || cxmax < -0.01 || cxmin > nx - 1 + 0.01)) {
-                long long zlo = tap_start_d<ORDER>(czmin) - 1, zhi = tap_start_d<ORDER>(czmax) + ORDER + 1;
-                long long xlo = tap_start_d<ORDER>(cxmin) - 1, xhi = tap_start_d<ORDER>(cxmax) + ORDER + 1;
-                zlo = zlo < 0 ? 0 : zlo;
-                xlo = xlo < 0 ? 0 : xlo;
-                zhi = zhi > nz - 1 ? nz - 1 : zhi;
-                xhi = xhi > nx - 1 ? nx - 1 : xhi;
-                z0 = (int)zlo;
-                x0 = (int)xlo;
-                zn = (int)(zhi - zlo + 1);
-                xn = (int)(xhi - xlo + 1);
-                if (zn > RY_BOX || xn > RY_BOX) {
-                    atomicOr(R.status, DEVCHK_BOX_OVERFLOW);
-                    zn = 0;
-                }
-            }
-            const double cz0 = (f0 + m00 * (double)oz0) + m01 * (double)ox0;
-            const double cx0 = (f1 + m10 * (double)oz0) + m11 * (double)ox0;
-            sax[0] = make_axis(cz0, m00, m01);
-            sax[1] = make_axis(cx0, m10, m11);
-            si[0] = z0;
-            si[1] = x0;
-            si[2] = zn;
-            si[3] = xn;
+    TileGeo cur = load_tile(tiles + (size_t)0 * ntz * ntx + tile);
+    if (cur.box_zn > 0)
+        stage_box(cur, slab + ((size_t)0 * ny + y) * plane_stride, nx, box[0]);
+    cp_async_commit();
+    const float dx = (float)(ox - ox0);
+    for (int a = 0; a < nb; ++a) {
+        TileGeo nxt;
+        if (a + 1 < nb) {
+            nxt = load_tile(tiles + (size_t)(a + 1) * ntz * ntx + tile);
+            if (nxt.box_zn > 0)
+                stage_box(nxt, slab + ((size_t)(a + 1) * ny + y) * plane_stride, nx, box[(a + 1) & 1]);
         }
+        cp_async_commit();
+        cp_async_wait<1>();
         __syncthreads();
-        const int zn = si[2];
-        if (zn > 0) {
-            const int bz0 = si[0], bx0 = si[1], xn = si[3];
-            const float2 *plane = slab + ((size_t)a * ny + y) * (size_t)nz * nx;
-            for (int zi = ty; zi < zn; zi += 8) {
-                const float2 *row = plane + (size_t)(bz0 + zi) * nx + bx0;
-                for (int xi = tx; xi < xn; xi += 32)
-                    box[zi * RY_BP + xi] = __ldg(row + xi);
-            }
-            __syncthreads();
-            const AxisCoord az = sax[0], ax = sax[1];
-            const float dx = (float)(ox - ox0);
+        if (cur.box_zn > 0) {
+            const float2 *b = box[a & 1];
+            const int bz0 = cur.box_z0, bx0 = cur.box_x0;
+            const bool interior = cur.interior != 0;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int oz = oz0 + ty + 8 * q;
@@ -281,27 +355,34 @@ __global__ void __launch_bounds__(256) k_rotate_y(RotParams R, const float2 *__r
                     continue;
                 const float dz = (float)(oz - oz0);
                 int Iz, Ix;
-                const float lz = eval_axis(az, dz, dx, Iz);
-                const float lx = eval_axis(ax, dz, dx, Ix);
-                const bool in_z = inside_axis(lz, Iz, nz, [&] {
-                    return __dadd_rn(__dadd_rn(sg[4], __dmul_rn(sg[0], (double)oz)), __dmul_rn(sg[1], (double)ox));
-                });
-                if (!in_z)
-                    continue;
-                const bool in_x = inside_axis(lx, Ix, nx, [&] {
-                    return __dadd_rn(__dadd_rn(sg[5], __dmul_rn(sg[2], (double)oz)), __dmul_rn(sg[3], (double)ox));
-                });
-                if (!in_x)
-                    continue;
+                const float lz = eval_axis(cur.z, dz, dx, Iz);
+                const float lx = eval_axis(cur.x, dz, dx, Ix);
+                if (!interior) {
+                    const double *g = geo + 6 * (size_t)a;
+                    const bool in_z = inside_axis(lz, Iz, nz, [&] {
+                        return __dadd_rn(__dadd_rn(__ldg(g + 4), __dmul_rn(__ldg(g + 0), (double)oz)),
+                                         __dmul_rn(__ldg(g + 1), (double)ox));
+                    });
+                    if (!in_z)
+                        continue;
+                    const bool in_x = inside_axis(lx, Ix, nx, [&] {
+                        return __dadd_rn(__dadd_rn(__ldg(g + 5), __dmul_rn(__ldg(g + 2), (double)oz)),
+                                         __dmul_rn(__ldg(g + 3), (double)ox));
+                    });
+                    if (!in_x)
+                        continue;
+                }
                 int tz0, tx0;
                 float wz[ORDER + 1], wx[ORDER + 1];
                 if (ORDER == 0) {
-                    // nearest neighbour: the rounding point is a discontinuity,
-                    // so take the tap from the exact FP64 coordinate
-                    const double cz = __dadd_rn(__dadd_rn(sg[4], __dmul_rn(sg[0], (double)oz)),
-                                                __dmul_rn(sg[1], (double)ox));
-                    const double cx = __dadd_rn(__dadd_rn(sg[5], __dmul_rn(sg[2], (double)oz)),
-                                                __dmul_rn(sg[3], (double)ox));
+                    // nearest neighbour: the rounding point is a
+                    // discontinuity, so take the tap from the exact FP64
+                    // coordinate
+                    const double *g = geo + 6 * (size_t)a;
+                    const double cz = __dadd_rn(__dadd_rn(__ldg(g + 4), __dmul_rn(__ldg(g + 0), (double)oz)),
+                                                __dmul_rn(__ldg(g + 1), (double)ox));
+                    const double cx = __dadd_rn(__dadd_rn(__ldg(g + 5), __dmul_rn(__ldg(g + 2), (double)oz)),
+                                                __dmul_rn(__ldg(g + 3), (double)ox));
                     tz0 = (int)floor(cz + 0.5);
                     tx0 = (int)floor(cx + 0.5);
                     wz[0] = 1.f;
@@ -310,30 +391,47 @@ __global__ void __launch_bounds__(256) k_rotate_y(RotParams R, const float2 *__r
                     tz0 = Iz + Spline<ORDER>::weights(lz, wz);
                     tx0 = Ix + Spline<ORDER>::weights(lx, wx);
                 }
-                int cx[ORDER + 1];
+                int rz[ORDER + 1], cx[ORDER + 1];
 #pragma unroll
-                for (int k = 0; k <= ORDER; ++k)
-                    cx[k] = mirror_idx(tx0 + k, nx) - bx0;
+                for (int k = 0; k <= ORDER; ++k) {
+                    if (interior) {
+                        rz[k] = (tz0 + k - bz0) * RY_BP;
+                        cx[k] = tx0 + k - bx0;
+                    } else {
+                        rz[k] = (mirror_idx(tz0 + k, nz) - bz0) * RY_BP;
+                        cx[k] = mirror_idx(tx0 + k, nx) - bx0;
+                    }
+                }
                 float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int i = 0; i <= ORDER; ++i) {
-                    const float2 *brow = box + (mirror_idx(tz0 + i, nz) - bz0) * RY_BP;
+                    const float2 *brow = b + rz[i];
                     float2 r = make_float2(0.f, 0.f);
 #pragma unroll
                     for (int k = 0; k <= ORDER; ++k) {
-                        const float2 b = brow[cx[k]];
-                        r.x = fmaf(wx[k], b.x, r.x);
+                        const float2 v = brow[cx[k]];
+                        r.x = fmaf(wx[k], v.x, r.x);
                         if (!ONLYREAL)
-                            r.y = fmaf(wx[k], b.y, r.y);
+                            r.y = fmaf(wx[k], v.y, r.y);
                     }
                     acc.x = fmaf(wz[i], r.x, acc.x);
                     if (!ONLYREAL)
                         acc.y = fmaf(wz[i], r.y, acc.y);
                 }
-                kahan_add(s[q], cp[q], acc);
+                part[q].x += acc.x;
+                part[q].y += acc.y;
+            }
+        }
+        if ((a % RY_KAHAN) == RY_KAHAN - 1 || a == nb - 1) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                kahan_add(s[q], cp[q], part[q]);
+                part[q] = make_float2(0.f, 0.f);
             }
         }
         __syncthreads();
+        if (a + 1 < nb)
+            cur = nxt;
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -444,11 +542,15 @@ __global__ void __launch_bounds__(256) k_rotate_3d(RotParams R, const float2 *__
 
 template <int ORDER, bool ONLYREAL>
 static cudaError_t rotate_impl(const RotParams &R, int tilted, const float2 *slab, const double *geo, void *volume,
-                               float2 *comp, cudaStream_t s)
+                               float2 *comp, void *scratch, cudaStream_t s)
 {
     if (!tilted) {
+        const int ntiles = ((R.nx + RY_T - 1) / RY_T) * ((R.nz + RY_T - 1) / RY_T);
+        const int nset = R.nbatch_angles * ntiles;
+        TileGeo *tiles = reinterpret_cast<TileGeo *>(scratch);
+        k_rotate_y_setup<ORDER><<<(nset + 127) / 128, 128, 0, s>>>(R, geo, tiles);
         dim3 grid((R.nx + RY_T - 1) / RY_T, (R.nz + RY_T - 1) / RY_T, R.ny);
-        k_rotate_y<ORDER, ONLYREAL><<<grid, 256, 0, s>>>(R, slab, geo, volume, comp);
+        k_rotate_y<ORDER, ONLYREAL><<<grid, 256, 0, s>>>(R, slab, geo, tiles, volume, comp);
     } else {
         dim3 grid((R.nx + 31) / 32, (R.ny + 7) / 8, R.nz);
         k_rotate_3d<ORDER, ONLYREAL><<<grid, 256, 0, s>>>(R, slab, geo, volume, comp);
@@ -456,13 +558,22 @@ static cudaError_t rotate_impl(const RotParams &R, int tilted, const float2 *sla
     return cudaGetLastError();
 }
 
-cudaError_t launch_rotate(const RotParams &R, int order, int tilted, const float2 *slab, const double *geo,
-                          void *volume, float2 *comp, cudaStream_t s)
+size_t rotate_scratch_bytes(int nbatch_angles, int ny, int nx, int nz, int tilted)
 {
-#define ODT_ROT_CASE(O)                                                              \
-    case O:                                                                          \
-        return R.onlyreal ? rotate_impl<O, true>(R, tilted, slab, geo, volume, comp, s) \
-                          : rotate_impl<O, false>(R, tilted, slab, geo, volume, comp, s);
+    (void)ny;
+    if (tilted)
+        return 0;
+    const size_t ntiles = (size_t)((nx + RY_T - 1) / RY_T) * ((nz + RY_T - 1) / RY_T);
+    return (size_t)nbatch_angles * ntiles * sizeof(TileGeo);
+}
+
+cudaError_t launch_rotate(const RotParams &R, int order, int tilted, const float2 *slab, const double *geo,
+                          void *volume, float2 *comp, void *scratch, cudaStream_t s)
+{
+#define ODT_ROT_CASE(O)                                                                       \
+    case O:                                                                                   \
+        return R.onlyreal ? rotate_impl<O, true>(R, tilted, slab, geo, volume, comp, scratch, s) \
+                          : rotate_impl<O, false>(R, tilted, slab, geo, volume, comp, scratch, s);
     switch (order) {
         ODT_ROT_CASE(0)
         ODT_ROT_CASE(1)

@@ -110,7 +110,8 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_forward(StageParams P, L 
 {
     extern __shared__ float2 smem[];
     const int n = line.size();
-    float2 *buf0 = smem, *buf1 = smem + LPC * n, *tw = smem + 2 * LPC * n;
+    const int ls = xslots(n);
+    float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
     const long long lid = (long long)blockIdx.x * LPC + l;
@@ -128,7 +129,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_forward(StageParams P, L 
     }
     __syncthreads();
     int flip = 0;
-    line.template run<-1>(v, j, buf0 + l * n, buf1 + l * n, 1, tw, flip);
+    line.template run<-1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip);
     if (!valid)
         return;
     float2 *dst = rowspec + (size_t)lid * n;
@@ -155,151 +156,241 @@ __device__ __forceinline__ bool held(const float2 (&v)[L::SLOTS], int j, int pos
     return true;
 }
 
-// ---------------------------------------------------------------------------
-// (b1) columns: forward FFT along y, filter, then for z planes p of jobs
-// q in [q0, q0+qn) (q = a*nz + p): propagator, backward FFT along y, crop.
-// T[(q-q0)][y][kx], y over the cropped height.
-template <class L, int KX>
-__global__ void __launch_bounds__(KX * L::TPL) k_columns_propagate(StageParams P, L line, const float2 *rowspec,
-                                                                   float2 *T, int q0, int qn, int ppc)
+// True when spectrum column kx can be nonzero.
+__device__ __forceinline__ bool column_active(const StageParams &P, int kx)
 {
-    extern __shared__ float2 smem[];
-    const int n = line.size();  // lNy
-    float2 *buf0 = smem, *buf1 = smem + KX * n, *tw = smem + 2 * KX * n;
-    float2 *edge = tw + n;  // [KX][4]
-    copy_twiddles<L>(tw, P.tab.twy, n);
-    const int c = threadIdx.x % KX, j = threadIdx.x / KX;
-    const int kx = blockIdx.x * KX + c;
-    const bool colok = kx < P.lNx;
-    const int lNx = P.lNx, nz = P.nz, ny = P.ny, padyl = P.padyl;
-    const int qb = q0 + blockIdx.y * ppc;
-    const int qe = min(q0 + qn, qb + ppc);
-    const bool pf = P.order >= 2;
-    const bool yfix = pf && P.tilted;
-    // y-prefilter edge positions (u at y0-1, y0+1, y1-1, y1+1)
-    const int e0 = (padyl - 1 + n) % n, e1 = (padyl + 1) % n;
-    const int e2 = (padyl + ny - 2 + n) % n, e3 = (padyl + ny) % n;
-    __syncthreads();
+    return kx < P.lNx && (kx < P.kx_zero_lo || kx >= P.kx_zero_hi);
+}
 
-    float2 Gs[L::SLOTS], E[L::SLOTS], st[L::SLOTS];
-    int flip = 0;
-    int cur_a = -1;
-    for (int q = qb; q < qe; ++q) {
-        const int a = q / nz, p = q % nz;
-        const float zp = (float)p - 0.5f * (float)nz;
-        if (a != cur_a) {
-            float2 v[L::SLOTS];
+// True when any of the KX columns starting at kx0 can be nonzero.
+template <int KX>
+__device__ __forceinline__ bool group_active(const StageParams &P, int kx0)
+{
+    return !(kx0 >= P.kx_zero_lo && kx0 + KX <= P.kx_zero_hi);
+}
+
+// ---------------------------------------------------------------------------
+// Column helpers shared by the two column kernels.  A CTA owns KX adjacent
+// spectrum columns kx; thread (c, j) holds rows ky = j + r*TPL of column c.
+
+// Column kx of angle a's row spectra, forward FFT along y, times the filter
+// table G (which includes the prefilter particular factors).
+template <class L, int KX>
+__device__ __forceinline__ void column_spectrum(const StageParams &P, const L &line, const float2 *rowspec, int a,
+                                                int kx, bool colok, int c, int j, float2 *buf0, float2 *buf1,
+                                                const float2 *tw, int &flip, float2 (&v)[L::SLOTS])
+{
+    const int n = line.size();
 #pragma unroll
-            for (int r = 0; r < L::SLOTS; ++r) {
-                const int ky = j + r * L::TPL;
-                v[r] = (colok && ky < n) ? rowspec[((size_t)a * n + ky) * lNx + kx] : make_float2(0.f, 0.f);
-            }
-            line.template run<-1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int ky = j + r * L::TPL;
+        v[r] = (colok && ky < n) ? rowspec[((size_t)a * n + ky) * P.lNx + kx] : make_float2(0.f, 0.f);
+    }
+    line.template run<-1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
 #pragma unroll
-            for (int r = 0; r < L::SLOTS; ++r) {
-                const int ky = j + r * L::TPL;
-                if (colok && ky < n) {
-                    const size_t k = (size_t)ky * lNx + kx;
-                    Gs[r] = cmul(v[r], P.tab.G[k]);
-                    E[r] = expi_phase(P.tab.wsplit[k], zp);
-                    st[r] = P.tab.step[k];
-                } else {
-                    Gs[r] = make_float2(0.f, 0.f);
-                    E[r] = make_float2(0.f, 0.f);
-                    st[r] = make_float2(0.f, 0.f);
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int ky = j + r * L::TPL;
+        v[r] = (colok && ky < n) ? cmul(v[r], P.tab.G[(size_t)ky * P.lNx + kx]) : make_float2(0.f, 0.f);
+    }
+}
+
+// Backward FFT along y of v, then the y-prefilter boundary terms (tilted
+// path, order >= 2) and the cropped store dst[yy * lNx] for yy < ny.
+template <class L, int KX>
+__device__ __forceinline__ void column_inverse_store(const StageParams &P, const L &line, float2 (&v)[L::SLOTS],
+                                                     int c, int j, bool colok, float2 *buf0, float2 *buf1,
+                                                     const float2 *tw, float2 *edge, int &flip, float2 *dst)
+{
+    const int n = line.size();
+    const int ny = P.ny, padyl = P.padyl;
+    line.template run<1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+    const bool yfix = P.order >= 2 && P.tilted;
+    float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
+    if (yfix) {
+        // u at y0-1, y0+1, y1-1, y1+1 (periodic over the padded height)
+        const int e0 = (padyl - 1 + n) % n, e1 = (padyl + 1) % n;
+        const int e2 = (padyl + ny - 2 + n) % n, e3 = (padyl + ny) % n;
+        float2 t;
+        if (held<L>(v, j, e0, t)) edge[c * 4 + 0] = t;
+        if (held<L>(v, j, e1, t)) edge[c * 4 + 1] = t;
+        if (held<L>(v, j, e2, t)) edge[c * 4 + 2] = t;
+        if (held<L>(v, j, e3, t)) edge[c * 4 + 3] = t;
+        __syncthreads();
+        const float2 d0 = edge[c * 4 + 0] - edge[c * 4 + 1];
+        const float2 d1 = edge[c * 4 + 3] - edge[c * 4 + 2];
+        Acoef = make_float2(P.by_ca * d0.x + P.by_cb * d1.x, P.by_ca * d0.y + P.by_cb * d1.y);
+        Bcoef = make_float2(P.by_ca * d1.x + P.by_cb * d0.x, P.by_ca * d1.y + P.by_cb * d0.y);
+    }
+    if (!colok)
+        return;
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int yy = j + r * L::TPL - padyl;
+        if (yy >= 0 && yy < ny) {
+            float2 o = v[r];
+            if (yfix) {
+                if (yy < ZPOW_N) {
+                    const float zz = P.tab.zpow[yy];
+                    o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
+                }
+                if (ny - 1 - yy < ZPOW_N) {
+                    const float zz = P.tab.zpow[ny - 1 - yy];
+                    o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
                 }
             }
-            cur_a = a;
-        }
-        float2 v[L::SLOTS];
-        const bool lowb = pf && p < ZPOW_N;
-        const bool highb = pf && (nz - 1 - p) < ZPOW_N;
-        const float zl = lowb ? P.tab.zpow[p] : 0.f;
-        const float zh = highb ? P.tab.zpow[nz - 1 - p] : 0.f;
-#pragma unroll
-        for (int r = 0; r < L::SLOTS; ++r) {
-            float2 e = E[r];
-            if (lowb || highb) {
-                const int ky = j + r * L::TPL;
-                if (colok && ky < n) {
-                    const size_t k = (size_t)ky * lNx + kx;
-                    if (lowb) {
-                        const float2 al = P.tab.alpha[k];
-                        e = make_float2(fmaf(al.x, zl, e.x), fmaf(al.y, zl, e.y));
-                    }
-                    if (highb) {
-                        const float2 be = P.tab.beta[k];
-                        e = make_float2(fmaf(be.x, zh, e.x), fmaf(be.y, zh, e.y));
-                    }
-                }
-            }
-            v[r] = cmul(Gs[r], e);
-            E[r] = cmul(E[r], st[r]);
-        }
-        line.template run<1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
-        float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
-        if (yfix) {
-            float2 t;
-            if (held<L>(v, j, e0, t)) edge[c * 4 + 0] = t;
-            if (held<L>(v, j, e1, t)) edge[c * 4 + 1] = t;
-            if (held<L>(v, j, e2, t)) edge[c * 4 + 2] = t;
-            if (held<L>(v, j, e3, t)) edge[c * 4 + 3] = t;
-            __syncthreads();
-            const float2 d0 = edge[c * 4 + 0] - edge[c * 4 + 1];
-            const float2 d1 = edge[c * 4 + 3] - edge[c * 4 + 2];
-            Acoef = make_float2(P.by_ca * d0.x + P.by_cb * d1.x, P.by_ca * d0.y + P.by_cb * d1.y);
-            Bcoef = make_float2(P.by_ca * d1.x + P.by_cb * d0.x, P.by_ca * d1.y + P.by_cb * d0.y);
-        }
-        if (colok) {
-            float2 *dst = T + (size_t)(q - q0) * ny * lNx + kx;
-#pragma unroll
-            for (int r = 0; r < L::SLOTS; ++r) {
-                const int yy = j + r * L::TPL - padyl;
-                if (yy >= 0 && yy < ny) {
-                    float2 o = v[r];
-                    if (yfix) {
-                        if (yy < ZPOW_N) {
-                            const float zz = P.tab.zpow[yy];
-                            o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
-                        }
-                        if (ny - 1 - yy < ZPOW_N) {
-                            const float zz = P.tab.zpow[ny - 1 - yy];
-                            o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
-                        }
-                    }
-                    dst[(size_t)yy * lNx] = o;
-                }
-            }
+            dst[(size_t)yy * P.lNx] = o;
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// (b2) rows: backward FFT along x, x-prefilter boundary terms, crop -> slab.
+// (b0) z-prefilter boundary columns, once per angle (order >= 2).  The
+// prefiltered propagator of plane p is E_p + alpha z^p + beta z^(nz-1-p);
+// by linearity the alpha and beta parts are transformed once here
+// (Tab[a][0] = column transform of G*alpha, Tab[a][1] of G*beta) and the row
+// stage adds z^p Tab[a][0] + z^(nz-1-p) Tab[a][1] to the first and last
+// planes' rows.
+template <class L, int KX>
+__global__ void __launch_bounds__(KX * L::TPL) k_columns_boundary(StageParams P, L line, const float2 *rowspec,
+                                                                  float2 *Tab)
+{
+    if (!group_active<KX>(P, blockIdx.x * KX))
+        return;  // all-zero columns: the row stage never reads them
+    extern __shared__ float2 smem[];
+    const int n = line.size();
+    const int ls = xslots(n);
+    float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls, *edge = tw + n;
+    copy_twiddles<L>(tw, P.tab.twy, n);
+    const int c = threadIdx.x % KX, j = threadIdx.x / KX;
+    const int kx = blockIdx.x * KX + c;
+    const bool colok = kx < P.lNx;
+    const int a = blockIdx.y;
+    __syncthreads();
+    int flip = 0;
+    float2 g[L::SLOTS];
+    column_spectrum<L, KX>(P, line, rowspec, a, kx, colok, c, j, buf0, buf1, tw, flip, g);
+#pragma unroll 1
+    for (int t = 0; t < 2; ++t) {
+        const float2 *tab = t == 0 ? P.tab.alpha : P.tab.beta;
+        float2 v[L::SLOTS];
+#pragma unroll
+        for (int r = 0; r < L::SLOTS; ++r) {
+            const int ky = j + r * L::TPL;
+            v[r] = (colok && ky < n) ? cmul(g[r], tab[(size_t)ky * P.lNx + kx]) : make_float2(0.f, 0.f);
+        }
+        column_inverse_store<L, KX>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
+                                    Tab + ((size_t)(a * 2 + t) * P.ny) * P.lNx + kx);
+    }
+}
+
+// (b1) columns: for the z planes of jobs q in [q0, q0+qn) (q = a*nz + p):
+// propagator (exact anchor, then a complex recurrence whose per-element step
+// lives in shared memory), backward FFT along y, crop.  Output
+// T[q-q0][y][kx], y over the cropped height.
+template <class L, int KX>
+__global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
+    k_columns_propagate(StageParams P, L line, const float2 *rowspec, float2 *T, int q0, int qn, int ppc)
+{
+    if (!group_active<KX>(P, blockIdx.x * KX))
+        return;  // all-zero columns: the row stage never reads them
+    extern __shared__ float2 smem[];
+    const int n = line.size();  // lNy
+    const int ls = xslots(n);
+    float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls;
+    float2 *edge = tw + n;           // [KX][4]
+    float2 *stp = edge + 4 * KX;     // [n][KX] propagator step per element
+    copy_twiddles<L>(tw, P.tab.twy, n);
+    const int c = threadIdx.x % KX, j = threadIdx.x / KX;
+    const int kx = blockIdx.x * KX + c;
+    const bool colok = kx < P.lNx;
+    const int lNx = P.lNx, nz = P.nz, ny = P.ny;
+    const int qb = q0 + blockIdx.y * ppc;
+    const int qe = min(q0 + qn, qb + ppc);
+    __syncthreads();
+
+    float2 V[L::SLOTS];  // G * exp(i w z_p) for this thread's elements
+    int flip = 0;
+    int cur_a = -1;
+    int a = qb / nz, p = qb % nz;
+    for (int q = qb; q < qe; ++q, ++p) {
+        if (p == nz) {
+            p = 0;
+            ++a;
+        }
+        if (a != cur_a) {
+            column_spectrum<L, KX>(P, line, rowspec, a, kx, colok, c, j, buf0, buf1, tw, flip, V);
+            const float zp = (float)p - 0.5f * (float)nz;
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int ky = j + r * L::TPL;
+                if (colok && ky < n) {
+                    const size_t k = (size_t)ky * lNx + kx;
+                    V[r] = cmul(V[r], expi_phase(P.tab.wsplit[k], zp));
+                    stp[ky * KX + c] = P.tab.step[k];
+                }
+            }
+            cur_a = a;
+        }
+        float2 v[L::SLOTS];
+#pragma unroll
+        for (int r = 0; r < L::SLOTS; ++r) {
+            v[r] = V[r];
+            const int ky = j + r * L::TPL;
+            if (ky < n)
+                V[r] = cmul(V[r], stp[ky * KX + c]);
+        }
+        column_inverse_store<L, KX>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
+                                    T + (size_t)(q - q0) * ny * lNx + kx);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// (b2) rows: (+ z-boundary rows), backward FFT along x, x-prefilter boundary
+// terms, crop -> slab.
 template <class L, int LPC>
 __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L line, const float2 *T,
-                                                               float2 *slab, int q0, int qn)
+                                                               const float2 *Tab, float2 *slab, int q0, int qn)
 {
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNx
-    float2 *buf0 = smem, *buf1 = smem + LPC * n, *tw = smem + 2 * LPC * n;
+    const int ls = xslots(n);
+    float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
     float2 *edge = tw + n;  // [LPC][4]
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
     const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl;
     const long long rid = (long long)blockIdx.x * LPC + l;
     const bool valid = rid < (long long)qn * ny;
-    float2 v[L::SLOTS];
+    const int qq = q0 + (int)((valid ? rid : 0) / ny);
+    const int y = (int)((valid ? rid : 0) % ny);
+    const int a = qq / nz, p = qq % nz;
+    const bool pf = P.order >= 2;
+    const float zl = (pf && p < ZPOW_N) ? P.tab.zpow[p] : 0.f;
+    const float zh = (pf && nz - 1 - p < ZPOW_N) ? P.tab.zpow[nz - 1 - p] : 0.f;
     const float2 *src = T + (size_t)(valid ? rid : 0) * n;
+    const float2 *ta = Tab + ((size_t)(a * 2 + 0) * ny + y) * n;
+    const float2 *tb = Tab + ((size_t)(a * 2 + 1) * ny + y) * n;
+    float2 v[L::SLOTS];
 #pragma unroll
     for (int r = 0; r < L::SLOTS; ++r) {
         const int x = j + r * L::TPL;
-        v[r] = (valid && x < n) ? src[x] : make_float2(0.f, 0.f);
+        float2 t = make_float2(0.f, 0.f);
+        if (valid && column_active(P, x)) {
+            t = __ldcs(src + x);  // read once: evict first
+            if (zl != 0.f) {
+                const float2 u = ta[x];
+                t = make_float2(fmaf(zl, u.x, t.x), fmaf(zl, u.y, t.y));
+            }
+            if (zh != 0.f) {
+                const float2 u = tb[x];
+                t = make_float2(fmaf(zh, u.x, t.x), fmaf(zh, u.y, t.y));
+            }
+        }
+        v[r] = t;
     }
     __syncthreads();
     int flip = 0;
-    line.template run<1>(v, j, buf0 + l * n, buf1 + l * n, 1, tw, flip);
-    const bool pf = P.order >= 2;
+    line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip);
     float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
     if (pf) {
         const int e0 = (padxl - 1 + n) % n, e1 = (padxl + 1) % n;
@@ -317,9 +408,6 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
     }
     if (!valid)
         return;
-    const int qq = q0 + (int)(rid / ny);
-    const int y = (int)(rid % ny);
-    const int a = qq / nz, p = qq % nz;
     size_t base;
     if (P.tilted)
         base = (((size_t)a * nz + p) * ny + y) * nx;
@@ -341,7 +429,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
                     o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
                 }
             }
-            dst[xx] = o;
+            __stcs(dst + xx, o);  // streamed: keep L2 for the column stage output
         }
     }
 }
@@ -360,9 +448,15 @@ struct Cfg<GenericLine> {
 };
 
 template <class L>
-static size_t smem_rows(int n) { return (size_t)(2 * Cfg<L>::LPC * n + n + 4 * Cfg<L>::LPC) * sizeof(float2); }
+static size_t smem_rows(int n)
+{
+    return (size_t)(2 * Cfg<L>::LPC * xslots(n) + n + 4 * Cfg<L>::LPC) * sizeof(float2);
+}
 template <class L>
-static size_t smem_cols(int n) { return (size_t)(2 * Cfg<L>::KX * n + n + 4 * Cfg<L>::KX) * sizeof(float2); }
+static size_t smem_cols(int n)
+{
+    return (size_t)(2 * Cfg<L>::KX * xslots(n) + Cfg<L>::KX * n + n + 4 * Cfg<L>::KX) * sizeof(float2);
+}
 
 constexpr int kPlanesPerColumnBlock = 16;
 
@@ -378,6 +472,16 @@ static cudaError_t rows_forward_impl(const StageParams &P, L line, const void *s
 }
 
 template <class L>
+static cudaError_t boundary_impl(const StageParams &P, L line, const float2 *rowspec, float2 *Tab, int nb,
+                                 cudaStream_t s)
+{
+    constexpr int KX = Cfg<L>::KX;
+    dim3 grid((P.lNx + KX - 1) / KX, nb);
+    k_columns_boundary<L, KX><<<grid, KX * L::TPL, smem_cols<L>(line.n), s>>>(P, line, rowspec, Tab);
+    return cudaGetLastError();
+}
+
+template <class L>
 static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rowspec, float2 *T, int q0, int qn,
                                 cudaStream_t s)
 {
@@ -389,13 +493,13 @@ static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rows
 }
 
 template <class L>
-static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 *T, float2 *slab, int q0, int qn,
-                                     cudaStream_t s)
+static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 *T, const float2 *Tab,
+                                     float2 *slab, int q0, int qn, cudaStream_t s)
 {
     constexpr int LPC = Cfg<L>::LPC;
     const long long lines = (long long)qn * P.ny;
     const unsigned grid = (unsigned)((lines + LPC - 1) / LPC);
-    k_rows_inverse<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, slab, q0, qn);
+    k_rows_inverse<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, Tab, slab, q0, qn);
     return cudaGetLastError();
 }
 
@@ -414,6 +518,10 @@ static cudaError_t set_smem_attrs(int n)
         return e;
     e = cudaFuncSetAttribute(k_rows_inverse<L, Cfg<L>::LPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem_rows<L>(n));
+    if (e != cudaSuccess)
+        return e;
+    e = cudaFuncSetAttribute(k_columns_boundary<L, Cfg<L>::KX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_cols<L>(n));
     if (e != cudaSuccess)
         return e;
     return cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -469,10 +577,16 @@ cudaError_t launch_columns_propagate(const StageParams &P, const float2 *rowspec
     return with_line(P.lNy, [&](auto line) { return columns_impl(P, line, rowspec, T, q0, qn, s); });
 }
 
-cudaError_t launch_rows_inverse(const StageParams &P, const float2 *T, float2 *slab, int q0, int qn,
-                                cudaStream_t s)
+cudaError_t launch_columns_boundary(const StageParams &P, const float2 *rowspec, float2 *Tab, int nb,
+                                    cudaStream_t s)
 {
-    return with_line(P.lNx, [&](auto line) { return rows_inverse_impl(P, line, T, slab, q0, qn, s); });
+    return with_line(P.lNy, [&](auto line) { return boundary_impl(P, line, rowspec, Tab, nb, s); });
+}
+
+cudaError_t launch_rows_inverse(const StageParams &P, const float2 *T, const float2 *Tab, float2 *slab, int q0,
+                                int qn, cudaStream_t s)
+{
+    return with_line(P.lNx, [&](auto line) { return rows_inverse_impl(P, line, T, Tab, slab, q0, qn, s); });
 }
 
 }  // namespace odt
