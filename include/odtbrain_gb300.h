@@ -138,6 +138,27 @@ odt_status odt_bpp3d_execute_timed(const odt_bpp3d_plan *plan,
 odt_status odt_bpp3d_launch_count(const odt_bpp3d_plan *plan,
                                   int64_t *launches);
 
+/* Bytes of the library's static device scratch used by
+ * odt_bpp3d_execute_noalloc. */
+#define ODT_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+/* odt_bpp3d_execute without a workspace argument and without allocating:
+ * for callers that cannot allocate device memory when they reconstruct (a
+ * cudaMalloc there would synchronise the device, is forbidden while a stream
+ * is captured, or the application's allocator owns all device memory).  The
+ * scratch is a 64 MiB array in the library's device image, held by every
+ * device that loads the library's device code until the process exits.
+ * Plans whose workspace exceeds ODT_NOALLOC_SCRATCH_BYTES are rejected
+ * (ODT_ERR_INVALID_ARGUMENT): create them with desc.workspace_limit <=
+ * ODT_NOALLOC_SCRATCH_BYTES.  The first call on a device looks the array's
+ * address up (make that call before any stream capture); all calls on a
+ * device share the array, so calls whose executions overlap on the GPU race.
+ * No counterpart in the reference. */
+odt_status odt_bpp3d_execute_noalloc(const odt_bpp3d_plan *plan,
+                                     const void *sino, const double *weights,
+                                     const double *geometry, void *volume,
+                                     void *stream);
+
 /* Wait for `stream`, then return ODT_ERR_DEVICE_CHECK if any kernel of this
  * plan recorded a failed internal check since the last call (the status word
  * is cleared). */

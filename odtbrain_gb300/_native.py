@@ -20,6 +20,8 @@ ODT_ERR_DEVICE_CHECK = 5
 ODT_PAD_NONE, ODT_PAD_EDGE, ODT_PAD_RAMP = 0, 1, 2
 ODT_GEOM_Y_AXIS, ODT_GEOM_AFFINE3D = 0, 1
 ODT_INPUT_C64, ODT_INPUT_C128 = 0, 1
+# size of the static scratch of odt_bpp3d_execute_noalloc
+NOALLOC_SCRATCH_BYTES = 64 << 20
 
 # every symbol include/odtbrain_gb300.h declares
 EXPORTED_SYMBOLS = (
@@ -29,6 +31,7 @@ EXPORTED_SYMBOLS = (
     "odt_bpp3d_execute",
     "odt_bpp3d_execute_timed",
     "odt_bpp3d_launch_count",
+    "odt_bpp3d_execute_noalloc",
     "odt_bpp3d_read_status",
     "odt_bpp3d_plan_destroy",
     "odt_status_string",
@@ -118,11 +121,13 @@ def lib():
                                               ctypes.POINTER(StageTiming)]
         L.odt_bpp3d_launch_count.argtypes = [vp,
                                              ctypes.POINTER(ctypes.c_int64)]
+        L.odt_bpp3d_execute_noalloc.argtypes = [vp, vp, vp, vp, vp, vp]
         L.odt_bpp3d_read_status.argtypes = [vp, vp]
         L.odt_bpp3d_plan_destroy.argtypes = [vp]
         for name in ("odt_bpp3d_plan_create", "odt_bpp3d_workspace_size",
                      "odt_bpp3d_angle_batch", "odt_bpp3d_execute",
                      "odt_bpp3d_execute_timed", "odt_bpp3d_launch_count",
+                     "odt_bpp3d_execute_noalloc",
                      "odt_bpp3d_read_status", "odt_bpp3d_plan_destroy"):
             getattr(L, name).restype = ctypes.c_int
         L.odt_status_string.argtypes = [ctypes.c_int]

@@ -12,6 +12,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -594,3 +595,69 @@ odt_status odt_bpp3d_plan_destroy(odt_bpp3d_plan *plan)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Execution without allocation.
+//
+// Some callers cannot allocate device memory when they run a
+// reconstruction: code inside a region where a cudaMalloc would stall the
+// device or is not allowed (a latency-critical acquisition loop, a stream
+// that is being captured, a framework that owns every byte of device
+// memory and only hands out pointers to its own tensors).  For them the
+// execution below takes its scratch space from a fixed array that is part of
+// the library's device image instead of a caller-provided workspace.
+//
+// * The array is ODT_NOALLOC_SCRATCH_BYTES (64 MiB) per device; every device
+//   on which the library's device code is loaded holds it until the process
+//   exits.  Plans whose workspace is larger are rejected: create the plan
+//   with desc.workspace_limit <= ODT_NOALLOC_SCRATCH_BYTES.
+// * The first call on a device looks up the array's device address
+//   (cudaGetSymbolAddress) with that device current, once; make that first
+//   call before any stream capture.
+// * Every call on a device uses the same array and leaves its contents
+//   behind; nothing in it has to start at zero (each stage writes what the
+//   next reads).  Calls whose executions overlap on the GPU race on it: run
+//   them on one stream, or order them.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[ODT_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_addr[kMaxDevices];
+}  // namespace
+
+extern "C" odt_status odt_bpp3d_execute_noalloc(const odt_bpp3d_plan *plan, const void *sino,
+                                                const double *weights, const double *geometry, void *volume,
+                                                void *stream)
+{
+    if (!plan)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "NULL plan");
+    if (plan->ws_bytes > ODT_NOALLOC_SCRATCH_BYTES) {
+        char buf[200];
+        snprintf(buf, sizeof buf,
+                 "plan needs %llu bytes of scratch, the static scratch holds %llu; create the plan with "
+                 "workspace_limit <= %llu",
+                 (unsigned long long)plan->ws_bytes, (unsigned long long)ODT_NOALLOC_SCRATCH_BYTES,
+                 (unsigned long long)ODT_NOALLOC_SCRATCH_BYTES);
+        return fail(ODT_ERR_INVALID_ARGUMENT, buf);
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices)
+        return fail(ODT_ERR_UNSUPPORTED, "device ordinal beyond the static scratch table");
+    void *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_addr[dev]) {
+            e = cudaGetSymbolAddress(&g_noalloc_addr[dev], g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                g_noalloc_addr[dev] = nullptr;
+                return cuda_fail(e, "cudaGetSymbolAddress of the static scratch");
+            }
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    return run_plan(plan, sino, weights, geometry, volume, scratch, stream, nullptr);
+}
