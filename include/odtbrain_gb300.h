@@ -107,6 +107,34 @@ odt_status odt_bpp3d_execute(const odt_bpp3d_plan *plan, const void *sino,
                              const double *weights, const double *geometry,
                              void *volume, void *workspace, void *stream);
 
+/* odt_bpp3d_execute with a real per-frequency gain multiplying the filter:
+ * gain is a device array of pad_ny*pad_nx floats in the filter's [ky][kx]
+ * FFT order (NULL: no gain).  The gain is the learnable input of the
+ * differentiable reconstruction; no counterpart in the reference. */
+odt_status odt_bpp3d_execute_gain(const odt_bpp3d_plan *plan, const void *sino,
+                                  const double *weights,
+                                  const double *geometry, const float *gain,
+                                  void *volume, void *workspace, void *stream);
+
+/* Bytes of device workspace odt_bpp3d_adjoint needs (y-axis plans). */
+odt_status odt_bpp3d_adjoint_workspace_size(const odt_bpp3d_plan *plan,
+                                            uint64_t *bytes);
+
+/* Vector-Jacobian product of odt_bpp3d_execute_gain (y-axis geometry,
+ * complex output).  Given the volume cotangent vol_grad (nx, ny, nx)
+ * complex64, writes
+ *   sino_grad (A, ny, nx) complex64 = J_sino^H vol_grad       (may be NULL)
+ *   gain_grad pad_ny*pad_nx float   = Re(J_gain^H vol_grad)   (may be NULL;
+ *                                     needs `sino`, overwritten)
+ * The transpose of every stage is computed, not stored: the spectra are
+ * recomputed from `sino` when the gain gradient is asked for.  No counterpart
+ * in the reference (which has no derivatives). */
+odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino,
+                             const double *weights, const double *geometry,
+                             const float *gain, const void *vol_grad,
+                             void *sino_grad, float *gain_grad,
+                             void *workspace, void *stream);
+
 /* Per-stage record of one execution, for measurement. */
 enum odt_stage {
     ODT_STAGE_ROWS_FORWARD = 0,      /* (a) pad, weight, forward FFT along x */

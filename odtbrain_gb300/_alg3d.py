@@ -239,6 +239,76 @@ class Backprop3D:
             self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
         return out
 
+    def forward_gain(self, sino, gain=None, out=None, check=True):
+        """Reconstruct with a real per-frequency gain (lNy, lNx) float32 on
+        the device multiplying the filter (None: no gain)."""
+        torch = _torch()
+        out, stream, args = self._args(sino, out)
+        gptr = ctypes.c_void_p(0)
+        if gain is not None:
+            g = self._check_gain(gain)
+            gptr = ctypes.c_void_p(g.data_ptr())
+        self.plan.execute_gain(args[0], args[1], args[2], gptr, args[3],
+                               args[4], args[5])
+        if check:
+            self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
+        return out
+
+    def gain_shape(self):
+        g = self.padding_geometry
+        return (g["lNy"], g["lNx"])
+
+    def _check_gain(self, gain):
+        torch = _torch()
+        if (not gain.is_cuda or gain.dtype != torch.float32
+                or tuple(gain.shape) != self.gain_shape()
+                or not gain.is_contiguous()):
+            raise ValueError("gain must be a contiguous float32 CUDA tensor "
+                             "of shape %s" % (self.gain_shape(),))
+        return gain
+
+    def adjoint(self, sino, vol_grad, gain=None, need_sino=True,
+                need_gain=False):
+        """Vector-Jacobian product of :meth:`forward_gain`: returns
+        (sino_grad or None, gain_grad or None) for the volume cotangent
+        ``vol_grad`` (complex64, volume shape)."""
+        torch = _torch()
+        if self.onlyreal:
+            raise NotImplementedError("the adjoint needs onlyreal=False")
+        if (vol_grad.dtype != torch.complex64
+                or tuple(vol_grad.shape) != self.volume_shape()):
+            raise ValueError("vol_grad must be complex64 of the volume shape")
+        vol_grad = vol_grad.contiguous()
+        ws_bytes = self.plan.adjoint_workspace_bytes()
+        ws = torch.empty(max(ws_bytes, 1), device=self.device,
+                         dtype=torch.uint8)
+        sgrad = (torch.empty(self.shape, device=self.device,
+                             dtype=torch.complex64) if need_sino else None)
+        ggrad = (torch.empty(self.gain_shape(), device=self.device,
+                             dtype=torch.float32) if need_gain else None)
+        stream = torch.cuda.current_stream(self.device)
+        if need_gain:
+            _o, _s, args = self._args(sino, vol_grad)
+            sptr = args[0]
+        else:
+            sptr = ctypes.c_void_p(sino.data_ptr() if sino is not None
+                                   else 0)
+        gptr = ctypes.c_void_p(self._check_gain(gain).data_ptr()
+                               if gain is not None else 0)
+        self.plan.adjoint(
+            sptr,
+            ctypes.c_void_p(self.weights.data_ptr()
+                            if self.weights is not None else 0),
+            ctypes.c_void_p(self.geometry.data_ptr()), gptr,
+            ctypes.c_void_p(vol_grad.data_ptr()),
+            ctypes.c_void_p(sgrad.data_ptr() if sgrad is not None else 0),
+            ctypes.c_void_p(ggrad.data_ptr() if ggrad is not None else 0),
+            ctypes.c_void_p(ws.data_ptr()),
+            ctypes.c_void_p(stream.cuda_stream))
+        self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
+        del ws
+        return sgrad, ggrad
+
     def timed(self, sino, out=None):
         """Run once with a CUDA event pair around every kernel launch;
         returns per-stage {"ms", "launches", "bytes"}."""

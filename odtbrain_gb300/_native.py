@@ -32,6 +32,9 @@ EXPORTED_SYMBOLS = (
     "odt_bpp3d_execute_timed",
     "odt_bpp3d_launch_count",
     "odt_bpp3d_execute_noalloc",
+    "odt_bpp3d_execute_gain",
+    "odt_bpp3d_adjoint_workspace_size",
+    "odt_bpp3d_adjoint",
     "odt_bpp3d_read_status",
     "odt_bpp3d_plan_destroy",
     "odt_status_string",
@@ -122,12 +125,21 @@ def lib():
         L.odt_bpp3d_launch_count.argtypes = [vp,
                                              ctypes.POINTER(ctypes.c_int64)]
         L.odt_bpp3d_execute_noalloc.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.odt_bpp3d_execute_gain.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
+        L.odt_bpp3d_adjoint_workspace_size.argtypes = [
+            vp, ctypes.POINTER(ctypes.c_uint64)]
+        L.odt_bpp3d_adjoint.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                        vp]
         L.odt_bpp3d_read_status.argtypes = [vp, vp]
         L.odt_bpp3d_plan_destroy.argtypes = [vp]
         for name in ("odt_bpp3d_plan_create", "odt_bpp3d_workspace_size",
                      "odt_bpp3d_angle_batch", "odt_bpp3d_execute",
                      "odt_bpp3d_execute_timed", "odt_bpp3d_launch_count",
-                     "odt_bpp3d_execute_noalloc",
+                     "odt_bpp3d_execute_noalloc", "odt_bpp3d_execute_gain",
+                     "odt_bpp3d_adjoint_workspace_size", "odt_bpp3d_adjoint",
+    "odt_bpp3d_execute_gain",
+    "odt_bpp3d_adjoint_workspace_size",
+    "odt_bpp3d_adjoint",
                      "odt_bpp3d_read_status", "odt_bpp3d_plan_destroy"):
             getattr(L, name).restype = ctypes.c_int
         L.odt_status_string.argtypes = [ctypes.c_int]
@@ -186,6 +198,27 @@ class Plan:
             self._h, sino_ptr, weights_ptr, geometry_ptr, volume_ptr,
             workspace_ptr, stream_handle, ctypes.byref(t)))
         return t.as_dict()
+
+    def execute_gain(self, sino_ptr, weights_ptr, geometry_ptr, gain_ptr,
+                     volume_ptr, workspace_ptr, stream_handle):
+        check(lib().odt_bpp3d_execute_gain(self._h, sino_ptr, weights_ptr,
+                                           geometry_ptr, gain_ptr,
+                                           volume_ptr, workspace_ptr,
+                                           stream_handle))
+
+    def adjoint_workspace_bytes(self):
+        ws = ctypes.c_uint64()
+        check(lib().odt_bpp3d_adjoint_workspace_size(self._h,
+                                                     ctypes.byref(ws)))
+        return int(ws.value)
+
+    def adjoint(self, sino_ptr, weights_ptr, geometry_ptr, gain_ptr,
+                vgrad_ptr, sgrad_ptr, ggrad_ptr, workspace_ptr,
+                stream_handle):
+        check(lib().odt_bpp3d_adjoint(self._h, sino_ptr, weights_ptr,
+                                      geometry_ptr, gain_ptr, vgrad_ptr,
+                                      sgrad_ptr, ggrad_ptr, workspace_ptr,
+                                      stream_handle))
 
     def read_status(self, stream_handle):
         check(lib().odt_bpp3d_read_status(self._h, stream_handle))

@@ -81,6 +81,7 @@ struct odt_bpp3d_plan {
     int batch;       // angles per batch
     int jobs;        // (angle, plane) jobs per column/row launch
     size_t off_rowspec, off_T, off_Tab, off_slab, off_comp, off_rot, ws_bytes;
+    size_t off_Qg, off_W, off_Pg, adj_ws_bytes;  // adjoint-only regions after ws_bytes
     double bx_ca, bx_cb, by_ca, by_cb;
     int kx_zero_lo, kx_zero_hi;  // all-zero spectrum columns [lo, hi)
     // device tables (one allocation)
@@ -115,6 +116,7 @@ StageParams stage_params(const odt_bpp3d_plan *p)
     P.by_ca = (float)p->by_ca;
     P.by_cb = (float)p->by_cb;
     P.tab = p->tab;
+    P.gain = nullptr;
     P.status = p->d_status;
     return P;
 }
@@ -368,8 +370,19 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
         layout(1, jobs, true);
     }
 
+    {
+        const size_t spec_b = (size_t)p->batch * lNy * lNx * 8;
+        size_t w = p->ws_bytes;
+        p->off_Qg = w; w = align_up(w + spec_b);
+        p->off_W = w; w = align_up(w + spec_b);
+        p->off_Pg = w; w = align_up(w + spec_b);
+        p->adj_ws_bytes = w;
+    }
+
     StageParams P = stage_params(p);
     e = odt::configure_kernels(P);
+    if (e == cudaSuccess && !tilted)
+        e = odt::configure_adjoint_kernels(P);
     if (e != cudaSuccess) {
         cudaFree(p->d_tables);
         delete p;
@@ -442,7 +455,7 @@ struct LaunchTimer {
 };
 
 odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *weights, const double *geometry,
-                    void *volume, void *workspace, void *stream, odt_stage_timing *timing)
+                    const float *gain, void *volume, void *workspace, void *stream, odt_stage_timing *timing)
 {
     if (!plan || !sino || !geometry || !volume || (!workspace && plan->ws_bytes))
         return fail(ODT_ERR_INVALID_ARGUMENT, "NULL pointer argument");
@@ -451,6 +464,7 @@ odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *
     const odt_bpp3d_desc &d = plan->d;
     cudaStream_t s = (cudaStream_t)stream;
     StageParams P = stage_params(plan);
+    P.gain = gain;
     char *ws = (char *)workspace;
     float2 *rowspec = (float2 *)(ws + plan->off_rowspec);
     float2 *T = (float2 *)(ws + plan->off_T);
@@ -532,7 +546,111 @@ extern "C" {
 odt_status odt_bpp3d_execute(const odt_bpp3d_plan *plan, const void *sino, const double *weights,
                              const double *geometry, void *volume, void *workspace, void *stream)
 {
-    return run_plan(plan, sino, weights, geometry, volume, workspace, stream, nullptr);
+    return run_plan(plan, sino, weights, geometry, nullptr, volume, workspace, stream, nullptr);
+}
+
+odt_status odt_bpp3d_execute_gain(const odt_bpp3d_plan *plan, const void *sino, const double *weights,
+                                  const double *geometry, const float *gain, void *volume, void *workspace,
+                                  void *stream)
+{
+    return run_plan(plan, sino, weights, geometry, gain, volume, workspace, stream, nullptr);
+}
+
+odt_status odt_bpp3d_adjoint_workspace_size(const odt_bpp3d_plan *plan, uint64_t *bytes)
+{
+    if (!plan || !bytes)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (plan->d.geometry != ODT_GEOM_Y_AXIS)
+        return fail(ODT_ERR_UNSUPPORTED, "the adjoint is implemented for the y-axis geometry");
+    *bytes = plan->adj_ws_bytes;
+    return ODT_OK;
+}
+
+odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const double *weights,
+                             const double *geometry, const float *gain, const void *vol_grad, void *sino_grad,
+                             float *gain_grad, void *workspace, void *stream)
+{
+    if (!plan || !geometry || !vol_grad || !workspace)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "NULL pointer argument");
+    if (!sino_grad && !gain_grad)
+        return ODT_OK;
+    if (gain_grad && !sino)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "the gain gradient needs the sinogram");
+    if (((uintptr_t)workspace % kAlign) != 0)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    const odt_bpp3d_desc &d = plan->d;
+    if (d.geometry != ODT_GEOM_Y_AXIS)
+        return fail(ODT_ERR_UNSUPPORTED, "the adjoint is implemented for the y-axis geometry");
+    if (d.onlyreal)
+        return fail(ODT_ERR_UNSUPPORTED, "the adjoint needs a complex (onlyreal=0) plan");
+    cudaStream_t s = (cudaStream_t)stream;
+    StageParams P = stage_params(plan);
+    P.gain = gain;
+    char *ws = (char *)workspace;
+    float2 *rowspec = (float2 *)(ws + plan->off_rowspec);
+    float2 *T = (float2 *)(ws + plan->off_T);
+    float2 *slab = (float2 *)(ws + plan->off_slab);
+    float2 *Qg = (float2 *)(ws + plan->off_Qg);
+    float2 *W = (float2 *)(ws + plan->off_W);
+    float2 *Pg = (float2 *)(ws + plan->off_Pg);
+    const size_t in_elem = d.input_dtype == ODT_INPUT_C128 ? 16 : 8;
+    const size_t spec = (size_t)d.pad_ny * d.pad_nx;
+    const int nbatches = (d.num_angles + plan->batch - 1) / plan->batch;
+    cudaError_t e;
+    if (gain_grad) {
+        e = cudaMemsetAsync(gain_grad, 0, spec * sizeof(float), s);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaMemsetAsync");
+    }
+    for (int b = 0; b < nbatches; ++b) {
+        const int a0 = b * plan->batch;
+        const int nb = std::min(plan->batch, d.num_angles - a0);
+        RotParams R;
+        R.ny = d.ny;
+        R.nx = d.nx;
+        R.nz = plan->nz;
+        R.nbatch_angles = nb;
+        R.first_pass = 1;
+        R.last_pass = 1;
+        R.onlyreal = 0;
+        R.status = plan->d_status;
+        e = odt::launch_rotate_adjoint(R, d.intp_order, 0, (const float2 *)vol_grad, geometry + (size_t)a0 * 6, slab,
+                                       s);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "rotate_adjoint launch");
+        if (gain_grad) {
+            const char *sino_b = (const char *)sino + (size_t)a0 * d.ny * d.nx * in_elem;
+            e = odt::launch_rows_forward(P, sino_b, weights ? weights + a0 : nullptr, nb, rowspec, s);
+            if (e != cudaSuccess)
+                return cuda_fail(e, "rows_forward launch");
+        }
+        e = cudaMemsetAsync(Qg, 0, (size_t)nb * spec * sizeof(float2), s);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaMemsetAsync");
+        const int total = nb * plan->nz;
+        for (int q0 = 0; q0 < total; q0 += plan->jobs) {
+            const int qn = std::min(plan->jobs, total - q0);
+            e = odt::launch_adj_rows(P, slab, T, q0, qn, s);
+            if (e != cudaSuccess)
+                return cuda_fail(e, "adj_rows launch");
+            e = odt::launch_adj_columns(P, T, Qg, q0, qn, s);
+            if (e != cudaSuccess)
+                return cuda_fail(e, "adj_columns launch");
+        }
+        e = odt::launch_adj_spectrum(P, rowspec, Qg, gain_grad, W, nb, s);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "adj_spectrum launch");
+        if (sino_grad) {
+            e = odt::launch_adj_rows_full(P, W, Pg, nb, s);
+            if (e != cudaSuccess)
+                return cuda_fail(e, "adj_rows_full launch");
+            e = odt::launch_adj_pad(P, Pg, weights ? weights + a0 : nullptr, nb,
+                                    (float2 *)sino_grad + (size_t)a0 * d.ny * d.nx, s);
+            if (e != cudaSuccess)
+                return cuda_fail(e, "adj_pad launch");
+        }
+    }
+    return ODT_OK;
 }
 
 odt_status odt_bpp3d_execute_timed(const odt_bpp3d_plan *plan, const void *sino, const double *weights,
@@ -541,7 +659,7 @@ odt_status odt_bpp3d_execute_timed(const odt_bpp3d_plan *plan, const void *sino,
 {
     if (!timing)
         return fail(ODT_ERR_INVALID_ARGUMENT, "timing is NULL");
-    return run_plan(plan, sino, weights, geometry, volume, workspace, stream, timing);
+    return run_plan(plan, sino, weights, geometry, nullptr, volume, workspace, stream, timing);
 }
 
 odt_status odt_bpp3d_launch_count(const odt_bpp3d_plan *plan, int64_t *launches)
@@ -659,5 +777,5 @@ extern "C" odt_status odt_bpp3d_execute_noalloc(const odt_bpp3d_plan *plan, cons
         }
         scratch = g_noalloc_addr[dev];
     }
-    return run_plan(plan, sino, weights, geometry, volume, scratch, stream, nullptr);
+    return run_plan(plan, sino, weights, geometry, nullptr, volume, scratch, stream, nullptr);
 }

@@ -40,6 +40,7 @@ struct StageParams {
     float bx_ca, bx_cb;  // x-prefilter boundary solve (n = nx)
     float by_ca, by_cb;  // y-prefilter boundary solve (n = ny)
     FilterTables tab;
+    const float *gain;  // optional real per-frequency gain [lNy*lNx] (NULL: 1)
     int *status;
 };
 
@@ -68,6 +69,18 @@ size_t rotate_scratch_bytes(int nbatch_angles, int ny, int nx, int nz, int tilte
 cudaError_t launch_rotate(const RotParams &R, int order, int tilted, const float2 *slab, const double *geo,
                           void *volume, float2 *comp, void *scratch, cudaStream_t s);
 cudaError_t configure_kernels(const StageParams &P);
+
+// Adjoint (adjoint.cu, rotate.cu).
+cudaError_t configure_adjoint_kernels(const StageParams &P);
+cudaError_t launch_rotate_adjoint(const RotParams &R, int order, int tilted, const float2 *vol_grad,
+                                  const double *geo, float2 *slab_grad, cudaStream_t s);
+cudaError_t launch_adj_rows(const StageParams &P, const float2 *sgrad, float2 *Tg, int q0, int qn, cudaStream_t s);
+cudaError_t launch_adj_columns(const StageParams &P, const float2 *Tg, float2 *Qg, int q0, int qn, cudaStream_t s);
+cudaError_t launch_adj_spectrum(const StageParams &P, const float2 *rowspec, const float2 *Qg, float *dgain,
+                                float2 *W, int nb, cudaStream_t s);
+cudaError_t launch_adj_rows_full(const StageParams &P, const float2 *W, float2 *Pg, int nb, cudaStream_t s);
+cudaError_t launch_adj_pad(const StageParams &P, const float2 *Pg, const double *weights, int nb, float2 *dsino,
+                           cudaStream_t s);
 bool line_size_supported(int n);
 
 }  // namespace odt

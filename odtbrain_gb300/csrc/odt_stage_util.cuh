@@ -1,0 +1,155 @@
+// Device helpers and launch-shape policy shared by the filter stages
+// (stages.cu) and their adjoints (adjoint.cu).
+#pragma once
+#include <type_traits>
+
+#include "odt_fft.cuh"
+#include "odt_internal.cuh"
+
+namespace odt {
+
+// exp(i * w * z) with w held as (hi, lo) floats and z a small half-integer:
+// exact product hi*z via FMA, Cody-Waite reduction by 2*pi, then sincosf.
+__device__ __forceinline__ float2 expi_phase(float2 w, float z)
+{
+    const float ph = w.x * z;
+    const float err = fmaf(w.x, z, -ph);
+    const float lo = fmaf(w.y, z, err);
+    const float k = rintf(ph * 0.15915494309189535f);
+    float r = fmaf(-k, 6.28125f, ph);
+    r = fmaf(-k, 1.9353071795864769253e-3f, r);
+    r += lo;
+    float s, c;
+    sincosf(r, &s, &c);
+    return make_float2(c, s);
+}
+
+__device__ __forceinline__ float2 load_sino(const void *sino, int in_c128, size_t idx, double w)
+{
+    if (in_c128) {
+        const double2 v = reinterpret_cast<const double2 *>(sino)[idx];
+        return make_float2((float)(v.x * w), (float)(v.y * w));
+    }
+    const float2 v = reinterpret_cast<const float2 *>(sino)[idx];
+    const float wf = (float)w;
+    return make_float2(v.x * wf, v.y * wf);
+}
+
+// np.pad linear_ramp value at ramp position i of `width` (i = 0 is the
+// outer edge): end + (edge - end) * i / width  (numpy linspace, endpoint
+// False).
+__device__ __forceinline__ float2 ramp(float2 edge, float2 end, int i, int width)
+{
+    const float t = (float)i / (float)width;
+    return make_float2(fmaf(edge.x - end.x, t, end.x), fmaf(edge.y - end.y, t, end.y));
+}
+
+// Padded, weighted sample (y, x) of the padded plane of angle row `arow`
+// (odtbrain/_alg3d_bpp.py:493-506: np.pad pads y first, then x).
+__device__ __forceinline__ float2 padded_sample(const StageParams &P, const void *sino, size_t arow, double w, int y, int x)
+{
+    const int ny = P.ny, nx = P.nx;
+    if (P.pad_mode == 0)
+        return load_sino(sino, P.in_c128, arow + (size_t)y * nx + x, w);
+    const int ys = y - P.padyl, xs = x - P.padxl;
+    if (P.pad_mode == 1) {
+        const int yc = min(max(ys, 0), ny - 1), xc = min(max(xs, 0), nx - 1);
+        return load_sino(sino, P.in_c128, arow + (size_t)yc * nx + xc, w);
+    }
+    const int padyr = P.lNy - ny - P.padyl, padxr = P.lNx - nx - P.padxl;
+    auto colval = [&](int xc) -> float2 {
+        if (ys >= 0 && ys < ny)
+            return load_sino(sino, P.in_c128, arow + (size_t)ys * nx + xc, w);
+        if (ys < 0)
+            return ramp(load_sino(sino, P.in_c128, arow + xc, w), P.padval, y, P.padyl);
+        const int jdx = ys - ny;
+        return ramp(load_sino(sino, P.in_c128, arow + (size_t)(ny - 1) * nx + xc, w), P.padval,
+                    padyr - 1 - jdx, padyr);
+    };
+    if (xs >= 0 && xs < nx)
+        return colval(xs);
+    if (xs < 0)
+        return ramp(colval(0), P.padval, x, P.padxl);
+    return ramp(colval(nx - 1), P.padval, padxr - 1 - (xs - nx), padxr);
+}
+
+template <class L>
+__device__ __forceinline__ void copy_twiddles(float2 *dst, const float2 *src, int n)
+{
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        dst[i] = src[i];
+}
+
+
+// Select v[pos / TPL] of the thread holding position `pos` without dynamic
+// register indexing; returns true when this thread holds it.
+template <class L>
+__device__ __forceinline__ bool held(const float2 (&v)[L::SLOTS], int j, int pos, float2 &out)
+{
+    if (pos % L::TPL != j)
+        return false;
+    const int rr = pos / L::TPL;
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r)
+        if (r == rr)
+            out = v[r];
+    return true;
+}
+
+// True when spectrum column kx can be nonzero.
+__device__ __forceinline__ bool column_active(const StageParams &P, int kx)
+{
+    return kx < P.lNx && (kx < P.kx_zero_lo || kx >= P.kx_zero_hi);
+}
+
+// True when any of the KX columns starting at kx0 can be nonzero.
+template <int KX>
+__device__ __forceinline__ bool group_active(const StageParams &P, int kx0)
+{
+    return !(kx0 >= P.kx_zero_lo && kx0 + KX <= P.kx_zero_hi);
+}
+
+// ---------------------------------------------------------------------------
+// Dispatch on the line length.
+template <class L>
+struct Cfg {
+    static constexpr int LPC = (L::TPL >= 256) ? 1 : 256 / L::TPL;
+    static constexpr int KX = (L::TPL >= 512) ? 1 : ((512 / L::TPL) > 16 ? 16 : 512 / L::TPL);
+};
+template <>
+struct Cfg<GenericLine> {
+    static constexpr int LPC = 4;
+    static constexpr int KX = 4;
+};
+
+template <class L>
+inline size_t smem_rows(int n)
+{
+    return (size_t)(2 * Cfg<L>::LPC * xslots(n) + n + 4 * Cfg<L>::LPC) * sizeof(float2);
+}
+template <class L>
+inline size_t smem_cols(int n)
+{
+    return (size_t)(2 * Cfg<L>::KX * xslots(n) + Cfg<L>::KX * n + n + 4 * Cfg<L>::KX) * sizeof(float2);
+}
+
+// Calls fn(line) with the line type for length n.
+template <class F>
+inline cudaError_t with_line(int n, F &&fn)
+{
+    switch (n) {
+    case 64: return fn(Pow2Line<64>{64});
+    case 128: return fn(Pow2Line<128>{128});
+    case 256: return fn(Pow2Line<256>{256});
+    case 512: return fn(Pow2Line<512>{512});
+    case 1024: return fn(Pow2Line<1024>{1024});
+    case 2048: return fn(Pow2Line<2048>{2048});
+    case 4096: return fn(Pow2Line<4096>{4096});
+    default:
+        if (n >= 1 && n <= GenericLine::TPL * GenericLine::SLOTS)
+            return fn(GenericLine{n});
+        return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace odt

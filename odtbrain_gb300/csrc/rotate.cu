@@ -585,4 +585,147 @@ cudaError_t launch_rotate(const RotParams &R, int order, int tilted, const float
 #undef ODT_ROT_CASE
 }
 
+// ---------------------------------------------------------------------------
+// Transpose of the y-axis resampling (the backward pass): for every
+// coefficient (iz, ix) of plane y and every angle a of the batch,
+//   slab_grad[a][y][iz][ix] = sum_o beta(c_z(o) - tz) beta(c_x(o) - tx)
+//                                   * vol_grad[o_z][y][o_x]
+// over the outputs o whose coordinate c(o) is inside the domain and whose
+// (unmirrored) taps tz, tx mirror onto (iz, ix).  beta is the centred
+// B-spline of the order, so beta(c - t) is exactly the forward weight of tap
+// t (and zero for non-taps).  The outputs that can reach a tap lie in the
+// rotated support square around o* = R^T (t - off); they are enumerated and
+// tested.  In/out decisions use the forward's FP64 rule.
+template <int ORDER>
+__device__ __forceinline__ float bspline_weight(float u)
+{
+    const float a = fabsf(u);
+    if (ORDER == 1)
+        return a < 1.f ? 1.f - a : 0.f;
+    if (ORDER == 2) {
+        if (a < 0.5f)
+            return 0.75f - a * a;
+        if (a < 1.5f) {
+            const float b = 1.5f - a;
+            return 0.5f * b * b;
+        }
+        return 0.f;
+    }
+    if (ORDER == 3) {
+        if (a < 1.f)
+            return (2.f / 3.f) - a * a + 0.5f * a * a * a;
+        if (a < 2.f) {
+            const float b = 2.f - a;
+            return b * b * b * (1.f / 6.f);
+        }
+        return 0.f;
+    }
+    return 0.f;
+}
+
+// Unmirrored tap positions that mirror onto index i (orders <= 3 reach one
+// position below 0 and up to two above n-1).
+template <int ORDER>
+__device__ __forceinline__ int virtual_taps(int i, int n, int *t)
+{
+    int k = 0;
+    t[k++] = i;
+    if (n >= 2) {
+        if (i == 1)
+            t[k++] = -1;
+        if (i == n - 2)
+            t[k++] = n;
+        if (ORDER == 3 && i == n - 3 && n >= 3)
+            t[k++] = n + 1;
+    }
+    return k;
+}
+
+template <int ORDER>
+__global__ void __launch_bounds__(256) k_rotate_y_adjoint(RotParams R, const float2 *__restrict__ vgrad,
+                                                          const double *__restrict__ geo, float2 *__restrict__ sgrad)
+{
+    const int ix = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int iz = blockIdx.y * 8 + (threadIdx.x >> 5);
+    const int y = blockIdx.z;
+    const int nx = R.nx, nz = R.nz, ny = R.ny;
+    if (ix >= nx || iz >= nz)
+        return;
+    int tzs[3], txs[3];
+    const int ntz = virtual_taps<ORDER>(iz, nz, tzs);
+    const int ntx = virtual_taps<ORDER>(ix, nx, txs);
+    const double supp = 0.5 * (ORDER + 1);
+    for (int a = 0; a < R.nbatch_angles; ++a) {
+        const double *g = geo + 6 * (size_t)a;
+        const double m00 = __ldg(g + 0), m01 = __ldg(g + 1), m10 = __ldg(g + 2), m11 = __ldg(g + 3);
+        const double f0 = __ldg(g + 4), f1 = __ldg(g + 5);
+        const float m00f = (float)m00, m01f = (float)m01, m10f = (float)m10, m11f = (float)m11;
+        const double rz = supp * (fabs(m00) + fabs(m01)), rx = supp * (fabs(m10) + fabs(m11));
+        float2 acc = make_float2(0.f, 0.f);
+        for (int u = 0; u < ntz; ++u) {
+            for (int v = 0; v < ntx; ++v) {
+                const double tz = (double)tzs[u], tx = (double)txs[v];
+                // o* = R^T (t - off)
+                const double dz = tz - f0, dx = tx - f1;
+                const double ozc = m00 * dz + m10 * dx, oxc = m01 * dz + m11 * dx;
+                const int oz_lo = max(0, (int)ceil(ozc - rz - 1e-9)), oz_hi = min(nz - 1, (int)floor(ozc + rz + 1e-9));
+                const int ox_lo = max(0, (int)ceil(oxc - rx - 1e-9)), ox_hi = min(nx - 1, (int)floor(oxc + rx + 1e-9));
+                for (int oz = oz_lo; oz <= oz_hi; ++oz) {
+                    for (int ox = ox_lo; ox <= ox_hi; ++ox) {
+                        float uz, ux;
+                        double cz = 0.0, cx = 0.0;
+                        bool exact = ORDER == 0;
+                        if (!exact) {
+                            // c(o) - t = R (o - o*)
+                            const float ez = (float)((double)oz - ozc), ex = (float)((double)ox - oxc);
+                            uz = fmaf(m01f, ex, m00f * ez);
+                            ux = fmaf(m11f, ex, m10f * ez);
+                            const float cze = (float)tz + uz, cxe = (float)tx + ux;
+                            exact = cze < kGuard || cze > (float)(nz - 1) - kGuard || cxe < kGuard ||
+                                    cxe > (float)(nx - 1) - kGuard;
+                        }
+                        if (exact) {
+                            cz = __dadd_rn(__dadd_rn(f0, __dmul_rn(m00, (double)oz)), __dmul_rn(m01, (double)ox));
+                            cx = __dadd_rn(__dadd_rn(f1, __dmul_rn(m10, (double)oz)), __dmul_rn(m11, (double)ox));
+                            if (cz < 0.0 || cz > (double)(nz - 1) || cx < 0.0 || cx > (double)(nx - 1))
+                                continue;
+                            if (ORDER == 0) {
+                                if (floor(cz + 0.5) != tz || floor(cx + 0.5) != tx)
+                                    continue;
+                                uz = ux = 0.f;
+                            } else {
+                                uz = (float)(cz - tz);
+                                ux = (float)(cx - tx);
+                            }
+                        }
+                        const float w = ORDER == 0 ? 1.f : bspline_weight<ORDER>(uz) * bspline_weight<ORDER>(ux);
+                        if (w == 0.f)
+                            continue;
+                        const float2 gv = __ldg(vgrad + ((size_t)oz * ny + y) * nx + ox);
+                        acc.x = fmaf(w, gv.x, acc.x);
+                        acc.y = fmaf(w, gv.y, acc.y);
+                    }
+                }
+            }
+        }
+        sgrad[(((size_t)a * ny + y) * nz + iz) * nx + ix] = acc;
+    }
+}
+
+cudaError_t launch_rotate_adjoint(const RotParams &R, int order, int tilted, const float2 *vol_grad,
+                                  const double *geo, float2 *slab_grad, cudaStream_t s)
+{
+    if (tilted)
+        return cudaErrorNotSupported;
+    dim3 grid((R.nx + 31) / 32, (R.nz + 7) / 8, R.ny);
+    switch (order) {
+    case 0: k_rotate_y_adjoint<0><<<grid, 256, 0, s>>>(R, vol_grad, geo, slab_grad); break;
+    case 1: k_rotate_y_adjoint<1><<<grid, 256, 0, s>>>(R, vol_grad, geo, slab_grad); break;
+    case 2: k_rotate_y_adjoint<2><<<grid, 256, 0, s>>>(R, vol_grad, geo, slab_grad); break;
+    case 3: k_rotate_y_adjoint<3><<<grid, 256, 0, s>>>(R, vol_grad, geo, slab_grad); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace odt

@@ -149,3 +149,19 @@ def test_oracle_weights_match_reference(golden):
         stem = k[:-len("__angles")]
         got = O.compute_angle_weights_1d(g[k])
         assert np.array_equal(got, g[stem + "__w"]), stem
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_dense_model_matches_oracle(order):
+    """The dense FP64 torch model (used to check the adjoint with autograd)
+    reproduces the oracle."""
+    import torch
+    from dense_model import DenseBackprop
+    rng = np.random.default_rng(40 + order)
+    A, n = 5, 12
+    angles = np.sort(rng.uniform(0, 2 * np.pi, A))
+    sino = rng.normal(0, .3, (A, n, n)) + 1j * rng.normal(0, 1, (A, n, n))
+    model = DenseBackprop(angles, n, n, 3.0, 1.333, order=order)
+    got = model(torch.from_numpy(sino)).numpy()
+    ref = O.backpropagate_3d(sino, angles, 3.0, 1.333, intp_order=order)
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
