@@ -107,14 +107,18 @@ odt_status odt_bpp3d_execute(const odt_bpp3d_plan *plan, const void *sino,
                              const double *weights, const double *geometry,
                              void *volume, void *workspace, void *stream);
 
-/* odt_bpp3d_execute with a real per-frequency gain multiplying the filter:
- * gain is a device array of pad_ny*pad_nx floats in the filter's [ky][kx]
- * FFT order (NULL: no gain).  The gain is the learnable input of the
- * differentiable reconstruction; no counterpart in the reference. */
+/* odt_bpp3d_execute with gains multiplying the filter, both in the
+ * filter's [ky][kx] FFT order (NULL: none):
+ *   gain        device, pad_ny*pad_nx floats, shared by all angles
+ *   angle_gain  device, A*pad_ny*pad_nx complex64, one map per angle (the
+ *               learned filter's output)
+ * The gains are the learnable inputs of the differentiable reconstruction;
+ * no counterpart in the reference. */
 odt_status odt_bpp3d_execute_gain(const odt_bpp3d_plan *plan, const void *sino,
                                   const double *weights,
                                   const double *geometry, const float *gain,
-                                  void *volume, void *workspace, void *stream);
+                                  const void *angle_gain, void *volume,
+                                  void *workspace, void *stream);
 
 /* Bytes of device workspace odt_bpp3d_adjoint needs (y-axis plans). */
 odt_status odt_bpp3d_adjoint_workspace_size(const odt_bpp3d_plan *plan,
@@ -122,17 +126,19 @@ odt_status odt_bpp3d_adjoint_workspace_size(const odt_bpp3d_plan *plan,
 
 /* Vector-Jacobian product of odt_bpp3d_execute_gain (y-axis geometry,
  * complex output).  Given the volume cotangent vol_grad (nx, ny, nx)
- * complex64, writes
- *   sino_grad (A, ny, nx) complex64 = J_sino^H vol_grad       (may be NULL)
- *   gain_grad pad_ny*pad_nx float   = Re(J_gain^H vol_grad)   (may be NULL;
- *                                     needs `sino`, overwritten)
- * The transpose of every stage is computed, not stored: the spectra are
- * recomputed from `sino` when the gain gradient is asked for.  No counterpart
- * in the reference (which has no derivatives). */
+ * complex64, writes (each may be NULL)
+ *   sino_grad       (A, ny, nx) complex64 = J_sino^H vol_grad
+ *   gain_grad       pad_ny*pad_nx float   = Re(J_gain^H vol_grad)
+ *   angle_gain_grad A*pad_ny*pad_nx complex64 = J_angle_gain^H vol_grad
+ * The gain gradients need `sino`.  The transpose of every stage is
+ * computed, not stored: the spectra are recomputed from `sino` when a gain
+ * gradient is asked for.  No counterpart in the reference (which has no
+ * derivatives). */
 odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino,
                              const double *weights, const double *geometry,
-                             const float *gain, const void *vol_grad,
-                             void *sino_grad, float *gain_grad,
+                             const float *gain, const void *angle_gain,
+                             const void *vol_grad, void *sino_grad,
+                             float *gain_grad, void *angle_gain_grad,
                              void *workspace, void *stream);
 
 /* Per-stage record of one execution, for measurement. */
@@ -186,6 +192,52 @@ odt_status odt_bpp3d_execute_noalloc(const odt_bpp3d_plan *plan,
                                      const void *sino, const double *weights,
                                      const double *geometry, void *volume,
                                      void *stream);
+
+/* ---- Learned filter gain ------------------------------------------------
+ * A 4-layer MLP (4 -> 64 -> 64 -> 64 -> 2, SiLU, BF16 operands, FP32
+ * accumulation on the tensor cores) that maps, for every angle a and padded
+ * spectrum position (ky, kx), the features (2*kx/pad_nx, 2*ky/pad_ny in
+ * fftfreq order, angle_features[2a], angle_features[2a+1]) to the complex
+ * gain 1 + out_re + i*out_im, the angle_gain of odt_bpp3d_execute_gain.
+ * No counterpart in the reference (its filter is fixed). */
+typedef struct odt_mlp_params {
+    const void *w1;   /* bf16 [64][16]: layer 1, columns 4..15 zero         */
+    const void *w2;   /* bf16 [64][64]                                       */
+    const void *w3;   /* bf16 [64][64]                                       */
+    const void *w4;   /* bf16 [8][64]: rows 2..7 zero                        */
+    const void *w2t;  /* bf16 [64][64]: transpose of w2 (training only)      */
+    const void *w3t;  /* bf16 [64][64]: transpose of w3 (training only)      */
+    const void *w4t;  /* bf16 [64][16]: transpose of w4, columns 8..15 zero  */
+    const float *b1, *b2, *b3;  /* [64]                                      */
+    const float *b4;            /* [8]: entries 2..7 zero                     */
+} odt_mlp_params;             /* all pointers device, 16-byte aligned        */
+
+typedef struct odt_mlp_grads {  /* FP32, the weights' shapes; added to (+=)  */
+    float *w1, *w2, *w3, *w4;
+    float *b1, *b2, *b3, *b4;   /* rows / entries of padding stay untouched  */
+} odt_mlp_grads;
+
+/* gain: complex64 [num_angles][pad_ny][pad_nx]; angle_features: float
+ * [num_angles][2]. */
+odt_status odt_mlp_gain_forward(const odt_mlp_params *params,
+                                int32_t num_angles, int32_t pad_ny,
+                                int32_t pad_nx, const float *angle_features,
+                                void *gain, void *stream);
+
+/* Device bytes of the activation store odt_mlp_gain_backward needs. */
+odt_status odt_mlp_store_size(int32_t num_angles, int32_t pad_ny,
+                              int32_t pad_nx, uint64_t *bytes);
+
+/* Gradients of a real loss with respect to the MLP parameters, given the
+ * loss gradient with respect to the gain (complex64, PyTorch's convention
+ * d/dRe + i d/dIm, e.g. the angle_gain_grad of odt_bpp3d_adjoint).  Recomputes
+ * the forward; `store` (256-byte aligned, odt_mlp_store_size bytes) holds the
+ * activations between the two kernels. */
+odt_status odt_mlp_gain_backward(const odt_mlp_params *params,
+                                 int32_t num_angles, int32_t pad_ny,
+                                 int32_t pad_nx, const float *angle_features,
+                                 const void *gain_grad, void *store,
+                                 const odt_mlp_grads *grads, void *stream);
 
 /* Wait for `stream`, then return ODT_ERR_DEVICE_CHECK if any kernel of this
  * plan recorded a failed internal check since the last call (the status word

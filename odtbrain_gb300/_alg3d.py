@@ -137,6 +137,7 @@ class Backprop3D:
         g = geom.padding_geometry(lny, lnx, padding, padfac)
         self.padding_geometry = g
         angles = np.asarray(angles)
+        self.angles = angles
         if tilted_axis is None:
             kind = _native.ODT_GEOM_Y_AXIS
             if weights is None and weight_angles:
@@ -215,10 +216,17 @@ class Backprop3D:
                              (self.input_dtype, self.shape))
         if not sino.is_contiguous():
             raise ValueError("sinogram must be contiguous")
+        vdtype = torch.float32 if self.onlyreal else torch.complex64
         if out is None:
             out = torch.empty(self.volume_shape(), device=self.device,
-                              dtype=torch.float32 if self.onlyreal
-                              else torch.complex64)
+                              dtype=vdtype)
+        elif (not out.is_cuda or out.device != self.device
+              or out.dtype != vdtype
+              or tuple(out.shape) != self.volume_shape()
+              or not out.is_contiguous()):
+            raise ValueError("out must be a contiguous %s tensor of shape %s "
+                             "on %s" % (vdtype, self.volume_shape(),
+                                        self.device))
         stream = torch.cuda.current_stream(self.device)
         args = (ctypes.c_void_p(sino.data_ptr()),
                 ctypes.c_void_p(self.weights.data_ptr()
@@ -239,17 +247,18 @@ class Backprop3D:
             self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
         return out
 
-    def forward_gain(self, sino, gain=None, out=None, check=True):
-        """Reconstruct with a real per-frequency gain (lNy, lNx) float32 on
-        the device multiplying the filter (None: no gain)."""
-        torch = _torch()
+    def forward_gain(self, sino, gain=None, angle_gain=None, out=None,
+                     check=True):
+        """Reconstruct with gains multiplying the filter: ``gain`` a real
+        (lNy, lNx) float32 map shared by all angles, ``angle_gain`` a
+        complex64 (A, lNy, lNx) map per angle (None: no gain)."""
         out, stream, args = self._args(sino, out)
-        gptr = ctypes.c_void_p(0)
-        if gain is not None:
-            g = self._check_gain(gain)
-            gptr = ctypes.c_void_p(g.data_ptr())
-        self.plan.execute_gain(args[0], args[1], args[2], gptr, args[3],
-                               args[4], args[5])
+        gptr = ctypes.c_void_p(self._check_gain(gain).data_ptr()
+                               if gain is not None else 0)
+        aptr = ctypes.c_void_p(self._check_angle_gain(angle_gain).data_ptr()
+                               if angle_gain is not None else 0)
+        self.plan.execute_gain(args[0], args[1], args[2], gptr, aptr,
+                               args[3], args[4], args[5])
         if check:
             self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
         return out
@@ -267,11 +276,22 @@ class Backprop3D:
                              "of shape %s" % (self.gain_shape(),))
         return gain
 
+    def _check_angle_gain(self, ag):
+        torch = _torch()
+        shape = (self.shape[0],) + self.gain_shape()
+        if (not ag.is_cuda or ag.dtype != torch.complex64
+                or tuple(ag.shape) != shape or not ag.is_contiguous()):
+            raise ValueError("angle_gain must be a contiguous complex64 CUDA "
+                             "tensor of shape %s" % (shape,))
+        return ag
+
     def adjoint(self, sino, vol_grad, gain=None, need_sino=True,
-                need_gain=False):
+                need_gain=False, angle_gain=None, need_angle_gain=False):
         """Vector-Jacobian product of :meth:`forward_gain`: returns
-        (sino_grad or None, gain_grad or None) for the volume cotangent
-        ``vol_grad`` (complex64, volume shape)."""
+        (sino_grad, gain_grad) -- or (sino_grad, gain_grad,
+        angle_gain_grad) when ``need_angle_gain`` -- for the volume cotangent
+        ``vol_grad`` (complex64, volume shape); entries not asked for are
+        None."""
         torch = _torch()
         if self.onlyreal:
             raise NotImplementedError("the adjoint needs onlyreal=False")
@@ -286,8 +306,11 @@ class Backprop3D:
                              dtype=torch.complex64) if need_sino else None)
         ggrad = (torch.empty(self.gain_shape(), device=self.device,
                              dtype=torch.float32) if need_gain else None)
+        aggrad = (torch.empty((self.shape[0],) + self.gain_shape(),
+                              device=self.device, dtype=torch.complex64)
+                  if need_angle_gain else None)
         stream = torch.cuda.current_stream(self.device)
-        if need_gain:
+        if need_gain or need_angle_gain:
             _o, _s, args = self._args(sino, vol_grad)
             sptr = args[0]
         else:
@@ -295,18 +318,19 @@ class Backprop3D:
                                    else 0)
         gptr = ctypes.c_void_p(self._check_gain(gain).data_ptr()
                                if gain is not None else 0)
+        aptr = ctypes.c_void_p(self._check_angle_gain(angle_gain).data_ptr()
+                               if angle_gain is not None else 0)
+
+        def ptr(t):
+            return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
         self.plan.adjoint(
-            sptr,
-            ctypes.c_void_p(self.weights.data_ptr()
-                            if self.weights is not None else 0),
-            ctypes.c_void_p(self.geometry.data_ptr()), gptr,
-            ctypes.c_void_p(vol_grad.data_ptr()),
-            ctypes.c_void_p(sgrad.data_ptr() if sgrad is not None else 0),
-            ctypes.c_void_p(ggrad.data_ptr() if ggrad is not None else 0),
-            ctypes.c_void_p(ws.data_ptr()),
+            sptr, ptr(self.weights), ptr(self.geometry), gptr, aptr,
+            ptr(vol_grad), ptr(sgrad), ptr(ggrad), ptr(aggrad), ptr(ws),
             ctypes.c_void_p(stream.cuda_stream))
         self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
         del ws
+        if need_angle_gain:
+            return sgrad, ggrad, aggrad
         return sgrad, ggrad
 
     def timed(self, sino, out=None):

@@ -37,6 +37,9 @@ EXPORTED_SYMBOLS = (
     "odt_bpp3d_adjoint",
     "odt_bpp3d_read_status",
     "odt_bpp3d_plan_destroy",
+    "odt_mlp_gain_forward",
+    "odt_mlp_store_size",
+    "odt_mlp_gain_backward",
     "odt_status_string",
     "odt_last_error",
 )
@@ -70,6 +73,20 @@ class Bpp3dDesc(ctypes.Structure):
         ("kz_phase", ctypes.POINTER(ctypes.c_double)),
         ("workspace_limit", ctypes.c_uint64),
     ]
+
+
+class MlpParams(ctypes.Structure):
+    """odt_mlp_params: device pointers of the BF16 weights (and transposes)
+    and FP32 biases of the learned-gain MLP."""
+    _fields_ = [(n, ctypes.c_void_p) for n in
+                ("w1", "w2", "w3", "w4", "w2t", "w3t", "w4t",
+                 "b1", "b2", "b3", "b4")]
+
+
+class MlpGrads(ctypes.Structure):
+    """odt_mlp_grads: FP32 device gradient buffers (accumulated)."""
+    _fields_ = [(n, ctypes.c_void_p) for n in
+                ("w1", "w2", "w3", "w4", "b1", "b2", "b3", "b4")]
 
 
 STAGE_NAMES = ("rows_forward", "columns_propagate", "rows_inverse",
@@ -125,22 +142,29 @@ def lib():
         L.odt_bpp3d_launch_count.argtypes = [vp,
                                              ctypes.POINTER(ctypes.c_int64)]
         L.odt_bpp3d_execute_noalloc.argtypes = [vp, vp, vp, vp, vp, vp]
-        L.odt_bpp3d_execute_gain.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
+        L.odt_bpp3d_execute_gain.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp,
+                                             vp]
         L.odt_bpp3d_adjoint_workspace_size.argtypes = [
             vp, ctypes.POINTER(ctypes.c_uint64)]
-        L.odt_bpp3d_adjoint.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp,
-                                        vp]
+        L.odt_bpp3d_adjoint.argtypes = [vp] * 12
         L.odt_bpp3d_read_status.argtypes = [vp, vp]
         L.odt_bpp3d_plan_destroy.argtypes = [vp]
+        i32 = ctypes.c_int32
+        L.odt_mlp_gain_forward.argtypes = [ctypes.POINTER(MlpParams), i32,
+                                           i32, i32, vp, vp, vp]
+        L.odt_mlp_store_size.argtypes = [i32, i32, i32,
+                                         ctypes.POINTER(ctypes.c_uint64)]
+        L.odt_mlp_gain_backward.argtypes = [
+            ctypes.POINTER(MlpParams), i32, i32, i32, vp, vp, vp,
+            ctypes.POINTER(MlpGrads), vp]
         for name in ("odt_bpp3d_plan_create", "odt_bpp3d_workspace_size",
                      "odt_bpp3d_angle_batch", "odt_bpp3d_execute",
                      "odt_bpp3d_execute_timed", "odt_bpp3d_launch_count",
                      "odt_bpp3d_execute_noalloc", "odt_bpp3d_execute_gain",
                      "odt_bpp3d_adjoint_workspace_size", "odt_bpp3d_adjoint",
-    "odt_bpp3d_execute_gain",
-    "odt_bpp3d_adjoint_workspace_size",
-    "odt_bpp3d_adjoint",
-                     "odt_bpp3d_read_status", "odt_bpp3d_plan_destroy"):
+                     "odt_bpp3d_read_status", "odt_bpp3d_plan_destroy",
+                     "odt_mlp_gain_forward", "odt_mlp_store_size",
+                     "odt_mlp_gain_backward"):
             getattr(L, name).restype = ctypes.c_int
         L.odt_status_string.argtypes = [ctypes.c_int]
         L.odt_status_string.restype = ctypes.c_char_p
@@ -200,9 +224,9 @@ class Plan:
         return t.as_dict()
 
     def execute_gain(self, sino_ptr, weights_ptr, geometry_ptr, gain_ptr,
-                     volume_ptr, workspace_ptr, stream_handle):
+                     again_ptr, volume_ptr, workspace_ptr, stream_handle):
         check(lib().odt_bpp3d_execute_gain(self._h, sino_ptr, weights_ptr,
-                                           geometry_ptr, gain_ptr,
+                                           geometry_ptr, gain_ptr, again_ptr,
                                            volume_ptr, workspace_ptr,
                                            stream_handle))
 
@@ -213,11 +237,12 @@ class Plan:
         return int(ws.value)
 
     def adjoint(self, sino_ptr, weights_ptr, geometry_ptr, gain_ptr,
-                vgrad_ptr, sgrad_ptr, ggrad_ptr, workspace_ptr,
-                stream_handle):
+                again_ptr, vgrad_ptr, sgrad_ptr, ggrad_ptr, aggrad_ptr,
+                workspace_ptr, stream_handle):
         check(lib().odt_bpp3d_adjoint(self._h, sino_ptr, weights_ptr,
-                                      geometry_ptr, gain_ptr, vgrad_ptr,
-                                      sgrad_ptr, ggrad_ptr, workspace_ptr,
+                                      geometry_ptr, gain_ptr, again_ptr,
+                                      vgrad_ptr, sgrad_ptr, ggrad_ptr,
+                                      aggrad_ptr, workspace_ptr,
                                       stream_handle))
 
     def read_status(self, stream_handle):

@@ -210,7 +210,8 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_columns(StageParams P, L li
 // spectra), then W = IFFT_y(conj(G g) Q) for every padded row.
 template <class L, int KX>
 __global__ void __launch_bounds__(KX * L::TPL) k_adj_spectrum(StageParams P, L line, const float2 *rowspec,
-                                                              const float2 *Qg, float *dgain, float2 *W)
+                                                              const float2 *Qg, float *dgain, float2 *dagain,
+                                                              float2 *W)
 {
     if (!group_active<KX>(P, blockIdx.x * KX))
         return;
@@ -226,7 +227,8 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_spectrum(StageParams P, L l
     __syncthreads();
     int flip = 0;
     float2 X[L::SLOTS];
-    if (dgain) {
+    const bool need_x = dgain || dagain;
+    if (need_x) {
 #pragma unroll
         for (int r = 0; r < L::SLOTS; ++r) {
             const int ky = j + r * L::TPL;
@@ -243,13 +245,22 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_spectrum(StageParams P, L l
             const size_t k = (size_t)ky * lNx + kx;
             const float2 q = Qg[((size_t)a * n + ky) * lNx + kx];
             const float2 G = P.tab.G[k];
+            const float gk = P.gain ? P.gain[k] : 1.f;
+            const size_t ak = (size_t)a * n * lNx + k;
+            const float2 ga = P.again ? P.again[ak] : make_float2(1.f, 0.f);
             if (dgain) {
-                const float2 gx = cmul(G, X[r]);
+                // d/dg of G g ga X: Re(conj(G ga X) q)
+                const float2 gx = cmul(cmul(G, ga), X[r]);
                 atomicAdd(dgain + k, gx.x * q.x + gx.y * q.y);
             }
-            const float gk = P.gain ? P.gain[k] : 1.f;
-            // conj(G g) q
-            v[r] = make_float2(gk * (G.x * q.x + G.y * q.y), gk * (G.x * q.y - G.y * q.x));
+            if (dagain) {
+                // d/d(ga) of G g ga X: conj(G g X) q
+                const float2 gx = cscale(cmul(G, X[r]), gk);
+                dagain[ak] = make_float2(gx.x * q.x + gx.y * q.y, gx.x * q.y - gx.y * q.x);
+            }
+            // conj(G g ga) q
+            const float2 h = cscale(cmul(G, ga), gk);
+            v[r] = make_float2(h.x * q.x + h.y * q.y, h.x * q.y - h.y * q.x);
         }
     }
     line.template run<1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
@@ -405,13 +416,14 @@ cudaError_t launch_adj_columns(const StageParams &P, const float2 *Tg, float2 *Q
 }
 
 cudaError_t launch_adj_spectrum(const StageParams &P, const float2 *rowspec, const float2 *Qg, float *dgain,
-                                float2 *W, int nb, cudaStream_t s)
+                                float2 *dagain, float2 *W, int nb, cudaStream_t s)
 {
     return with_line(P.lNy, [&](auto line) {
         using L = decltype(line);
         constexpr int KX = Cfg<L>::KX;
         dim3 grid((P.lNx + KX - 1) / KX, nb);
-        k_adj_spectrum<L, KX><<<grid, KX * L::TPL, smem_adj_cols<L>(line.n), s>>>(P, line, rowspec, Qg, dgain, W);
+        k_adj_spectrum<L, KX><<<grid, KX * L::TPL, smem_adj_cols<L>(line.n), s>>>(P, line, rowspec, Qg, dgain,
+                                                                                 dagain, W);
         return cudaGetLastError();
     });
 }

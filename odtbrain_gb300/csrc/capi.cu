@@ -75,6 +75,11 @@ double fftfreq_rad(int k, int n)
 
 }  // namespace
 
+int odt::set_error(int status, const char *msg)
+{
+    return (int)fail((odt_status)status, msg ? msg : "");
+}
+
 struct odt_bpp3d_plan {
     odt_bpp3d_desc d;
     int nz;
@@ -117,6 +122,7 @@ StageParams stage_params(const odt_bpp3d_plan *p)
     P.by_cb = (float)p->by_cb;
     P.tab = p->tab;
     P.gain = nullptr;
+    P.again = nullptr;
     P.status = p->d_status;
     return P;
 }
@@ -455,7 +461,8 @@ struct LaunchTimer {
 };
 
 odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *weights, const double *geometry,
-                    const float *gain, void *volume, void *workspace, void *stream, odt_stage_timing *timing)
+                    const float *gain, const void *again, void *volume, void *workspace, void *stream,
+                    odt_stage_timing *timing)
 {
     if (!plan || !sino || !geometry || !volume || (!workspace && plan->ws_bytes))
         return fail(ODT_ERR_INVALID_ARGUMENT, "NULL pointer argument");
@@ -465,6 +472,7 @@ odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *
     cudaStream_t s = (cudaStream_t)stream;
     StageParams P = stage_params(plan);
     P.gain = gain;
+    const size_t spec_elems = (size_t)plan->d.pad_ny * plan->d.pad_nx;
     char *ws = (char *)workspace;
     float2 *rowspec = (float2 *)(ws + plan->off_rowspec);
     float2 *T = (float2 *)(ws + plan->off_T);
@@ -486,6 +494,7 @@ odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *
         const int a0 = b * plan->batch;
         const int nb = std::min(plan->batch, d.num_angles - a0);
         const char *sino_b = (const char *)sino + (size_t)a0 * d.ny * d.nx * in_elem;
+        P.again = again ? (const float2 *)again + (size_t)a0 * spec_elems : nullptr;
         lt.begin(ODT_STAGE_ROWS_FORWARD);
         e = odt::launch_rows_forward(P, sino_b, weights ? weights + a0 : nullptr, nb, rowspec, s);
         if (e != cudaSuccess)
@@ -546,14 +555,14 @@ extern "C" {
 odt_status odt_bpp3d_execute(const odt_bpp3d_plan *plan, const void *sino, const double *weights,
                              const double *geometry, void *volume, void *workspace, void *stream)
 {
-    return run_plan(plan, sino, weights, geometry, nullptr, volume, workspace, stream, nullptr);
+    return run_plan(plan, sino, weights, geometry, nullptr, nullptr, volume, workspace, stream, nullptr);
 }
 
 odt_status odt_bpp3d_execute_gain(const odt_bpp3d_plan *plan, const void *sino, const double *weights,
-                                  const double *geometry, const float *gain, void *volume, void *workspace,
-                                  void *stream)
+                                  const double *geometry, const float *gain, const void *angle_gain,
+                                  void *volume, void *workspace, void *stream)
 {
-    return run_plan(plan, sino, weights, geometry, gain, volume, workspace, stream, nullptr);
+    return run_plan(plan, sino, weights, geometry, gain, angle_gain, volume, workspace, stream, nullptr);
 }
 
 odt_status odt_bpp3d_adjoint_workspace_size(const odt_bpp3d_plan *plan, uint64_t *bytes)
@@ -567,14 +576,15 @@ odt_status odt_bpp3d_adjoint_workspace_size(const odt_bpp3d_plan *plan, uint64_t
 }
 
 odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const double *weights,
-                             const double *geometry, const float *gain, const void *vol_grad, void *sino_grad,
-                             float *gain_grad, void *workspace, void *stream)
+                             const double *geometry, const float *gain, const void *angle_gain,
+                             const void *vol_grad, void *sino_grad, float *gain_grad, void *angle_gain_grad,
+                             void *workspace, void *stream)
 {
     if (!plan || !geometry || !vol_grad || !workspace)
         return fail(ODT_ERR_INVALID_ARGUMENT, "NULL pointer argument");
-    if (!sino_grad && !gain_grad)
+    if (!sino_grad && !gain_grad && !angle_gain_grad)
         return ODT_OK;
-    if (gain_grad && !sino)
+    if ((gain_grad || angle_gain_grad) && !sino)
         return fail(ODT_ERR_INVALID_ARGUMENT, "the gain gradient needs the sinogram");
     if (((uintptr_t)workspace % kAlign) != 0)
         return fail(ODT_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
@@ -605,6 +615,7 @@ odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const
     for (int b = 0; b < nbatches; ++b) {
         const int a0 = b * plan->batch;
         const int nb = std::min(plan->batch, d.num_angles - a0);
+        P.again = angle_gain ? (const float2 *)angle_gain + (size_t)a0 * spec : nullptr;
         RotParams R;
         R.ny = d.ny;
         R.nx = d.nx;
@@ -618,7 +629,7 @@ odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const
                                        s);
         if (e != cudaSuccess)
             return cuda_fail(e, "rotate_adjoint launch");
-        if (gain_grad) {
+        if (gain_grad || angle_gain_grad) {
             const char *sino_b = (const char *)sino + (size_t)a0 * d.ny * d.nx * in_elem;
             e = odt::launch_rows_forward(P, sino_b, weights ? weights + a0 : nullptr, nb, rowspec, s);
             if (e != cudaSuccess)
@@ -637,7 +648,9 @@ odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const
             if (e != cudaSuccess)
                 return cuda_fail(e, "adj_columns launch");
         }
-        e = odt::launch_adj_spectrum(P, rowspec, Qg, gain_grad, W, nb, s);
+        e = odt::launch_adj_spectrum(P, rowspec, Qg, gain_grad,
+                                     angle_gain_grad ? (float2 *)angle_gain_grad + (size_t)a0 * spec : nullptr, W,
+                                     nb, s);
         if (e != cudaSuccess)
             return cuda_fail(e, "adj_spectrum launch");
         if (sino_grad) {
@@ -659,7 +672,7 @@ odt_status odt_bpp3d_execute_timed(const odt_bpp3d_plan *plan, const void *sino,
 {
     if (!timing)
         return fail(ODT_ERR_INVALID_ARGUMENT, "timing is NULL");
-    return run_plan(plan, sino, weights, geometry, nullptr, volume, workspace, stream, timing);
+    return run_plan(plan, sino, weights, geometry, nullptr, nullptr, volume, workspace, stream, timing);
 }
 
 odt_status odt_bpp3d_launch_count(const odt_bpp3d_plan *plan, int64_t *launches)
@@ -777,5 +790,5 @@ extern "C" odt_status odt_bpp3d_execute_noalloc(const odt_bpp3d_plan *plan, cons
         }
         scratch = g_noalloc_addr[dev];
     }
-    return run_plan(plan, sino, weights, geometry, nullptr, volume, scratch, stream, nullptr);
+    return run_plan(plan, sino, weights, geometry, nullptr, nullptr, volume, scratch, stream, nullptr);
 }

@@ -40,7 +40,9 @@ struct StageParams {
     float bx_ca, bx_cb;  // x-prefilter boundary solve (n = nx)
     float by_ca, by_cb;  // y-prefilter boundary solve (n = ny)
     FilterTables tab;
-    const float *gain;  // optional real per-frequency gain [lNy*lNx] (NULL: 1)
+    const float *gain;   // optional real per-frequency gain [lNy*lNx] (NULL: 1)
+    const float2 *again; // optional complex per-angle gain [A][lNy*lNx], this
+                         // batch's first angle at again (NULL: 1)
     int *status;
 };
 
@@ -77,10 +79,14 @@ cudaError_t launch_rotate_adjoint(const RotParams &R, int order, int tilted, con
 cudaError_t launch_adj_rows(const StageParams &P, const float2 *sgrad, float2 *Tg, int q0, int qn, cudaStream_t s);
 cudaError_t launch_adj_columns(const StageParams &P, const float2 *Tg, float2 *Qg, int q0, int qn, cudaStream_t s);
 cudaError_t launch_adj_spectrum(const StageParams &P, const float2 *rowspec, const float2 *Qg, float *dgain,
-                                float2 *W, int nb, cudaStream_t s);
+                                float2 *dagain, float2 *W, int nb, cudaStream_t s);
 cudaError_t launch_adj_rows_full(const StageParams &P, const float2 *W, float2 *Pg, int nb, cudaStream_t s);
 cudaError_t launch_adj_pad(const StageParams &P, const float2 *Pg, const double *weights, int nb, float2 *dsino,
                            cudaStream_t s);
 bool line_size_supported(int n);
+
+// Record `msg` as the calling thread's last error (odt_last_error) and
+// return `status`.
+int set_error(int status, const char *msg);
 
 }  // namespace odt

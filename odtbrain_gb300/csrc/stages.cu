@@ -96,6 +96,8 @@ __device__ __forceinline__ void column_spectrum(const StageParams &P, const L &l
             v[r] = cmul(v[r], P.tab.G[k]);
             if (P.gain)
                 v[r] = cscale(v[r], P.gain[k]);
+            if (P.again)
+                v[r] = cmul(v[r], P.again[(size_t)a * P.lNy * P.lNx + k]);
         } else {
             v[r] = make_float2(0.f, 0.f);
         }

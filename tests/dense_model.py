@@ -83,7 +83,8 @@ def prefilter_matrix(n, order):
 
 
 class DenseBackprop:
-    """Differentiable FP64 model: __call__(sino, gain) -> volume [z,y,x]."""
+    """Differentiable FP64 model: __call__(sino, gain, angle_gain) -> volume
+    [z,y,x]; gain (lNy, lNx) real, angle_gain (A, lNy, lNx) complex."""
 
     def __init__(self, angles, ny, nx, res, nm, lD=0.0, padfac=1.75,
                  order=2, weight_angles=True):
@@ -117,7 +118,7 @@ class DenseBackprop:
         self.ys = torch.from_numpy(ys)
         self.xs = torch.from_numpy(xs)
 
-    def __call__(self, sino, gain=None):
+    def __call__(self, sino, gain=None, angle_gain=None):
         g = self.geo
         lNy, lNx = g["lNy"], g["lNx"]
         s = sino * self.w.reshape(-1, 1, 1)
@@ -125,6 +126,8 @@ class DenseBackprop:
         X = torch.fft.fft2(padded)
         F = self.filt if gain is None else self.filt * gain
         X = X * F
+        if angle_gain is not None:
+            X = X * angle_gain
         prop = torch.exp(1j * self.phase[None] * self.z.reshape(-1, 1, 1))
         V = X[:, None] * prop[None]                    # (A, nz, lNy, lNx)
         u = torch.fft.ifft2(V, norm="forward")

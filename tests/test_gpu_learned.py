@@ -1,0 +1,145 @@
+"""GPU tests of the learned filter gain.
+
+* the BF16 tensor-core MLP kernels (odt_mlp_gain_forward / _backward)
+  against the CPU oracle (oracle/mlp_oracle.py) with the same BF16 operand
+  rounding, at ragged sizes (point counts that are not multiples of the
+  16-point tile);
+* the chain used in training: reconstruction adjoint -> gain gradient ->
+  MLP parameter gradients, against central differences of the loss in the
+  output bias (FP32 in the kernels, so the perturbation is exact);
+* a short training run on a small wedge: the learned gain beats the plain
+  filter on held-out phantoms, and the plain filter stays available as the
+  fallback.
+"""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / \
+        np.linalg.norm(np.asarray(b))
+
+
+def _random_mlp(torch, dev, seed, scale=1.0):
+    from odtbrain_gb300.learned import GainMLP, PARAM_SHAPES
+    rng = np.random.default_rng(seed)
+    st = {}
+    for k, shape in PARAM_SHAPES.items():
+        fan = shape[1] if len(shape) == 2 else 64
+        st[k] = rng.normal(0, scale / np.sqrt(fan), shape).astype(np.float32)
+    m = GainMLP(device=dev)
+    m.load_state(st)
+    return m, st
+
+
+@pytest.mark.parametrize("A,lNy,lNx", [(3, 32, 32), (2, 17, 30), (1, 5, 3)])
+def test_mlp_forward_matches_oracle(cuda_ready, A, lNy, lNx):
+    import torch
+    dev = cuda_ready
+    m, st = _random_mlp(torch, dev, seed=A + lNx)
+    rng = np.random.default_rng(7)
+    af = rng.uniform(-1.5, 1.5, (A, 2)).astype(np.float32)
+    g = m.gains(torch.tensor(af, device=dev), lNy, lNx).cpu().numpy()
+    X = M.features(af, lNy, lNx)
+    ref, _ = M.forward(st, X, bf16=True)
+    exact, _ = M.forward(st, X, bf16=False)
+    got = g.reshape(-1)
+    assert np.all(np.isfinite(got))
+    assert _rel(got - 1, ref - 1) < 1e-3
+    # BF16 operands against the exact FP64 network
+    assert _rel(got - 1, exact - 1) < 5e-2
+
+
+@pytest.mark.parametrize("A,lNy,lNx", [(3, 32, 32), (2, 17, 30)])
+def test_mlp_backward_matches_oracle(cuda_ready, A, lNy, lNx):
+    import torch
+    dev = cuda_ready
+    m, st = _random_mlp(torch, dev, seed=11 + A)
+    rng = np.random.default_rng(8)
+    af = rng.uniform(-1.5, 1.5, (A, 2)).astype(np.float32)
+    dg = (rng.normal(size=(A, lNy, lNx)) +
+          1j * rng.normal(size=(A, lNy, lNx))).astype(np.complex64)
+    grads = m.grads(torch.tensor(af, device=dev), torch.tensor(dg,
+                                                             device=dev))
+    X = M.features(af, lNy, lNx)
+    ref = M.backward(st, X, dg.reshape(-1), bf16=True)
+    exact = M.backward(st, X, dg.reshape(-1), bf16=False)
+    for k in ref:
+        got = grads[k].cpu().numpy()
+        assert got.shape == ref[k].shape, k
+        assert _rel(got, ref[k]) < 2e-3, k
+        assert _rel(got, exact[k]) < 5e-2, k
+
+
+def test_training_chain_matches_finite_differences(cuda_ready):
+    """d loss / d b4 through the reconstruction adjoint and the MLP
+    backward, against central differences of the FP32 forward."""
+    import torch
+    from odtbrain_gb300._alg3d import Backprop3D
+    from odtbrain_gb300.learned import LearnedFilter, wedge_angles
+    from odtbrain_gb300 import phantoms
+    dev = cuda_ready
+    n, A = 24, 10
+    angles = wedge_angles(A, 2 * np.pi / 3)
+    rec = Backprop3D((A, n, n), angles, 3.0, 1.333, input_dtype="complex64",
+                     device=dev)
+    m, st = _random_mlp(torch, dev, seed=5, scale=0.5)
+    lf = LearnedFilter(rec, m)
+    rng = np.random.default_rng(4)
+    ells = phantoms.random_ellipsoids(rng, n, (2, 4), (3, 8))
+    sino = phantoms.project([ells], angles, n, amp_sigma=0.01, seed=1,
+                            device=dev)[0].contiguous()
+    tgt = torch.tensor((rng.normal(size=(n, n, n)) +
+                        1j * rng.normal(size=(n, n, n))).astype(np.complex64),
+                       device=dev) * 0.01
+
+    def loss():
+        v = lf(sino).to(torch.complex128) - tgt.to(torch.complex128)
+        return (v.abs() ** 2).sum().item()
+
+    vol = lf(sino)
+    cot = (2 * (vol - tgt)).to(torch.complex64)
+    _s, _g, dgain = rec.adjoint(sino, cot, angle_gain=lf.gains(),
+                                need_sino=False, need_angle_gain=True)
+    g = m.grads(lf.feat, dgain)
+    # b4 is FP32 in the kernels: perturb it directly
+    for j in range(2):
+        h = 1e-2
+        base = st["b4"].copy()
+        vals = []
+        for s in (+1, -1):
+            st2 = dict(st)
+            st2["b4"] = base.copy()
+            st2["b4"][j] += s * h
+            m.load_state(st2)
+            vals.append(loss())
+        m.load_state(st)
+        fd = (vals[0] - vals[1]) / (2 * h)
+        an = g["b4"][j].item()
+        assert abs(fd - an) <= 3e-3 * abs(an) + 2e-5 * vals[0], (j, fd, an)
+
+
+def test_short_training_beats_plain_filter(cuda_ready):
+    from odtbrain_gb300.learned import train_wedge_filter
+    lf, rep = train_wedge_filter(dict(
+        n=32, num_angles=12, dense_angles=120, count_range=(1, 4),
+        semi_range=(3.0, 9.0), n_train=64, n_val=16, n_eval=16, epochs=3,
+        batch=4, lr=3e-3), device=cuda_ready, log=lambda *a: None)
+    print("\nsmall wedge: eval rel-L2 learned %.4f plain %.4f (%.1f%%)"
+          % (rep["eval_rel_l2_learned"], rep["eval_rel_l2_plain"],
+             100 * rep["reduction"]))
+    assert rep["enabled"]
+    assert rep["eval_rel_l2_learned"] < rep["eval_rel_l2_plain"]
+    # the fallback is the plain reconstruction
+    lf.enabled = False
+    import torch
+    s = torch.zeros(lf.rec.shape, dtype=torch.complex64,
+                    device=cuda_ready)
+    s[:, 3, 4] = 1.0
+    a = lf(s)
+    b = lf.rec(s)
+    assert torch.equal(a, b)
