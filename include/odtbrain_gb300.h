@@ -218,24 +218,34 @@ typedef struct odt_mlp_grads {  /* FP32, the weights' shapes; added to (+=)  */
 } odt_mlp_grads;
 
 /* gain: complex64 [num_angles][pad_ny][pad_nx]; angle_features: float
- * [num_angles][2]. */
+ * [num_angles][2].  positions (device, optional): the num_positions flat
+ * spectrum positions ky*pad_nx + kx evaluated for every angle, e.g. the
+ * support of the filter; other gain entries are left untouched (NULL: all
+ * pad_ny*pad_nx positions).  Listed positions outside the grid are skipped. */
 odt_status odt_mlp_gain_forward(const odt_mlp_params *params,
                                 int32_t num_angles, int32_t pad_ny,
                                 int32_t pad_nx, const float *angle_features,
-                                void *gain, void *stream);
+                                const int32_t *positions,
+                                int32_t num_positions, void *gain,
+                                void *stream);
 
-/* Device bytes of the activation store odt_mlp_gain_backward needs. */
-odt_status odt_mlp_store_size(int32_t num_angles, int32_t pad_ny,
-                              int32_t pad_nx, uint64_t *bytes);
+/* Device bytes of the activation store odt_mlp_gain_backward needs for
+ * num_positions positions per angle. */
+odt_status odt_mlp_store_size(int32_t num_angles, int32_t num_positions,
+                              uint64_t *bytes);
 
 /* Gradients of a real loss with respect to the MLP parameters, given the
  * loss gradient with respect to the gain (complex64, PyTorch's convention
  * d/dRe + i d/dIm, e.g. the angle_gain_grad of odt_bpp3d_adjoint).  Recomputes
  * the forward; `store` (256-byte aligned, odt_mlp_store_size bytes) holds the
- * activations between the two kernels. */
+ * activations between the two kernels.  Only the listed positions
+ * contribute (the gradient elsewhere must be zero for the result to be the
+ * full gradient, as it is outside the filter's support). */
 odt_status odt_mlp_gain_backward(const odt_mlp_params *params,
                                  int32_t num_angles, int32_t pad_ny,
                                  int32_t pad_nx, const float *angle_features,
+                                 const int32_t *positions,
+                                 int32_t num_positions,
                                  const void *gain_grad, void *store,
                                  const odt_mlp_grads *grads, void *stream);
 

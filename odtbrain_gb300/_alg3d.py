@@ -129,7 +129,10 @@ class Backprop3D:
                                    "is available (there is no CPU "
                                    "fallback)")
             device = torch.device("cuda", torch.cuda.current_device())
-        self.device = torch.device(device)
+        device = torch.device(device)
+        if device.type == "cuda" and device.index is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = device
         A, lny, lnx = shape
         self.shape = (A, lny, lnx)
         self.onlyreal = bool(onlyreal)
@@ -138,6 +141,8 @@ class Backprop3D:
         self.padding_geometry = g
         angles = np.asarray(angles)
         self.angles = angles
+        self._res, self._nm, self._lD = float(res), float(nm), float(lD)
+        self._support = None
         if tilted_axis is None:
             kind = _native.ODT_GEOM_Y_AXIS
             if weights is None and weight_angles:
@@ -158,6 +163,7 @@ class Backprop3D:
                             _native.ODT_INPUT_C64 else torch.complex128)
         if workspace_limit is None:
             workspace_limit = _WS_SAVE_MEMORY if save_memory else _WS_DEFAULT
+        self._taxis = taxis
         taxis_key = None if taxis is None else tuple(float(t) for t in taxis)
         key = (self.device.index, A, lny, lnx, g["lNy"], g["lNx"],
                g["padyl"], g["padxl"], pad_mode, padval_c, int(intp_order),
@@ -262,6 +268,18 @@ class Backprop3D:
         if check:
             self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
         return out
+
+    def filter_support(self):
+        """Flat positions ky*lNx + kx (int32, ascending) where the filter is
+        nonzero: the only positions where a gain has an effect."""
+        if self._support is None:
+            g = self.padding_geometry
+            filt, _ph = geom.filter_tables(self.shape[0], g["lNx"], g["lNy"],
+                                           self._res, self._nm, self._lD,
+                                           tilted_axis=self._taxis)
+            self._support = np.flatnonzero(filt.reshape(-1) != 0).astype(
+                np.int32)
+        return self._support
 
     def gain_shape(self):
         g = self.padding_geometry

@@ -151,11 +151,11 @@ def lib():
         L.odt_bpp3d_plan_destroy.argtypes = [vp]
         i32 = ctypes.c_int32
         L.odt_mlp_gain_forward.argtypes = [ctypes.POINTER(MlpParams), i32,
-                                           i32, i32, vp, vp, vp]
-        L.odt_mlp_store_size.argtypes = [i32, i32, i32,
+                                           i32, i32, vp, vp, i32, vp, vp]
+        L.odt_mlp_store_size.argtypes = [i32, i32,
                                          ctypes.POINTER(ctypes.c_uint64)]
         L.odt_mlp_gain_backward.argtypes = [
-            ctypes.POINTER(MlpParams), i32, i32, i32, vp, vp, vp,
+            ctypes.POINTER(MlpParams), i32, i32, i32, vp, vp, i32, vp, vp,
             ctypes.POINTER(MlpGrads), vp]
         for name in ("odt_bpp3d_plan_create", "odt_bpp3d_workspace_size",
                      "odt_bpp3d_angle_batch", "odt_bpp3d_execute",

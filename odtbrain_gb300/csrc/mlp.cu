@@ -19,6 +19,10 @@
 // operand of the next layer's 16-column k-tile: a warp carries 16 points
 // through all layers in registers.
 //
+// The points evaluated are, per angle, either every padded spectrum position
+// or a caller's list of positions (the filter's support: elsewhere the
+// filter is zero and the gain has no effect).
+//
 // Training: k_mlp_backward_data recomputes the forward for 16 points per
 // warp, back-propagates the gain gradient through the layers (with the
 // transposed weights, again on the tensor cores) and stores the BF16
@@ -145,16 +149,35 @@ __device__ void load_forward(const MlpWeights &W, SmemForward &S)
 
 struct MlpGrid {
     int A, lNy, lNx;
-    long long P;               // A * lNy * lNx points
+    const int *pos;            // spectrum positions ky*lNx + kx evaluated
+                               // (NULL: all lNy*lNx)
+    int npos;                  // positions per angle
+    long long P;               // A * npos points
     const float2 *angle_feat;  // per angle: (angle feature, gap feature)
 };
 
-// Features of point idx = (a*lNy + ky)*lNx + kx.
-__device__ __forceinline__ void point_features(const MlpGrid &Gd, long long idx, float (&f)[4])
+// Spectrum position of the j-th evaluated point of an angle; positions
+// outside [0, lNy*lNx) in a caller's list give -1 (the point is skipped).
+__device__ __forceinline__ int position(const MlpGrid &Gd, int j)
 {
-    const long long K = (long long)Gd.lNy * Gd.lNx;
-    const int a = (int)(idx / K);
-    const int k = (int)(idx - (long long)a * K);
+    const int k = Gd.pos ? __ldg(Gd.pos + j) : j;
+    return (unsigned)k < (unsigned)(Gd.lNy * Gd.lNx) ? k : -1;
+}
+
+// Point p = a*npos + j stands for the gain entry a*lNy*lNx + pos[j] (-1:
+// skipped).
+__device__ __forceinline__ long long gain_index(const MlpGrid &Gd, long long p)
+{
+    const int a = (int)(p / Gd.npos);
+    const int k = position(Gd, (int)(p - (long long)a * Gd.npos));
+    return k < 0 ? -1 : (long long)a * Gd.lNy * Gd.lNx + k;
+}
+
+// Features of point p.
+__device__ __forceinline__ void point_features(const MlpGrid &Gd, long long p, float (&f)[4])
+{
+    const int a = (int)(p / Gd.npos);
+    const int k = max(position(Gd, (int)(p - (long long)a * Gd.npos)), 0);
     const int ky = k / Gd.lNx, kx = k - ky * Gd.lNx;
     // fftfreq order: index m stands for m (m <= (N-1)/2) or m - N
     const int hx = (Gd.lNx - 1) / 2, hy = (Gd.lNy - 1) / 2;
@@ -266,10 +289,12 @@ __global__ void __launch_bounds__(32 * FWD_WARPS) k_mlp_forward(MlpWeights W, Ml
         dense<4, 1>(A, S.w4, LD64, S.b4, lane, O);
         if (t == 0) {
             const long long i0 = p0 + g, i1 = p0 + g + 8;
-            if (i0 < Gd.P)
-                gain[i0] = make_float2(1.f + O[0][0], O[0][1]);
-            if (i1 < Gd.P)
-                gain[i1] = make_float2(1.f + O[0][2], O[0][3]);
+            const long long k0 = i0 < Gd.P ? gain_index(Gd, i0) : -1;
+            const long long k1 = i1 < Gd.P ? gain_index(Gd, i1) : -1;
+            if (k0 >= 0)
+                gain[k0] = make_float2(1.f + O[0][0], O[0][1]);
+            if (k1 >= 0)
+                gain[k1] = make_float2(1.f + O[0][2], O[0][3]);
         }
     }
 }
@@ -361,7 +386,8 @@ __global__ void __launch_bounds__(32 * BWD_WARPS) k_mlp_backward_data(MlpWeights
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const long long idx = p0 + g + 8 * h;
-            const float2 d = idx < P ? dgain[idx] : make_float2(0.f, 0.f);
+            const long long gi = idx < P ? gain_index(Gd, idx) : -1;
+            const float2 d = gi >= 0 ? dgain[gi] : make_float2(0.f, 0.f);
             dO[h][0] = d.x;
             dO[h][1] = d.y;
             if (idx < P) {
@@ -484,12 +510,14 @@ bool aligned(const void *p, size_t a) { return ((uintptr_t)p % a) == 0; }
 odt_status err(odt_status st, const std::string &msg) { return (odt_status)set_error(st, msg.c_str()); }
 
 odt_status check_params(const odt_mlp_params *p, int32_t A, int32_t lNy, int32_t lNx, const float *feat,
-                        MlpWeights &W, MlpGrid &Gd)
+                        const int32_t *positions, int32_t num_positions, MlpWeights &W, MlpGrid &Gd)
 {
     if (!p || !feat)
         return err(ODT_ERR_INVALID_ARGUMENT, "NULL argument");
     if (A < 1 || lNy < 1 || lNx < 1)
         return err(ODT_ERR_INVALID_ARGUMENT, "need num_angles, pad_ny, pad_nx >= 1");
+    if (positions && (num_positions < 1 || num_positions > lNy * lNx || !aligned(positions, 4)))
+        return err(ODT_ERR_INVALID_ARGUMENT, "need 1 <= num_positions <= pad_ny*pad_nx (4-byte aligned list)");
     const void *ptrs[] = {p->w1, p->w2, p->w3, p->w4, p->w2t, p->w3t, p->w4t, p->b1, p->b2, p->b3, p->b4};
     for (const void *q : ptrs)
         if (!q || !aligned(q, 16))
@@ -510,7 +538,9 @@ odt_status check_params(const odt_mlp_params *p, int32_t A, int32_t lNy, int32_t
     Gd.A = A;
     Gd.lNy = lNy;
     Gd.lNx = lNx;
-    Gd.P = (long long)A * lNy * lNx;
+    Gd.pos = positions;
+    Gd.npos = positions ? num_positions : lNy * lNx;
+    Gd.P = (long long)A * Gd.npos;
     Gd.angle_feat = (const float2 *)feat;
     return ODT_OK;
 }
@@ -528,11 +558,13 @@ using namespace odt;
 extern "C" {
 
 odt_status odt_mlp_gain_forward(const odt_mlp_params *params, int32_t num_angles, int32_t pad_ny, int32_t pad_nx,
-                                const float *angle_features, void *gain, void *stream)
+                                const float *angle_features, const int32_t *positions, int32_t num_positions,
+                                void *gain, void *stream)
 {
     MlpWeights W;
     MlpGrid Gd;
-    odt_status st = check_params(params, num_angles, pad_ny, pad_nx, angle_features, W, Gd);
+    odt_status st =
+        check_params(params, num_angles, pad_ny, pad_nx, angle_features, positions, num_positions, W, Gd);
     if (st != ODT_OK)
         return st;
     if (!gain || !aligned(gain, 8))
@@ -548,21 +580,22 @@ odt_status odt_mlp_gain_forward(const odt_mlp_params *params, int32_t num_angles
     return ODT_OK;
 }
 
-odt_status odt_mlp_store_size(int32_t num_angles, int32_t pad_ny, int32_t pad_nx, uint64_t *bytes)
+odt_status odt_mlp_store_size(int32_t num_angles, int32_t num_positions, uint64_t *bytes)
 {
-    if (!bytes || num_angles < 1 || pad_ny < 1 || pad_nx < 1)
-        return err(ODT_ERR_INVALID_ARGUMENT, "need num_angles, pad_ny, pad_nx >= 1 and a result pointer");
-    *bytes = store_bytes((long long)num_angles * pad_ny * pad_nx);
+    if (!bytes || num_angles < 1 || num_positions < 1)
+        return err(ODT_ERR_INVALID_ARGUMENT, "need num_angles, num_positions >= 1 and a result pointer");
+    *bytes = store_bytes((long long)num_angles * num_positions);
     return ODT_OK;
 }
 
 odt_status odt_mlp_gain_backward(const odt_mlp_params *params, int32_t num_angles, int32_t pad_ny, int32_t pad_nx,
-                                 const float *angle_features, const void *gain_grad, void *store,
-                                 const odt_mlp_grads *grads, void *stream)
+                                 const float *angle_features, const int32_t *positions, int32_t num_positions,
+                                 const void *gain_grad, void *store, const odt_mlp_grads *grads, void *stream)
 {
     MlpWeights W;
     MlpGrid Gd;
-    odt_status st = check_params(params, num_angles, pad_ny, pad_nx, angle_features, W, Gd);
+    odt_status st =
+        check_params(params, num_angles, pad_ny, pad_nx, angle_features, positions, num_positions, W, Gd);
     if (st != ODT_OK)
         return st;
     if (!gain_grad || !aligned(gain_grad, 8) || !store || !aligned(store, 256) || !grads)

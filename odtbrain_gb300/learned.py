@@ -81,7 +81,10 @@ class GainMLP:
 
     def __init__(self, device="cuda", seed=0):
         torch = _torch()
-        self.device = torch.device(device)
+        device = torch.device(device)
+        if device.type == "cuda" and device.index is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = device
         g = torch.Generator().manual_seed(int(seed))
         p = {}
         for name, shape in PARAM_SHAPES.items():
@@ -166,28 +169,53 @@ class GainMLP:
             raise ValueError("angle features must have shape (A, 2)")
         return feat
 
-    def gains(self, feat, pad_ny, pad_nx, out=None):
+    def _positions(self, positions, pad_ny, pad_nx):
+        """Device int32 list of flat spectrum positions (None: all)."""
+        torch = _torch()
+        if positions is None:
+            return None, 0
+        if not isinstance(positions, torch.Tensor):
+            positions = torch.tensor(np.asarray(positions, dtype=np.int32))
+        positions = positions.to(device=self.device,
+                                 dtype=torch.int32).contiguous().reshape(-1)
+        if positions.numel() < 1:
+            raise ValueError("empty position list")
+        return positions, int(positions.numel())
+
+    def gains(self, feat, pad_ny, pad_nx, out=None, positions=None):
         """Complex64 gains (A, pad_ny, pad_nx) for per-angle features
-        (A, 2)."""
+        (A, 2).  With ``positions`` (flat ky*pad_nx + kx indices) only those
+        entries are evaluated; the others are 1 in a new ``out`` and left
+        untouched in a given one."""
         torch = _torch()
         feat = self._feat(feat)
         A = feat.shape[0]
+        shape = (A, pad_ny, pad_nx)
+        pos, npos = self._positions(positions, pad_ny, pad_nx)
         if out is None:
-            out = torch.empty((A, pad_ny, pad_nx), dtype=torch.complex64,
-                              device=self.device)
+            out = (torch.empty if pos is None else torch.ones)(
+                shape, dtype=torch.complex64, device=self.device)
+        elif (out.dtype != torch.complex64 or tuple(out.shape) != shape
+              or out.device != self.device or not out.is_contiguous()):
+            raise ValueError("out must be a contiguous complex64 tensor of "
+                             "shape %s on %s" % (shape, self.device))
         _t, s = self._pack()
         stream = torch.cuda.current_stream(self.device)
         L = _native.lib()
         _native.check(L.odt_mlp_gain_forward(
             ctypes.byref(s), A, pad_ny, pad_nx,
-            ctypes.c_void_p(feat.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+            ctypes.c_void_p(feat.data_ptr()),
+            ctypes.c_void_p(pos.data_ptr() if pos is not None else 0), npos,
+            ctypes.c_void_p(out.data_ptr()),
             ctypes.c_void_p(stream.cuda_stream)))
         return out
 
-    def grads(self, feat, gain_grad):
+    def grads(self, feat, gain_grad, positions=None):
         """Gradients of the loss with respect to the FP32 master parameters
         for the loss gradient ``gain_grad`` (complex64 (A, pad_ny, pad_nx),
-        d/dRe + i d/dIm) with respect to the gains."""
+        d/dRe + i d/dIm) with respect to the gains.  With ``positions`` only
+        those entries contribute (exact where gain_grad is zero elsewhere,
+        as it is outside the filter's support)."""
         torch = _torch()
         feat = self._feat(feat)
         A, pad_ny, pad_nx = gain_grad.shape
@@ -196,10 +224,12 @@ class GainMLP:
             raise ValueError("gain_grad must be complex64 (A, pad_ny, pad_nx)"
                              " on the device")
         gain_grad = gain_grad.contiguous()
+        pos, npos = self._positions(positions, pad_ny, pad_nx)
         L = _native.lib()
         nbytes = ctypes.c_uint64()
-        _native.check(L.odt_mlp_store_size(A, pad_ny, pad_nx,
-                                           ctypes.byref(nbytes)))
+        _native.check(L.odt_mlp_store_size(
+            A, npos if pos is not None else pad_ny * pad_nx,
+            ctypes.byref(nbytes)))
         if self._store is None or self._store.numel() < nbytes.value:
             self._store = torch.empty(int(nbytes.value), dtype=torch.uint8,
                                       device=self.device)
@@ -218,6 +248,7 @@ class GainMLP:
         _native.check(L.odt_mlp_gain_backward(
             ctypes.byref(s), A, pad_ny, pad_nx,
             ctypes.c_void_p(feat.data_ptr()),
+            ctypes.c_void_p(pos.data_ptr() if pos is not None else 0), npos,
             ctypes.c_void_p(gain_grad.data_ptr()),
             ctypes.c_void_p(self._store.data_ptr()), ctypes.byref(gs),
             ctypes.c_void_p(stream.cuda_stream)))
@@ -235,6 +266,8 @@ class LearnedFilter:
         self.mlp = mlp
         self.enabled = bool(enabled)
         self.feat = mlp._feat(angle_features(rec.angles))
+        # the gain only matters where the filter is nonzero
+        self.positions = mlp._positions(rec.filter_support(), 0, 0)[0]
         self._gain = None
         self._gain_version = -1
 
@@ -243,7 +276,8 @@ class LearnedFilter:
         version)."""
         if self._gain_version != self.mlp.version:
             lNy, lNx = self.rec.gain_shape()
-            self._gain = self.mlp.gains(self.feat, lNy, lNx, out=self._gain)
+            self._gain = self.mlp.gains(self.feat, lNy, lNx, out=self._gain,
+                                        positions=self.positions)
             self._gain_version = self.mlp.version
         return self._gain
 
@@ -251,6 +285,24 @@ class LearnedFilter:
         if not self.enabled:
             return self.rec(sino, out=out)
         return self.rec.forward_gain(sino, angle_gain=self.gains(), out=out)
+
+
+def pretrained_path(name="wedge40_128"):
+    """Path of a network shipped with the package: ``wedge40_128`` was
+    trained by :func:`train_wedge_filter` with :data:`WEDGE_CONFIG` (40
+    angles over a 120 degree wedge, 128^2 sinograms); its report is the
+    ``.json`` beside it."""
+    import os
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "data",
+                        name + ".npz")
+
+
+def load_learned_filter(rec, name="wedge40_128"):
+    """:class:`LearnedFilter` for the plan ``rec`` with a shipped network;
+    enabled as the network's validation decided (otherwise the plain
+    filter)."""
+    mlp = GainMLP.load(pretrained_path(name), device=rec.device)
+    return LearnedFilter(rec, mlp, enabled=mlp.meta.get("enabled", True))
 
 
 # ---------------------------------------------------------------------------
@@ -334,6 +386,8 @@ def train_wedge_filter(cfg=None, device="cuda", log=print):
     c = dict(WEDGE_CONFIG)
     c.update(cfg or {})
     dev = torch.device(device)
+    if dev.type == "cuda" and dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
     n, A = c["n"], c["num_angles"]
     sp_angles = wedge_angles(A, c["span"])
     de_angles = np.linspace(0, 2 * np.pi, c["dense_angles"], endpoint=False)
@@ -374,7 +428,7 @@ def train_wedge_filter(cfg=None, device="cuda", log=print):
         ep_loss = 0.0
         for b in range(steps_per_epoch):
             idx = perm[b * c["batch"]:(b + 1) * c["batch"]]
-            gain = mlp.gains(feat, lNy, lNx)
+            gain = lf.gains()
             dgain = torch.zeros_like(gain)
             loss = 0.0
             for i in idx:
@@ -389,7 +443,7 @@ def train_wedge_filter(cfg=None, device="cuda", log=print):
                                          need_sino=False,
                                          need_angle_gain=True)
                 dgain += ag
-            g = mlp.grads(feat, dgain)
+            g = mlp.grads(feat, dgain, positions=lf.positions)
             for k in PARAM_SHAPES:
                 mlp.params[k].grad = g[k].clone()
             opt.step()
@@ -414,7 +468,8 @@ def train_wedge_filter(cfg=None, device="cuda", log=print):
     gain = lf.gains()
     ms_learned = _event_ms(lambda: rec.forward_gain(
         sino0, angle_gain=gain, out=vol, check=False), 20)
-    ms_infer = _event_ms(lambda: mlp.gains(feat, lNy, lNx, out=gain), 20)
+    ms_infer = _event_ms(lambda: mlp.gains(feat, lNy, lNx, out=gain,
+                                           positions=lf.positions), 20)
     report = {
         "config": {k: (list(v) if isinstance(v, tuple) else v)
                    for k, v in c.items()},

@@ -75,6 +75,35 @@ def test_mlp_backward_matches_oracle(cuda_ready, A, lNy, lNx):
         assert _rel(got, exact[k]) < 5e-2, k
 
 
+def test_mlp_positions(cuda_ready):
+    """A position list evaluates only the listed entries (others keep their
+    value) and restricts the backward to them."""
+    import torch
+    dev = cuda_ready
+    m, st = _random_mlp(torch, dev, seed=3)
+    A, lNy, lNx = 3, 20, 24
+    rng = np.random.default_rng(9)
+    pos = np.sort(rng.choice(lNy * lNx, size=157, replace=False)).astype(
+        np.int32)
+    af = rng.uniform(-1, 1, (A, 2)).astype(np.float32)
+    fd = torch.tensor(af, device=dev)
+    full = m.gains(fd, lNy, lNx).cpu().numpy().reshape(A, -1)
+    part = m.gains(fd, lNy, lNx, positions=pos).cpu().numpy().reshape(A, -1)
+    mask = np.zeros(lNy * lNx, bool)
+    mask[pos] = True
+    assert np.all(part[:, ~mask] == 1)
+    np.testing.assert_array_equal(part[:, mask], full[:, mask])
+    dg = (rng.normal(size=(A, lNy * lNx)) +
+          1j * rng.normal(size=(A, lNy * lNx))).astype(np.complex64)
+    dg[:, ~mask] = 0
+    dgt = torch.tensor(dg.reshape(A, lNy, lNx), device=dev)
+    g_full = m.grads(fd, dgt)
+    g_part = m.grads(fd, dgt, positions=torch.tensor(pos, device=dev))
+    for k in g_full:
+        a, b = g_part[k].cpu().numpy(), g_full[k].cpu().numpy()
+        assert _rel(a, b) < 1e-5, k
+
+
 def test_training_chain_matches_finite_differences(cuda_ready):
     """d loss / d b4 through the reconstruction adjoint and the MLP
     backward, against central differences of the FP32 forward."""
@@ -105,7 +134,7 @@ def test_training_chain_matches_finite_differences(cuda_ready):
     cot = (2 * (vol - tgt)).to(torch.complex64)
     _s, _g, dgain = rec.adjoint(sino, cot, angle_gain=lf.gains(),
                                 need_sino=False, need_angle_gain=True)
-    g = m.grads(lf.feat, dgain)
+    g = m.grads(lf.feat, dgain, positions=lf.positions)
     # b4 is FP32 in the kernels: perturb it directly
     for j in range(2):
         h = 1e-2
@@ -143,3 +172,27 @@ def test_short_training_beats_plain_filter(cuda_ready):
     a = lf(s)
     b = lf.rec(s)
     assert torch.equal(a, b)
+
+
+def test_shipped_wedge_network_beats_plain_filter(cuda_ready):
+    """The committed network (trained on 2000 phantoms) on 12 phantoms from
+    the held-out seed range: rel-L2 to the dense plain reconstruction."""
+    from odtbrain_gb300._alg3d import Backprop3D
+    from odtbrain_gb300.learned import (WEDGE_CONFIG, evaluate,
+                                        load_learned_filter, make_pairs,
+                                        wedge_angles)
+    c = dict(WEDGE_CONFIG)
+    n, A = c["n"], c["num_angles"]
+    sp = wedge_angles(A, c["span"])
+    de = np.linspace(0, 2 * np.pi, c["dense_angles"], endpoint=False)
+    rec = Backprop3D((A, n, n), sp, c["res"], c["nm"], device=cuda_ready)
+    rec_d = Backprop3D((c["dense_angles"], n, n), de, c["res"], c["nm"],
+                       device=cuda_ready)
+    seeds = 2_000_000 + np.arange(12)
+    s, t = make_pairs(c, seeds, rec, rec_d, sp, de, cuda_ready)
+    lf = load_learned_filter(rec)
+    assert lf.enabled
+    learned, plain = evaluate(lf, s, t)
+    print("\nshipped wedge network: rel-L2 learned %.4f plain %.4f (%.1f%%)"
+          % (learned, plain, 100 * (1 - learned / plain)))
+    assert learned < 0.7 * plain
