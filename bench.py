@@ -84,6 +84,9 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--config", choices=sorted(WORKLOADS), default="c2",
                     help="workload (default c2, the headline configuration)")
+    ap.add_argument("--ncu-rotate-case", action="store_true",
+                    help="16 angles in one batch (one resampling launch) "
+                    "for ncu captures of the resampling kernel")
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: the workload's plane and volume "
                          "size with 8 angles and the save_memory workspace, "
@@ -461,18 +464,24 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def run_ncu_case():
+def run_ncu_case(rotate_case=False):
+    """Small case for ncu captures: the workload's plane and volume sizes
+    with 8 angles and the save_memory workspace, or (``rotate_case``) 16
+    angles in one batch, so that one resampling launch covers 16 angles as
+    in the full run."""
     import torch
     from odtbrain_gb300 import build as native_build
     native_build.build()
     from odtbrain_gb300._alg3d import Backprop3D
     w = WORKLOAD
     sino, angles = make_workload()
-    sino, angles = sino[:8].copy(), angles[:8].copy()
+    k = 16 if rotate_case else 8
+    sino, angles = sino[:k].copy(), angles[:k].copy()
     dev = torch.device("cuda", 0)
     rec = Backprop3D(tuple(sino.shape), angles, w["res"], w["nm"],
                      lD=w["lD"], padfac=w["padfac"],
-                     intp_order=w["intp_order"], save_memory=True,
+                     intp_order=w["intp_order"],
+                     save_memory=not rotate_case,
                      input_dtype="complex64", device=dev)
     d = torch.from_numpy(sino).to(dev)
     for _ in range(2):
@@ -487,8 +496,8 @@ def main():
     args = parse_args()
     WORKLOAD = WORKLOADS[args.config]
     WORKLOAD_NAME = WORKLOAD["name"]
-    if args.ncu_case:
-        run_ncu_case()
+    if args.ncu_case or args.ncu_rotate_case:
+        run_ncu_case(rotate_case=args.ncu_rotate_case)
     elif args.impl == "reference":
         run_reference(args)
     else:

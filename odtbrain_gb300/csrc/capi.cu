@@ -120,6 +120,7 @@ StageParams stage_params(const odt_bpp3d_plan *p)
     P.bx_cb = (float)p->bx_cb;
     P.by_ca = (float)p->by_ca;
     P.by_cb = (float)p->by_cb;
+    P.ypitch = odt::yaxis_slab_pitch(d.ny);
     P.tab = p->tab;
     P.gain = nullptr;
     P.again = nullptr;
@@ -319,7 +320,9 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     // ---- batching: the largest angle batch (and column-stage chunk) whose
     // workspace fits the limit
     const size_t plane_row_bytes = (size_t)d.ny * lNx * 8;           // one job's column-stage output
-    const size_t slab_bytes = (size_t)nz * d.ny * d.nx * 8;          // one angle's coefficient slab
+    // one angle's coefficient slab ([z][y][x] tilted, [z][x][ypitch] y-axis;
+    // the adjoint's slab gradients [y][z][x] fit either)
+    const size_t slab_bytes = (size_t)nz * (tilted ? d.ny : odt::yaxis_slab_pitch(d.ny)) * d.nx * 8;
     const size_t rowspec_bytes = (size_t)lNy * lNx * 8;              // one angle's row spectra
     const size_t tab_bytes = pf ? (size_t)2 * d.ny * lNx * 8 : 0;    // one angle's z-boundary rows
     const size_t vol_bytes = (size_t)nz * d.ny * d.nx * 8;           // compensation buffer
@@ -387,6 +390,8 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
 
     StageParams P = stage_params(p);
     e = odt::configure_kernels(P);
+    if (e == cudaSuccess && !tilted)
+        e = odt::configure_rotate_kernels();
     if (e == cudaSuccess && !tilted)
         e = odt::configure_adjoint_kernels(P);
     if (e != cudaSuccess) {
@@ -525,6 +530,7 @@ odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *
         R.ny = d.ny;
         R.nx = d.nx;
         R.nz = plan->nz;
+        R.ypitch = P.ypitch;
         R.nbatch_angles = nb;
         R.first_pass = b == 0;
         R.last_pass = b == nbatches - 1;
@@ -620,6 +626,7 @@ odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const
         R.ny = d.ny;
         R.nx = d.nx;
         R.nz = plan->nz;
+        R.ypitch = P.ypitch;
         R.nbatch_angles = nb;
         R.first_pass = 1;
         R.last_pass = 1;

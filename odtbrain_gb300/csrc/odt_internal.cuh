@@ -39,6 +39,8 @@ struct StageParams {
                                  // (outside the |k| < km disc)
     float bx_ca, bx_cb;  // x-prefilter boundary solve (n = nx)
     float by_ca, by_cb;  // y-prefilter boundary solve (n = ny)
+    int ypitch;          // y-axis slab [a][z][x][y]: y pitch (ny rounded up
+                         // to a multiple of 32)
     FilterTables tab;
     const float *gain;   // optional real per-frequency gain [lNy*lNx] (NULL: 1)
     const float2 *again; // optional complex per-angle gain [A][lNy*lNx], this
@@ -46,8 +48,12 @@ struct StageParams {
     int *status;
 };
 
+// y pitch of the y-axis slab layout [a][z][x][y]
+inline int yaxis_slab_pitch(int ny) { return (ny + 31) / 32 * 32; }
+
 struct RotParams {
     int ny, nx, nz;
+    int ypitch;       // y-axis slab pitch (yaxis_slab_pitch)
     int nbatch_angles;
     int first_pass;   // this launch starts the sum (overwrite)
     int last_pass;    // this launch ends the sum (drop the compensation)
@@ -71,6 +77,7 @@ size_t rotate_scratch_bytes(int nbatch_angles, int ny, int nx, int nz, int tilte
 cudaError_t launch_rotate(const RotParams &R, int order, int tilted, const float2 *slab, const double *geo,
                           void *volume, float2 *comp, void *scratch, cudaStream_t s);
 cudaError_t configure_kernels(const StageParams &P);
+cudaError_t configure_rotate_kernels();
 
 // Adjoint (adjoint.cu, rotate.cu).
 cudaError_t configure_adjoint_kernels(const StageParams &P);

@@ -195,28 +195,55 @@ __device__ __forceinline__ void store_sum(const RotParams &R, void *volume, floa
 }
 
 // ---------------------------------------------------------------------------
-// y-axis path: every (z, x) plane at fixed y is rotated; the slab layout is
-// [a][y][z][x] so that a plane is contiguous.
+// y-axis path: every (z, x) plane at fixed y is rotated by the same 2D map,
+// so the weights and taps of an output (z, x) are the same for all y.  The
+// slab layout is [a][z][x][y] (y innermost, pitch R.ypitch) and the lanes of
+// a half-warp are 16 consecutive y: every tap read is one contiguous,
+// conflict-free 128-byte row of shared memory, and the per-output work
+// (coordinates, in/out decision, weights) is done once per 16 updates.
 //
-// Work split: a CTA owns a 32 (z) x 32 (x) output tile of one y plane and
-// loops over the batch's angles.  The footprint of the rotated tile
-// (<= 52 x 52 coefficients for orders <= 3) is staged in shared memory with
+// Work split: a CTA owns a 16 (z) x 16 (x) output tile and 16 y values and
+// loops over the batch's angles.  Per angle, the footprint of the rotated
+// tile (<= 28 x 28 tap positions, 16 y each) is staged in shared memory with
 // cp.async, double-buffered so that the next angle's footprint streams in
-// while the current one is interpolated.  Everything that depends only on
-// (angle, tile) -- the footprint box, the FP32 coordinate split, whether
-// the tile needs bounds checks and mirrored taps -- is computed once per
-// launch by k_rotate_y_setup and read back as a 64-byte record.
-constexpr int RY_T = 32;       // output tile is 32 (z) x 32 (x)
-constexpr int RY_BOX = 52;     // footprint of a rotated tile + taps + margin
-constexpr int RY_BP = 53;      // shared-memory row pitch (float2)
-constexpr int RY_KAHAN = 8;    // angles summed plainly between Kahan steps
+// while the current one is interpolated.  Footprint positions are virtual:
+// positions outside [0, n-1] are filled from their mirror images, so the
+// interpolation itself never mirrors.  Threads 0..255 compute the parameter
+// record (box offset, in/out flag, weights) of one output each per angle.
+constexpr int R2_T = 16;        // output tile 16 (z) x 16 (x)
+constexpr int R2_Y = 16;        // y values per CTA (a half-warp)
+constexpr int R2_BOX = 28;      // max footprint per axis (virtual positions)
+constexpr int R2_THREADS = 512; // 32 half-warps
+constexpr int R2_OUT = 8;       // outputs per thread
+constexpr int R2_KAHAN = 8;     // angles summed plainly between Kahan steps
+constexpr int R2_BOXE = R2_BOX * R2_BOX * R2_Y;  // float2 per footprint buffer
+constexpr int R2_RING = 4;      // tile records in flight (angles a..a+3)
+// parameter record of an output: 4 words (box offset, in/out flag), then the
+// z and x weights, each duplicated into a (w, w) pair for packed FMAs
+template <int ORDER>
+constexpr int r2_words() { return 4 + 4 * (ORDER + 1); }
+constexpr size_t R2_SMEM = (size_t)2 * R2_BOXE * sizeof(float2) + (size_t)R2_T * R2_T * r2_words<3>() * sizeof(float) +
+                           (size_t)R2_RING * 64;
+
+// d = a * b + c on (re, im) pairs: one packed FP32 FMA
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;\n"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<unsigned long long *>(&a)), "l"(*reinterpret_cast<unsigned long long *>(&b)),
+          "l"(*reinterpret_cast<unsigned long long *>(&c)));
+    return *reinterpret_cast<float2 *>(&d);
+}
 
 struct __align__(16) TileGeo {
     AxisCoord z, x;            // coordinates at the tile origin
-    short box_z0, box_x0;      // footprint origin
+    short box_z0, box_x0;      // footprint origin (virtual: may be < 0)
     short box_zn, box_xn;      // footprint size; box_zn == 0: no output of
                                // the tile is inside for this angle
-    int interior;              // all taps in range: no checks, no mirroring
+    short interior;            // every output of the tile inside with margin:
+                               // no in/out decisions needed
+    short box_real;            // every footprint position in [0, n-1]
     int pad;
 };
 static_assert(sizeof(TileGeo) == 64, "TileGeo is one 64-byte record");
@@ -224,16 +251,16 @@ static_assert(sizeof(TileGeo) == 64, "TileGeo is one 64-byte record");
 template <int ORDER>
 __global__ void k_rotate_y_setup(RotParams R, const double *__restrict__ geo, TileGeo *__restrict__ tiles)
 {
-    const int ntz = (R.nz + RY_T - 1) / RY_T, ntx = (R.nx + RY_T - 1) / RY_T;
+    const int ntz = (R.nz + R2_T - 1) / R2_T, ntx = (R.nx + R2_T - 1) / R2_T;
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= R.nbatch_angles * ntz * ntx)
         return;
     const int a = id / (ntz * ntx), t = id % (ntz * ntx);
-    const int oz0 = (t / ntx) * RY_T, ox0 = (t % ntx) * RY_T;
+    const int oz0 = (t / ntx) * R2_T, ox0 = (t % ntx) * R2_T;
     const int nz = R.nz, nx = R.nx;
     const double *g = geo + 6 * (size_t)a;
     const double m00 = g[0], m01 = g[1], m10 = g[2], m11 = g[3], f0 = g[4], f1 = g[5];
-    const int ozB = min(oz0 + RY_T - 1, nz - 1), oxB = min(ox0 + RY_T - 1, nx - 1);
+    const int ozB = min(oz0 + R2_T - 1, nz - 1), oxB = min(ox0 + R2_T - 1, nx - 1);
     double czmin = DBL_MAX, czmax = -DBL_MAX, cxmin = DBL_MAX, cxmax = -DBL_MAX;
     for (int k = 0; k < 4; ++k) {
         const double oz = (k & 1) ? ozB : oz0, oxx = (k & 2) ? oxB : ox0;
@@ -248,51 +275,84 @@ __global__ void k_rotate_y_setup(RotParams R, const double *__restrict__ geo, Ti
     tg.x = make_axis((f1 + m10 * (double)oz0) + m11 * (double)ox0, m10, m11);
     tg.box_z0 = tg.box_x0 = tg.box_zn = tg.box_xn = 0;
     tg.interior = 0;
+    tg.box_real = 0;
     tg.pad = 0;
-    if (!(czmax < -0.01 || czmin > nz - 1 + 0.01 || cxmax < -0.01 || cxmin > nx - 1 + 0.01)) {
-        long long zlo = tap_start_d<ORDER>(czmin) - 1, zhi = tap_start_d<ORDER>(czmax) + ORDER + 1;
-        long long xlo = tap_start_d<ORDER>(cxmin) - 1, xhi = tap_start_d<ORDER>(cxmax) + ORDER + 1;
-        zlo = zlo < 0 ? 0 : zlo;
-        xlo = xlo < 0 ? 0 : xlo;
-        zhi = zhi > nz - 1 ? nz - 1 : zhi;
-        xhi = xhi > nx - 1 ? nx - 1 : xhi;
+    // only outputs with coordinates in [0, n-1] are interpolated: their taps
+    // span the clamped coordinate range plus the spline support (and one
+    // position of margin on each side for FP32 rounding of the tap start)
+    const double zlo_c = fmax(czmin, 0.0), zhi_c = fmin(czmax, (double)(nz - 1));
+    const double xlo_c = fmax(cxmin, 0.0), xhi_c = fmin(cxmax, (double)(nx - 1));
+    if (zlo_c <= zhi_c + 0.01 && xlo_c <= xhi_c + 0.01) {
+        const long long zlo = tap_start_d<ORDER>(zlo_c) - 1, zhi = tap_start_d<ORDER>(zhi_c) + ORDER + 1;
+        const long long xlo = tap_start_d<ORDER>(xlo_c) - 1, xhi = tap_start_d<ORDER>(xhi_c) + ORDER + 1;
         const long long zn = zhi - zlo + 1, xn = xhi - xlo + 1;
-        if (zn > RY_BOX || xn > RY_BOX) {
+        if (zn > R2_BOX || xn > R2_BOX) {
             atomicOr(R.status, DEVCHK_BOX_OVERFLOW);
-        } else if (zn > 0 && xn > 0) {
+        } else {
             tg.box_z0 = (short)zlo;
             tg.box_x0 = (short)xlo;
             tg.box_zn = (short)zn;
             tg.box_xn = (short)xn;
-            // every output of the tile well inside and every tap of every
-            // output within [0, n-1]: no checks and no mirroring needed
-            tg.interior = (czmin >= 2.0 && czmax <= nz - 3.0 && cxmin >= 2.0 && cxmax <= nx - 3.0 &&
-                           ozB == oz0 + RY_T - 1 && oxB == ox0 + RY_T - 1)
+            tg.interior = (czmin > 0.01 && czmax < nz - 1 - 0.01 && cxmin > 0.01 && cxmax < nx - 1 - 0.01 &&
+                           ozB == oz0 + R2_T - 1 && oxB == ox0 + R2_T - 1)
                               ? 1
                               : 0;
+            tg.box_real = (zlo >= 0 && zhi <= nz - 1 && xlo >= 0 && xhi <= nx - 1) ? 1 : 0;
         }
     }
     tiles[id] = tg;
 }
 
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-// Issue the footprint copy of one (angle, tile) into `buf`.
-__device__ __forceinline__ void stage_box(const TileGeo &tg, const float2 *plane, int nx, float2 *buf)
+// Issue the footprint copy of one (angle, tile) for y values [y0, y0+16):
+// position p = (vz, vx) of the box holds 16 y at buf[p*16 .. p*16+15], read
+// from the mirror image of (vz, vx).  Thread t copies 16-byte part t&7 of
+// positions (t>>3) + 64k.
+__device__ __forceinline__ void stage_box(const TileGeo &tg, const float2 *aslab, int nz, int nx, int ypitch,
+                                          int y0, float2 *buf)
 {
-    const int zn = tg.box_zn, xn = tg.box_xn;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int zi = ty; zi < zn; zi += 8) {
-        const float2 *row = plane + (size_t)(tg.box_z0 + zi) * nx + tg.box_x0;
-        for (int xi = tx; xi < xn; xi += 32)
-            cp_async8(buf + zi * RY_BP + xi, row + xi);
+    const int zn = tg.box_zn, xn = tg.box_xn, np = zn * xn;
+    const int part = threadIdx.x & 7;
+    int pidx = threadIdx.x >> 3;
+    if (pidx >= np)
+        return;
+    constexpr int step = R2_THREADS / 8;  // 64 positions per pass
+    const int sq = step / xn, sr = step % xn;
+    int pz = pidx / xn, px = pidx % xn;
+    if (tg.box_real) {
+        // every position is real: walk the source address incrementally
+        const float2 *src = aslab + ((size_t)(tg.box_z0 + pz) * nx + tg.box_x0 + px) * ypitch + y0 + 2 * part;
+        const long long dstep = ((long long)sq * nx + sr) * ypitch, dwrap = (long long)(nx - xn) * ypitch;
+        float2 *dst = buf + pidx * R2_Y + 2 * part;
+        for (; pidx < np; pidx += step) {
+            cp_async16(dst, src);
+            dst += step * R2_Y;
+            src += dstep;
+            px += sr;
+            if (px >= xn) {
+                px -= xn;
+                src += dwrap;
+            }
+        }
+        return;
+    }
+    for (; pidx < np; pidx += step) {
+        const int mz = mirror_idx(tg.box_z0 + pz, nz), mx = mirror_idx(tg.box_x0 + px, nx);
+        cp_async16(buf + pidx * R2_Y + 2 * part, aslab + ((size_t)mz * nx + mx) * ypitch + y0 + 2 * part);
+        px += sr;
+        pz += sq;
+        if (px >= xn) {
+            px -= xn;
+            ++pz;
+        }
     }
 }
 
@@ -303,141 +363,183 @@ __device__ __forceinline__ TileGeo load_tile(const TileGeo *p)
     int4 *d = reinterpret_cast<int4 *>(&t);
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-        d[k] = __ldg(s + k);
+        d[k] = s[k];
     return t;
 }
 
-template <int ORDER, bool ONLYREAL>
-__global__ void __launch_bounds__(256, 3) k_rotate_y(RotParams R, const float2 *__restrict__ slab,
-                                                     const double *__restrict__ geo,
-                                                     const TileGeo *__restrict__ tiles, void *volume,
-                                                     float2 *comp)
+// Parameter record of output (oz, ox) for one angle: word 0 box offset of
+// the first tap (float2 units), word 1 in/out flag, then (wz_i, wz_i) pairs
+// and (wx_k, wx_k) pairs, i, k = 0..ORDER.
+template <int ORDER>
+__device__ __forceinline__ void output_params(const RotParams &R, const TileGeo &cur, const double *g, int oz0,
+                                              int ox0, int oz, int ox, float *rec)
 {
-    __shared__ float2 box[2][RY_BOX * RY_BP];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int ntx = (R.nx + RY_T - 1) / RY_T, ntz = (R.nz + RY_T - 1) / RY_T;
-    const int tile = blockIdx.y * ntx + blockIdx.x;
-    const int ox0 = blockIdx.x * RY_T, oz0 = blockIdx.y * RY_T, y = blockIdx.z;
-    const int nx = R.nx, nz = R.nz, ny = R.ny;
-    const int ox = ox0 + tx;
-    const int nb = R.nbatch_angles;
-    const size_t plane_stride = (size_t)nz * nx;
-    float2 s[4], cp[4], part[4];
+    int off = 0, ok = 0;
+    float wz[4] = {0.f, 0.f, 0.f, 0.f}, wx[4] = {0.f, 0.f, 0.f, 0.f};
+    const int nz = R.nz, nx = R.nx;
+    if (cur.box_zn > 0 && oz < nz && ox < nx) {
+        int Iz, Ix;
+        const float dz = (float)(oz - oz0), dx = (float)(ox - ox0);
+        const float lz = eval_axis(cur.z, dz, dx, Iz);
+        const float lx = eval_axis(cur.x, dz, dx, Ix);
+        bool in = true;
+        if (!cur.interior) {
+            in = inside_axis(lz, Iz, nz, [&] {
+                return __dadd_rn(__dadd_rn(__ldg(g + 4), __dmul_rn(__ldg(g + 0), (double)oz)),
+                                 __dmul_rn(__ldg(g + 1), (double)ox));
+            });
+            in = in && inside_axis(lx, Ix, nx, [&] {
+                return __dadd_rn(__dadd_rn(__ldg(g + 5), __dmul_rn(__ldg(g + 2), (double)oz)),
+                                 __dmul_rn(__ldg(g + 3), (double)ox));
+            });
+        }
+        if (in) {
+            int tz0, tx0;
+            if (ORDER == 0) {
+                // nearest neighbour: the rounding point is a discontinuity,
+                // so take the tap from the exact FP64 coordinate
+                const double cz = __dadd_rn(__dadd_rn(__ldg(g + 4), __dmul_rn(__ldg(g + 0), (double)oz)),
+                                            __dmul_rn(__ldg(g + 1), (double)ox));
+                const double cx = __dadd_rn(__dadd_rn(__ldg(g + 5), __dmul_rn(__ldg(g + 2), (double)oz)),
+                                            __dmul_rn(__ldg(g + 3), (double)ox));
+                tz0 = (int)floor(cz + 0.5);
+                tx0 = (int)floor(cx + 0.5);
+                wz[0] = 1.f;
+                wx[0] = 1.f;
+            } else {
+                float w[ORDER + 1];
+                tz0 = Iz + Spline<ORDER>::weights(lz, w);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+                for (int k = 0; k <= ORDER; ++k)
+                    wz[k] = w[k];
+                tx0 = Ix + Spline<ORDER>::weights(lx, w);
+#pragma unroll
+                for (int k = 0; k <= ORDER; ++k)
+                    wx[k] = w[k];
+            }
+            const int rz = tz0 - cur.box_z0, rx = tx0 - cur.box_x0;
+            if (rz >= 0 && rz + ORDER < cur.box_zn && rx >= 0 && rx + ORDER < cur.box_xn) {
+                off = (rz * cur.box_xn + rx) * R2_Y;
+                ok = 1;
+            } else {
+                atomicOr(R.status, DEVCHK_BOX_OVERFLOW);  // tap outside the staged box
+            }
+        }
+    }
+    float4 *r4 = reinterpret_cast<float4 *>(rec);
+    r4[0] = make_float4(__int_as_float(off), __int_as_float(ok), 0.f, 0.f);
+    float2 *w2 = reinterpret_cast<float2 *>(rec + 4);
+#pragma unroll
+    for (int k = 0; k <= ORDER; ++k) {
+        w2[k] = make_float2(wz[k], wz[k]);
+        w2[ORDER + 1 + k] = make_float2(wx[k], wx[k]);
+    }
+}
+
+template <int ORDER, bool ONLYREAL>
+__global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const float2 *__restrict__ slab,
+                                                            const double *__restrict__ geo,
+                                                            const TileGeo *__restrict__ tiles, void *volume,
+                                                            float2 *comp)
+{
+    extern __shared__ float4 r2_smem[];
+    float2 *box = reinterpret_cast<float2 *>(r2_smem);       // [2][R2_BOXE]
+    constexpr int PW = r2_words<ORDER>();
+    float *prm = reinterpret_cast<float *>(box + 2 * R2_BOXE); // [256][PW]
+    TileGeo *ring = reinterpret_cast<TileGeo *>(prm + R2_T * R2_T * r2_words<3>());  // [R2_RING]
+    const int tid = threadIdx.x;
+    const int hw = tid >> 4, yl = tid & 15;
+    const int ntx = (R.nx + R2_T - 1) / R2_T, ntz = (R.nz + R2_T - 1) / R2_T;
+    const int tile = blockIdx.y * ntx + blockIdx.x;
+    const int ox0 = blockIdx.x * R2_T, oz0 = blockIdx.y * R2_T, y0 = blockIdx.z * R2_Y;
+    const int nx = R.nx, nz = R.nz, ny = R.ny, yp = R.ypitch;
+    const int nb = R.nbatch_angles;
+    const size_t aslab_stride = (size_t)nz * nx * yp;
+    // this thread's outputs: x = ox0 + (hw & 15), z = oz0 + (hw >> 4) * 8 + i
+    const int hx = hw & 15, hz0 = (hw >> 4) * R2_OUT;
+    float2 s[R2_OUT], cp[R2_OUT], part[R2_OUT];
+#pragma unroll
+    for (int q = 0; q < R2_OUT; ++q) {
         s[q] = make_float2(0.f, 0.f);
         cp[q] = make_float2(0.f, 0.f);
         part[q] = make_float2(0.f, 0.f);
     }
-    TileGeo cur = load_tile(tiles + (size_t)0 * ntz * ntx + tile);
+    // tile records: angles 0..2 now; angle a+3 travels with the footprint
+    // copy of angle a+1, so a record is in shared memory two angles before
+    // its footprint copy is issued
+    const size_t rec_stride = (size_t)ntz * ntx;
+    if (tid < 12 && tid / 4 < nb)
+        reinterpret_cast<int4 *>(ring + tid / 4)[tid % 4] =
+            __ldg(reinterpret_cast<const int4 *>(tiles + (size_t)(tid / 4) * rec_stride + tile) + tid % 4);
+    __syncthreads();
+    TileGeo cur = load_tile(ring);
     if (cur.box_zn > 0)
-        stage_box(cur, slab + ((size_t)0 * ny + y) * plane_stride, nx, box[0]);
+        stage_box(cur, slab, nz, nx, yp, y0, box);
     cp_async_commit();
-    const float dx = (float)(ox - ox0);
     for (int a = 0; a < nb; ++a) {
-        TileGeo nxt;
         if (a + 1 < nb) {
-            nxt = load_tile(tiles + (size_t)(a + 1) * ntz * ntx + tile);
+            const TileGeo nxt = load_tile(ring + (a + 1) % R2_RING);
             if (nxt.box_zn > 0)
-                stage_box(nxt, slab + ((size_t)(a + 1) * ny + y) * plane_stride, nx, box[(a + 1) & 1]);
+                stage_box(nxt, slab + (size_t)(a + 1) * aslab_stride, nz, nx, yp, y0, box + ((a + 1) & 1) * R2_BOXE);
         }
+        if (a + 3 < nb && tid < 4)
+            cp_async16(reinterpret_cast<int4 *>(ring + (a + 3) % R2_RING) + tid,
+                       reinterpret_cast<const int4 *>(tiles + (size_t)(a + 3) * rec_stride + tile) + tid);
         cp_async_commit();
+        if (tid < R2_T * R2_T)
+            output_params<ORDER>(R, cur, geo + 6 * (size_t)a, oz0, ox0, oz0 + (tid >> 4), ox0 + (tid & 15),
+                                 prm + tid * PW);
         cp_async_wait<1>();
         __syncthreads();
         if (cur.box_zn > 0) {
-            const float2 *b = box[a & 1];
-            const int bz0 = cur.box_z0, bx0 = cur.box_x0;
-            const bool interior = cur.interior != 0;
+            const float2 *b = box + (a & 1) * R2_BOXE + yl;
+            const int rowstride = cur.box_xn * R2_Y;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int oz = oz0 + ty + 8 * q;
-                if (oz >= nz || ox >= nx)
+            for (int q = 0; q < R2_OUT; ++q) {
+                const float *rec = prm + ((hz0 + q) * R2_T + hx) * PW;
+                const float4 h = *reinterpret_cast<const float4 *>(rec);
+                if (__float_as_int(h.y) == 0)
                     continue;
-                const float dz = (float)(oz - oz0);
-                int Iz, Ix;
-                const float lz = eval_axis(cur.z, dz, dx, Iz);
-                const float lx = eval_axis(cur.x, dz, dx, Ix);
-                if (!interior) {
-                    const double *g = geo + 6 * (size_t)a;
-                    const bool in_z = inside_axis(lz, Iz, nz, [&] {
-                        return __dadd_rn(__dadd_rn(__ldg(g + 4), __dmul_rn(__ldg(g + 0), (double)oz)),
-                                         __dmul_rn(__ldg(g + 1), (double)ox));
-                    });
-                    if (!in_z)
-                        continue;
-                    const bool in_x = inside_axis(lx, Ix, nx, [&] {
-                        return __dadd_rn(__dadd_rn(__ldg(g + 5), __dmul_rn(__ldg(g + 2), (double)oz)),
-                                         __dmul_rn(__ldg(g + 3), (double)ox));
-                    });
-                    if (!in_x)
-                        continue;
-                }
-                int tz0, tx0;
-                float wz[ORDER + 1], wx[ORDER + 1];
-                if (ORDER == 0) {
-                    // nearest neighbour: the rounding point is a
-                    // discontinuity, so take the tap from the exact FP64
-                    // coordinate
-                    const double *g = geo + 6 * (size_t)a;
-                    const double cz = __dadd_rn(__dadd_rn(__ldg(g + 4), __dmul_rn(__ldg(g + 0), (double)oz)),
-                                                __dmul_rn(__ldg(g + 1), (double)ox));
-                    const double cx = __dadd_rn(__dadd_rn(__ldg(g + 5), __dmul_rn(__ldg(g + 2), (double)oz)),
-                                                __dmul_rn(__ldg(g + 3), (double)ox));
-                    tz0 = (int)floor(cz + 0.5);
-                    tx0 = (int)floor(cx + 0.5);
-                    wz[0] = 1.f;
-                    wx[0] = 1.f;
-                } else {
-                    tz0 = Iz + Spline<ORDER>::weights(lz, wz);
-                    tx0 = Ix + Spline<ORDER>::weights(lx, wx);
-                }
-                int rz[ORDER + 1], cx[ORDER + 1];
+                float2 w[2 * (ORDER + 1)];
 #pragma unroll
-                for (int k = 0; k <= ORDER; ++k) {
-                    if (interior) {
-                        rz[k] = (tz0 + k - bz0) * RY_BP;
-                        cx[k] = tx0 + k - bx0;
-                    } else {
-                        rz[k] = (mirror_idx(tz0 + k, nz) - bz0) * RY_BP;
-                        cx[k] = mirror_idx(tx0 + k, nx) - bx0;
-                    }
+                for (int k = 0; k < 2 * (ORDER + 1); k += 2) {
+                    const float4 t4 = *reinterpret_cast<const float4 *>(rec + 4 + 2 * k);
+                    w[k] = make_float2(t4.x, t4.y);
+                    w[k + 1] = make_float2(t4.z, t4.w);
                 }
-                float2 acc = make_float2(0.f, 0.f);
+                const float2 *t = b + __float_as_int(h.x);
+                float2 acc = part[q];
 #pragma unroll
                 for (int i = 0; i <= ORDER; ++i) {
-                    const float2 *brow = b + rz[i];
+                    const float2 *row = t + i * rowstride;
                     float2 r = make_float2(0.f, 0.f);
 #pragma unroll
-                    for (int k = 0; k <= ORDER; ++k) {
-                        const float2 v = brow[cx[k]];
-                        r.x = fmaf(wx[k], v.x, r.x);
-                        if (!ONLYREAL)
-                            r.y = fmaf(wx[k], v.y, r.y);
-                    }
-                    acc.x = fmaf(wz[i], r.x, acc.x);
-                    if (!ONLYREAL)
-                        acc.y = fmaf(wz[i], r.y, acc.y);
+                    for (int k = 0; k <= ORDER; ++k)
+                        r = ffma2(w[ORDER + 1 + k], row[k * R2_Y], r);
+                    acc = ffma2(w[i], r, acc);
                 }
-                part[q].x += acc.x;
-                part[q].y += acc.y;
+                part[q] = acc;
             }
         }
-        if ((a % RY_KAHAN) == RY_KAHAN - 1 || a == nb - 1) {
+        if ((a % R2_KAHAN) == R2_KAHAN - 1 || a == nb - 1) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < R2_OUT; ++q) {
                 kahan_add(s[q], cp[q], part[q]);
                 part[q] = make_float2(0.f, 0.f);
             }
         }
         __syncthreads();
         if (a + 1 < nb)
-            cur = nxt;
+            cur = load_tile(ring + (a + 1) % R2_RING);
     }
+    const int y = y0 + yl, ox = ox0 + hx;
+    if (y < ny && ox < nx) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int oz = oz0 + ty + 8 * q;
-        if (oz < nz && ox < nx)
-            store_sum<ONLYREAL>(R, volume, comp, ((size_t)oz * ny + y) * nx + ox, s[q], cp[q]);
+        for (int q = 0; q < R2_OUT; ++q) {
+            const int oz = oz0 + hz0 + q;
+            if (oz < nz)
+                store_sum<ONLYREAL>(R, volume, comp, ((size_t)oz * ny + y) * nx + ox, s[q], cp[q]);
+        }
     }
 }
 
@@ -545,12 +647,12 @@ static cudaError_t rotate_impl(const RotParams &R, int tilted, const float2 *sla
                                float2 *comp, void *scratch, cudaStream_t s)
 {
     if (!tilted) {
-        const int ntiles = ((R.nx + RY_T - 1) / RY_T) * ((R.nz + RY_T - 1) / RY_T);
+        const int ntiles = ((R.nx + R2_T - 1) / R2_T) * ((R.nz + R2_T - 1) / R2_T);
         const int nset = R.nbatch_angles * ntiles;
         TileGeo *tiles = reinterpret_cast<TileGeo *>(scratch);
         k_rotate_y_setup<ORDER><<<(nset + 127) / 128, 128, 0, s>>>(R, geo, tiles);
-        dim3 grid((R.nx + RY_T - 1) / RY_T, (R.nz + RY_T - 1) / RY_T, R.ny);
-        k_rotate_y<ORDER, ONLYREAL><<<grid, 256, 0, s>>>(R, slab, geo, tiles, volume, comp);
+        dim3 grid((R.nx + R2_T - 1) / R2_T, (R.nz + R2_T - 1) / R2_T, (R.ny + R2_Y - 1) / R2_Y);
+        k_rotate_y<ORDER, ONLYREAL><<<grid, R2_THREADS, R2_SMEM, s>>>(R, slab, geo, tiles, volume, comp);
     } else {
         dim3 grid((R.nx + 31) / 32, (R.ny + 7) / 8, R.nz);
         k_rotate_3d<ORDER, ONLYREAL><<<grid, 256, 0, s>>>(R, slab, geo, volume, comp);
@@ -563,8 +665,22 @@ size_t rotate_scratch_bytes(int nbatch_angles, int ny, int nx, int nz, int tilte
     (void)ny;
     if (tilted)
         return 0;
-    const size_t ntiles = (size_t)((nx + RY_T - 1) / RY_T) * ((nz + RY_T - 1) / RY_T);
+    const size_t ntiles = (size_t)((nx + R2_T - 1) / R2_T) * ((nz + R2_T - 1) / R2_T);
     return (size_t)nbatch_angles * ntiles * sizeof(TileGeo);
+}
+
+cudaError_t configure_rotate_kernels()
+{
+    const void *fns[] = {
+        (const void *)k_rotate_y<0, false>, (const void *)k_rotate_y<0, true>, (const void *)k_rotate_y<1, false>,
+        (const void *)k_rotate_y<1, true>,  (const void *)k_rotate_y<2, false>, (const void *)k_rotate_y<2, true>,
+        (const void *)k_rotate_y<3, false>, (const void *)k_rotate_y<3, true>};
+    for (const void *f : fns) {
+        const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)R2_SMEM);
+        if (e != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_rotate(const RotParams &R, int order, int tilted, const float2 *slab, const double *geo,

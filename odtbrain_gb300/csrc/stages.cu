@@ -257,6 +257,11 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
 // ---------------------------------------------------------------------------
 // (b2) rows: (+ z-boundary rows), backward FFT along x, x-prefilter boundary
 // terms, crop -> slab.
+// Tilted path: slab[a][z][y][x], one CTA line per (job, y) row.
+// y-axis path: slab[a][z][x][y] with the y pitch P.ypitch (a multiple of
+// LPC and of 16): the LPC lines of a CTA are consecutive y of one plane, the
+// cropped rows are transposed through shared memory and stored as runs of
+// LPC consecutive y per x (rows y >= ny are zero).
 template <class L, int LPC>
 __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L line, const float2 *T,
                                                                const float2 *Tab, float2 *slab, int q0, int qn)
@@ -269,17 +274,21 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
     const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl;
+    const bool yaxis = !P.tilted;
+    const int rows = yaxis ? P.ypitch : ny;  // rows per job in the grid
     const long long rid = (long long)blockIdx.x * LPC + l;
-    const bool valid = rid < (long long)qn * ny;
-    const int qq = q0 + (int)((valid ? rid : 0) / ny);
-    const int y = (int)((valid ? rid : 0) % ny);
+    const int qrel = (int)(rid / rows);
+    const int y = (int)(rid % rows);
+    const bool valid = qrel < qn && y < ny;
+    const int qq = q0 + (qrel < qn ? qrel : qn - 1);
+    const int yc = y < ny ? y : ny - 1;
     const int a = qq / nz, p = qq % nz;
     const bool pf = P.order >= 2;
     const float zl = (pf && p < ZPOW_N) ? P.tab.zpow[p] : 0.f;
     const float zh = (pf && nz - 1 - p < ZPOW_N) ? P.tab.zpow[nz - 1 - p] : 0.f;
-    const float2 *src = T + (size_t)(valid ? rid : 0) * n;
-    const float2 *ta = Tab + ((size_t)(a * 2 + 0) * ny + y) * n;
-    const float2 *tb = Tab + ((size_t)(a * 2 + 1) * ny + y) * n;
+    const float2 *src = T + ((size_t)(qq - q0) * ny + yc) * n;
+    const float2 *ta = Tab + ((size_t)(a * 2 + 0) * ny + yc) * n;
+    const float2 *tb = Tab + ((size_t)(a * 2 + 1) * ny + yc) * n;
     float2 v[L::SLOTS];
 #pragma unroll
     for (int r = 0; r < L::SLOTS; ++r) {
@@ -316,31 +325,50 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
         Acoef = make_float2(P.bx_ca * d0.x + P.bx_cb * d1.x, P.bx_ca * d0.y + P.bx_cb * d1.y);
         Bcoef = make_float2(P.bx_ca * d1.x + P.bx_cb * d0.x, P.bx_ca * d1.y + P.bx_cb * d0.y);
     }
-    if (!valid)
+    // boundary-corrected value o of cropped sample xx of this line
+    auto cropped = [&](float2 o, int xx) {
+        if (pf) {
+            if (xx < ZPOW_N) {
+                const float zz = P.tab.zpow[xx];
+                o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
+            }
+            if (nx - 1 - xx < ZPOW_N) {
+                const float zz = P.tab.zpow[nx - 1 - xx];
+                o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
+            }
+        }
+        return o;
+    };
+    if (!yaxis) {
+        if (!valid)
+            return;
+        float2 *dst = slab + (((size_t)a * nz + p) * ny + y) * nx;
+#pragma unroll
+        for (int r = 0; r < L::SLOTS; ++r) {
+            const int xx = j + r * L::TPL - padxl;
+            if (xx >= 0 && xx < nx)
+                __stcs(dst + xx, cropped(v[r], xx));  // streamed: keep L2 for the column stage output
+        }
         return;
-    size_t base;
-    if (P.tilted)
-        base = (((size_t)a * nz + p) * ny + y) * nx;
-    else
-        base = (((size_t)a * ny + y) * nz + p) * nx;
-    float2 *dst = slab + base;
+    }
+    // y-axis: stage[x][l] (pitch LPC+1), then runs of LPC y per x
+    __syncthreads();  // every line is done with buf0
+    float2 *stage = buf0;
+    constexpr int SP = LPC + 1;
 #pragma unroll
     for (int r = 0; r < L::SLOTS; ++r) {
         const int xx = j + r * L::TPL - padxl;
-        if (xx >= 0 && xx < nx) {
-            float2 o = v[r];
-            if (pf) {
-                if (xx < ZPOW_N) {
-                    const float zz = P.tab.zpow[xx];
-                    o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
-                }
-                if (nx - 1 - xx < ZPOW_N) {
-                    const float zz = P.tab.zpow[nx - 1 - xx];
-                    o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
-                }
-            }
-            __stcs(dst + xx, o);  // streamed: keep L2 for the column stage output
-        }
+        if (xx >= 0 && xx < nx)
+            stage[xx * SP + l] = valid ? cropped(v[r], xx) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    if (qrel >= qn)
+        return;
+    const int ybase = (int)(((long long)blockIdx.x * LPC) % rows);
+    float2 *dst = slab + ((size_t)a * nz + p) * nx * P.ypitch + ybase;
+    for (int e = threadIdx.x; e < nx * LPC; e += LPC * L::TPL) {
+        const int xx = e / LPC, ll = e % LPC;
+        __stcs(dst + (size_t)xx * P.ypitch + ll, stage[xx * SP + ll]);
     }
 }
 
@@ -384,7 +412,7 @@ static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 
                                      float2 *slab, int q0, int qn, cudaStream_t s)
 {
     constexpr int LPC = Cfg<L>::LPC;
-    const long long lines = (long long)qn * P.ny;
+    const long long lines = (long long)qn * (P.tilted ? P.ny : P.ypitch);
     const unsigned grid = (unsigned)((lines + LPC - 1) / LPC);
     k_rows_inverse<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, Tab, slab, q0, qn);
     return cudaGetLastError();
