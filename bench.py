@@ -19,7 +19,10 @@ value   device-resident throughput (sinogram already in HBM; the prepared
 e2e     the same metric through the public API ``backpropagate_3d`` with a
         pinned host sinogram in and a host volume out (H2D + D2H inside)
 roofline  the dominant kernel stage, timed live with CUDA events around
-        each of its launches, against MEASURED_PEAKS.json's HBM bandwidth
+        each of its launches, against MEASURED_PEAKS.json's HBM bandwidth;
+        for the FFT stages (FP32-arithmetic bound, L2-resident data) also
+        their FP32 rate against the nominal FP32 peak ("fp32")
+roofline_rotate  the resampling/accumulation stage against HBM
 cpu_baseline  the FP64 oracle port on this host's cores, on a bounded
         sample of the same workload (a few angles)
 With --gpus N > 1 (torchrun), every rank runs an independent replica of the
@@ -177,6 +180,28 @@ def measured_peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def stage_flops(rec, A):
+    """Algorithmic FP32 flops of the two FFT stages of one reconstruction:
+    5 N log2 N per complex N-point transform, 6 per complex multiply.
+    Column stage: the forward y transform of every nonzero spectrum column
+    once per angle, then per plane the propagator multiply and the backward
+    y transform of those columns; row stage: per plane the backward x
+    transform of every cropped row."""
+    import math
+    g = rec.padding_geometry
+    lNy, lNx = g["lNy"], g["lNx"]
+    _A, ny, nx = rec.shape
+    nz = nx
+    cols = np.unique(rec.filter_support() % lNx).size
+
+    def f(n):
+        return 5.0 * n * math.log2(n)
+    planes = A * nz
+    return {"columns_propagate": planes * cols * (f(lNy) + 6 * lNy)
+            + A * cols * f(lNy),
+            "rows_inverse": planes * ny * f(lNx)}
 
 
 def profile_traffic(stage):
@@ -376,6 +401,31 @@ def run_ours(args):
                 "traffic": traffic,
                 "algorithmic_bytes_per_launch": per_launch_bytes,
                 "launch_ms": per_launch_s * 1e3}
+    # the FFT stages are FP32-arithmetic bound (their inputs and outputs stay
+    # in L2): their compute roofline, algorithmic flops 5 N log2 N per
+    # complex N-point transform plus 6 per propagator multiply, against the
+    # nominal FP32 rate 152 SMs x 128 lanes x 2 flops at the median SM clock
+    # sampled during the timed steps
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fl = stage_flops(rec, A)
+    fp32 = {k: {"tflops": fl[k] / (stages[k]["ms"] / 1e3) / 1e12,
+                "frac": fl[k] / (stages[k]["ms"] / 1e3) / 1e12 / fp32_peak,
+                "algorithmic_gflop": fl[k] / 1e9}
+            for k in fl if stages.get(k, {}).get("ms")}
+    if dom in fp32:
+        roofline["fp32"] = dict(fp32[dom], peak_tflops=fp32_peak,
+                                peak_source="nominal at %.0f MHz" % sm_mhz)
+    # rotate-accumulate against HBM: slab read + volume traffic
+    rs = stages["rotate"]
+    rot_achieved = rs["bytes"] / (rs["ms"] / 1e3) / 1e9
+    roofline_rotate = {"bound": "hbm", "kernel": "rotate",
+                       "achieved": rot_achieved, "peak": peak, "unit": "GB/s",
+                       "frac": rot_achieved / peak,
+                       "traffic": profile_traffic("rotate"),
+                       "algorithmic_bytes_per_launch":
+                           rs["bytes"] / rs["launches"],
+                       "launch_ms": rs["ms"] / rs["launches"]}
     stage_summary = {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
                          "share": round(v["ms"] / sum(x["ms"] for x in
                                                       stages.values()), 4),
@@ -451,6 +501,8 @@ def run_ours(args):
             "e2e": e2e,
             "gpu_launches": rec.launches_per_call * args.steps,
             "roofline": roofline,
+            "roofline_rotate": roofline_rotate,
+            "fp32_stages": fp32,
             "stages": stage_summary,
             "save_memory_ms_per_step": sm_ms,
             "save_memory_max_rel_diff": sm_diff,

@@ -32,7 +32,8 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_adj_rows(StageParams P, L line
 {
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNx
-    float2 *buf0 = smem, *buf1 = smem + LPC * n, *tw = smem + 2 * LPC * n;
+    const int xs = xslots<false>(n);
+    float2 *buf0 = smem, *buf1 = smem + LPC * xs, *tw = smem + 2 * LPC * xs;
     float2 *red = tw + n;  // [LPC][2] boundary sums
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_adj_rows(StageParams P, L line
         }
     }
     int flip = 0;
-    line.template run<-1>(v, j, buf0 + l * n, buf1 + l * n, 1, tw, flip);
+    line.template run<-1>(v, j, buf0 + l * xs, buf1 + l * xs, 1, tw, flip);
     if (!valid)
         return;
     float2 *dst = Tg + (size_t)rid * n;
@@ -118,7 +119,8 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_columns(StageParams P, L li
         return;
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNy
-    float2 *buf0 = smem, *buf1 = smem + KX * n, *tw = smem + 2 * KX * n;
+    const int xs = xslots<true>(n);
+    float2 *buf0 = smem, *buf1 = smem + KX * xs, *tw = smem + 2 * KX * xs;
     float2 *stp = tw + n;  // [n][KX]
     copy_twiddles<L>(tw, P.tab.twy, n);
     const int c = threadIdx.x % KX, j = threadIdx.x / KX;
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_columns(StageParams P, L li
             const int yy = j + r * L::TPL - padyl;
             v[r] = (colok && yy >= 0 && yy < ny) ? src[(size_t)yy * lNx] : make_float2(0.f, 0.f);
         }
-        line.template run<-1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+        line.template run<-1, true>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
         const float zl = (pf && p < ZPOW_N) ? P.tab.zpow[p] : 0.f;
         const float zh = (pf && nz - 1 - p < ZPOW_N) ? P.tab.zpow[nz - 1 - p] : 0.f;
 #pragma unroll
@@ -217,7 +219,8 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_spectrum(StageParams P, L l
         return;
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNy
-    float2 *buf0 = smem, *buf1 = smem + KX * n, *tw = smem + 2 * KX * n;
+    const int xs = xslots<true>(n);
+    float2 *buf0 = smem, *buf1 = smem + KX * xs, *tw = smem + 2 * KX * xs;
     copy_twiddles<L>(tw, P.tab.twy, n);
     const int c = threadIdx.x % KX, j = threadIdx.x / KX;
     const int kx = blockIdx.x * KX + c;
@@ -234,7 +237,7 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_spectrum(StageParams P, L l
             const int ky = j + r * L::TPL;
             X[r] = (colok && ky < n) ? rowspec[((size_t)a * n + ky) * lNx + kx] : make_float2(0.f, 0.f);
         }
-        line.template run<-1>(X, j, buf0 + c, buf1 + c, KX, tw, flip);
+        line.template run<-1, true>(X, j, buf0 + c, buf1 + c, KX, tw, flip);
     }
     float2 v[L::SLOTS];
 #pragma unroll
@@ -263,7 +266,7 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_spectrum(StageParams P, L l
             v[r] = make_float2(h.x * q.x + h.y * q.y, h.x * q.y - h.y * q.x);
         }
     }
-    line.template run<1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+    line.template run<1, true>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
     if (!colok)
         return;
 #pragma unroll
@@ -281,7 +284,8 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_adj_rows_full(StageParams P, L
 {
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNx
-    float2 *buf0 = smem, *buf1 = smem + LPC * n, *tw = smem + 2 * LPC * n;
+    const int xs = xslots<false>(n);
+    float2 *buf0 = smem, *buf1 = smem + LPC * xs, *tw = smem + 2 * LPC * xs;
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
     const long long lid = (long long)blockIdx.x * LPC + l;
@@ -295,7 +299,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_adj_rows_full(StageParams P, L
     }
     __syncthreads();
     int flip = 0;
-    line.template run<1>(v, j, buf0 + l * n, buf1 + l * n, 1, tw, flip);
+    line.template run<1>(v, j, buf0 + l * xs, buf1 + l * xs, 1, tw, flip);
     if (!valid)
         return;
     float2 *dst = Pg + (size_t)lid * n;
@@ -357,9 +361,15 @@ __global__ void k_adj_pad(StageParams P, const float2 *Pg, const double *weights
 constexpr int kAdjPlanesPerBlock = 16;
 
 template <class L>
-static size_t smem_adj_rows(int n) { return (size_t)(2 * Cfg<L>::LPC * n + n + 2 * Cfg<L>::LPC) * sizeof(float2); }
+static size_t smem_adj_rows(int n)
+{
+    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + n + 2 * Cfg<L>::LPC) * sizeof(float2);
+}
 template <class L>
-static size_t smem_adj_cols(int n) { return (size_t)(3 * Cfg<L>::KX * n + n) * sizeof(float2); }
+static size_t smem_adj_cols(int n)
+{
+    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + Cfg<L>::KX * n + n) * sizeof(float2);
+}
 
 template <class L>
 static cudaError_t set_adj_attrs(int n)

@@ -22,8 +22,29 @@
 
 namespace odt {
 
-__device__ __forceinline__ float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add / subtract as one packed FP32 instruction each (sm_100+
+// .f32x2 forms; every component rounds exactly like the scalar operation).
+__device__ __forceinline__ unsigned long long f2bits(float2 a) { return *reinterpret_cast<unsigned long long *>(&a); }
+__device__ __forceinline__ float2 bitsf2(unsigned long long d) { return *reinterpret_cast<float2 *>(&d); }
+__device__ __forceinline__ float2 operator+(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2bits(a)), "l"(f2bits(b)));
+    return bitsf2(d);
+}
+__device__ __forceinline__ float2 operator-(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2bits(a)), "l"(f2bits(b)));
+    return bitsf2(d);
+}
+// s * a + c with a real scalar s (one packed FMA)
+__device__ __forceinline__ float2 sfma2(float s, float2 a, float2 c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2bits(make_float2(s, s))), "l"(f2bits(a)), "l"(f2bits(c)));
+    return bitsf2(d);
+}
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
@@ -54,14 +75,21 @@ __device__ __forceinline__ void dft2(float2 &a, float2 &b)
     b = t - b;
 }
 
+// a + DIR*i*d and a - DIR*i*d
+template <int DIR>
+__device__ __forceinline__ void add_sub_i(float2 a, float2 d, float2 &p, float2 &m)
+{
+    p = make_float2(a.x - DIR * d.y, a.y + DIR * d.x);
+    m = make_float2(a.x + DIR * d.y, a.y - DIR * d.x);
+}
+
 template <int DIR>
 __device__ __forceinline__ void dft4(float2 &x0, float2 &x1, float2 &x2, float2 &x3)
 {
-    float2 a0 = x0 + x2, a1 = x0 - x2, a2 = x1 + x3, a3 = mul_i<DIR>(x1 - x3);
+    const float2 a0 = x0 + x2, a1 = x0 - x2, a2 = x1 + x3, d = x1 - x3;
     x0 = a0 + a2;
     x2 = a0 - a2;
-    x1 = a1 + a3;
-    x3 = a1 - a3;
+    add_sub_i<DIR>(a1, d, x1, x3);
 }
 
 template <int DIR>
@@ -72,30 +100,41 @@ __device__ __forceinline__ void dft8(float2 *x)
     dft4<DIR>(e0, e1, e2, e3);
     dft4<DIR>(o0, o1, o2, o3);
     const float r = 0.70710678118654752440f;
-    // o1 *= (1 + DIR i)/sqrt2 ; o2 *= DIR i ; o3 *= (-1 + DIR i)/sqrt2
-    o1 = make_float2((o1.x - DIR * o1.y) * r, (o1.y + DIR * o1.x) * r);
-    o2 = mul_i<DIR>(o2);
-    o3 = make_float2((-o3.x - DIR * o3.y) * r, (-o3.y + DIR * o3.x) * r);
+    // o1 *= (1 + DIR i)/sqrt2 ; o2 *= DIR i ; o3 *= (-1 + DIR i)/sqrt2, the
+    // 1/sqrt2 folded into packed FMAs with the even half
+    const float2 t1 = make_float2(o1.x - DIR * o1.y, o1.y + DIR * o1.x);
+    const float2 t3 = make_float2(o3.x + DIR * o3.y, o3.y - DIR * o3.x);  // -o3 rotated
     x[0] = e0 + o0;
     x[4] = e0 - o0;
-    x[1] = e1 + o1;
-    x[5] = e1 - o1;
-    x[2] = e2 + o2;
-    x[6] = e2 - o2;
-    x[3] = e3 + o3;
-    x[7] = e3 - o3;
+    x[1] = sfma2(r, t1, e1);
+    x[5] = sfma2(-r, t1, e1);
+    add_sub_i<DIR>(e2, o2, x[2], x[6]);
+    x[3] = sfma2(-r, t3, e3);
+    x[7] = sfma2(r, t3, e3);
 }
 
 constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
-// Exchange-buffer slot of line position p: bits 3..6 are XORed into bits
-// 0..3.  This permutes each 128-position block, and makes every access
-// pattern of the Stockham passes (unit-stride reads, stride-8 and stride-64
-// writes) hit distinct banks within a half-warp, for element strides 1, 2,
-// 4, 8 and 16 (the row and column buffer layouts).
-__device__ __forceinline__ int xslot(int p) { return p ^ ((p >> 3) & 15); }
-// Slots a line of n positions occupies in an exchange buffer.
-__host__ __device__ constexpr int xslots(int n) { return n; }
+// Exchange-buffer slot of line position p.  The Stockham passes read
+// positions j + r*TPL and write positions 8*j' + r (first pass) or
+// blocks + 8*r (later passes).
+// Row layout (element stride 1, the threads of a half-warp on one line):
+//   bits 3..6 XORed into bits 0..3, conflict-free for every pattern.
+// Column layout (KX interleaved lines, a half-warp spans 8 lines and 2
+//   positions): one slot of padding after every 8 positions, conflict-free
+//   there, and every slot is a per-thread base plus a compile-time offset,
+//   so those exchanges need no index arithmetic per element.
+template <bool PAD>
+__device__ __forceinline__ int xslot(int p)
+{
+    return PAD ? p + (p >> 3) : p ^ ((p >> 3) & 15);
+}
+// Slots a line of n positions occupies in an exchange buffer of the layout.
+template <bool PAD>
+__host__ __device__ constexpr int xslots(int n)
+{
+    return PAD ? n + n / 8 + 1 : n;
+}
 constexpr int ipow8(int k) { return k == 0 ? 1 : 8 * ipow8(k - 1); }
 
 // Power-of-two line, 64 <= N <= 4096.
@@ -112,7 +151,9 @@ struct Pow2Line {
     // v: positions j + r*TPL in, same positions out.  `line[0/1]` point at
     // element 0 of this line in the two exchange buffers; `es` is the
     // element stride.  `flip` alternates the buffers across exchanges.
-    template <int DIR>
+    // PAD selects the exchange layout (xslot): false for rows, true for
+    // interleaved columns.
+    template <int DIR, bool PAD = false>
     __device__ __forceinline__ void run(float2 (&v)[8], int j, float2 *line0, float2 *line1, int es,
                                         const float2 *tw, int &flip) const
     {
@@ -134,11 +175,11 @@ struct Pow2Line {
             const int idxD = (j / Ns) * Ns * 8 + (j & (Ns - 1));
 #pragma unroll
             for (int r = 0; r < 8; ++r)
-                b[xslot(idxD + r * Ns) * es] = v[r];
+                b[xslot<PAD>(idxD + r * Ns) * es] = v[r];
             __syncthreads();
 #pragma unroll
             for (int r = 0; r < 8; ++r)
-                v[r] = b[xslot(j + r * TPL) * es];
+                v[r] = b[xslot<PAD>(j + r * TPL) * es];
             Ns *= 8;
         }
         if (TAIL == 4) {
@@ -175,7 +216,7 @@ struct GenericLine {
     int n;
     __device__ __forceinline__ int size() const { return n; }
 
-    template <int DIR>
+    template <int DIR, bool PAD = false>
     __device__ __forceinline__ void run(float2 (&v)[16], int j, float2 *line0, float2 *line1, int es,
                                         const float2 *tw, int &flip) const
     {

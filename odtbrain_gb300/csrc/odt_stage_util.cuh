@@ -125,12 +125,12 @@ struct Cfg<GenericLine> {
 template <class L>
 inline size_t smem_rows(int n)
 {
-    return (size_t)(2 * Cfg<L>::LPC * xslots(n) + n + 4 * Cfg<L>::LPC) * sizeof(float2);
+    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + n + 4 * Cfg<L>::LPC) * sizeof(float2);
 }
 template <class L>
 inline size_t smem_cols(int n)
 {
-    return (size_t)(2 * Cfg<L>::KX * xslots(n) + Cfg<L>::KX * n + n + 4 * Cfg<L>::KX) * sizeof(float2);
+    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + Cfg<L>::KX * n + n + 4 * Cfg<L>::KX) * sizeof(float2);
 }
 
 // Calls fn(line) with the line type for length n.

@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_forward(StageParams P, L 
 {
     extern __shared__ float2 smem[];
     const int n = line.size();
-    const int ls = xslots(n);
+    const int ls = xslots<false>(n);
     float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
@@ -87,7 +87,7 @@ __device__ __forceinline__ void column_spectrum(const StageParams &P, const L &l
         const int ky = j + r * L::TPL;
         v[r] = (colok && ky < n) ? rowspec[((size_t)a * n + ky) * P.lNx + kx] : make_float2(0.f, 0.f);
     }
-    line.template run<-1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+    line.template run<-1, true>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
 #pragma unroll
     for (int r = 0; r < L::SLOTS; ++r) {
         const int ky = j + r * L::TPL;
@@ -113,7 +113,7 @@ __device__ __forceinline__ void column_inverse_store(const StageParams &P, const
 {
     const int n = line.size();
     const int ny = P.ny, padyl = P.padyl;
-    line.template run<1>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+    line.template run<1, true>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
     const bool yfix = P.order >= 2 && P.tilted;
     float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
     if (yfix) {
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(KX * L::TPL) k_columns_boundary(StageParams P,
         return;  // all-zero columns: the row stage never reads them
     extern __shared__ float2 smem[];
     const int n = line.size();
-    const int ls = xslots(n);
+    const int ls = xslots<true>(n);
     float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls, *edge = tw + n;
     copy_twiddles<L>(tw, P.tab.twy, n);
     const int c = threadIdx.x % KX, j = threadIdx.x / KX;
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
         return;  // all-zero columns: the row stage never reads them
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNy
-    const int ls = xslots(n);
+    const int ls = xslots<true>(n);
     float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls;
     float2 *edge = tw + n;           // [KX][4]
     float2 *stp = edge + 4 * KX;     // [n][KX] propagator step per element
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
 {
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNx
-    const int ls = xslots(n);
+    const int ls = xslots<false>(n);
     float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
     float2 *edge = tw + n;  // [LPC][4]
     copy_twiddles<L>(tw, P.tab.twx, n);
