@@ -320,9 +320,9 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     // ---- batching: the largest angle batch (and column-stage chunk) whose
     // workspace fits the limit
     const size_t plane_row_bytes = (size_t)d.ny * lNx * 8;           // one job's column-stage output
-    // one angle's coefficient slab ([z][y][x] tilted, [z][x][ypitch] y-axis;
-    // the adjoint's slab gradients [y][z][x] fit either)
-    const size_t slab_bytes = (size_t)nz * (tilted ? d.ny : odt::yaxis_slab_pitch(d.ny)) * d.nx * 8;
+    // one angle's coefficient slab [z][x][ypitch] (the adjoint's slab
+    // gradients [y][z][x] fit too)
+    const size_t slab_bytes = (size_t)nz * odt::yaxis_slab_pitch(d.ny) * d.nx * 8;
     const size_t rowspec_bytes = (size_t)lNy * lNx * 8;              // one angle's row spectra
     const size_t tab_bytes = pf ? (size_t)2 * d.ny * lNx * 8 : 0;    // one angle's z-boundary rows
     const size_t vol_bytes = (size_t)nz * d.ny * d.nx * 8;           // compensation buffer

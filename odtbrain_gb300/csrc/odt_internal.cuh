@@ -32,15 +32,15 @@ struct StageParams {
     int pad_mode;
     float2 padval;
     int order;        // spline order; >= 2 means the prefilter is folded in
-    int tilted;       // 1: slabs for the 3D affine path ([a][z][y][x] and a
-                      //    y-prefilter); 0: y-axis path ([a][y][z][x])
+    int tilted;       // 1: 3D affine path (with a y-prefilter); 0: y-axis
+                      //    path
     int in_c128;      // input sinogram is complex128
     int kx_zero_lo, kx_zero_hi;  // spectrum columns in [lo, hi) are all zero
                                  // (outside the |k| < km disc)
     float bx_ca, bx_cb;  // x-prefilter boundary solve (n = nx)
     float by_ca, by_cb;  // y-prefilter boundary solve (n = ny)
-    int ypitch;          // y-axis slab [a][z][x][y]: y pitch (ny rounded up
-                         // to a multiple of 32)
+    int ypitch;          // slab [a][z][x][y]: y pitch (ny rounded up to a
+                         // multiple of 32)
     FilterTables tab;
     const float *gain;   // optional real per-frequency gain [lNy*lNx] (NULL: 1)
     const float2 *again; // optional complex per-angle gain [A][lNy*lNx], this
@@ -48,12 +48,12 @@ struct StageParams {
     int *status;
 };
 
-// y pitch of the y-axis slab layout [a][z][x][y]
+// y pitch of the slab layout [a][z][x][y]
 inline int yaxis_slab_pitch(int ny) { return (ny + 31) / 32 * 32; }
 
 struct RotParams {
     int ny, nx, nz;
-    int ypitch;       // y-axis slab pitch (yaxis_slab_pitch)
+    int ypitch;       // slab y pitch (yaxis_slab_pitch)
     int nbatch_angles;
     int first_pass;   // this launch starts the sum (overwrite)
     int last_pass;    // this launch ends the sum (drop the compensation)

@@ -545,101 +545,199 @@ __global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const f
 
 // ---------------------------------------------------------------------------
 // Tilted path: 3D affine resampling in the reference's (x, -y, z) frame.
-// Slab layout [a][z][y][x].  Output voxel (z, y, x) <- frame point
-// o = (x, ny-1-y, z); coordinate c = M o + off (scipy order); taps are read
-// back through the same mapping.
+// Output voxel (z, y, x) <- frame point o = (x, ny-1-y, z); coordinate
+// c = M o + off (scipy order); tap (t0, t1, t2) is read back through the
+// same mapping: slab[a][mirror(t2)][mirror(t0)][ny-1-mirror(t1)] in the
+// layout [a][z][x][y] (y innermost, pitch R.ypitch).
+//
+// Work split: a CTA owns 32 y (the lanes) x 8 x (the warps) x 4 z (per
+// thread) outputs.  The rotation axis is close to y, so the frame point of
+// consecutive y moves almost along the slab's y axis: the 32 lanes of a tap
+// load read one nearly contiguous 256-byte run, served by L1 for the
+// neighbouring outputs that share it.  Per angle, the FP32 coordinate
+// splits of the tile origin (three axes) and an "interior" flag (every tap
+// of every output in range: no in/out decisions, no mirroring) are computed
+// once per CTA in FP64 and kept in shared memory for a chunk of angles.
+constexpr int R3_Y = 32, R3_X = 8, R3_Z = 4;
+constexpr int R3_CHUNK = 64;
+constexpr int R3_KAHAN = 8;
+
+// c(d) = I + f + sum_j m_j d_j for small integer offsets d (three slopes,
+// split as in AxisCoord).
+struct AxisCoord3 {
+    float f, mh0, ml0, mh1, ml1, mh2, ml2;
+    int I;
+};
+
+__device__ __forceinline__ AxisCoord3 make_axis3(double c0, double m0, double m1, double m2)
+{
+    AxisCoord3 a;
+    const double I = floor(c0);
+    a.I = (int)I;
+    a.f = (float)(c0 - I);
+    const double h0 = rint(m0 * 4096.0) / 4096.0, h1 = rint(m1 * 4096.0) / 4096.0, h2 = rint(m2 * 4096.0) / 4096.0;
+    a.mh0 = (float)h0;
+    a.ml0 = (float)(m0 - h0);
+    a.mh1 = (float)h1;
+    a.ml1 = (float)(m1 - h1);
+    a.mh2 = (float)h2;
+    a.ml2 = (float)(m2 - h2);
+    return a;
+}
+
+__device__ __forceinline__ float eval_axis3(const AxisCoord3 &a, float d0, float d1, float d2, int &B)
+{
+    const float S = fmaf(a.mh2, d2, fmaf(a.mh1, d1, a.mh0 * d0));  // exact
+    const float Rr = fmaf(a.ml2, d2, fmaf(a.ml1, d1, fmaf(a.ml0, d0, a.f)));
+    const float Sf = floorf(S);
+    B = a.I + (int)Sf;
+    return (S - Sf) + Rr;
+}
+
 template <int ORDER, bool ONLYREAL>
-__global__ void __launch_bounds__(256) k_rotate_3d(RotParams R, const float2 *__restrict__ slab,
+__global__ void __launch_bounds__(256, 2) k_rotate_3d(RotParams R, const float2 *__restrict__ slab,
                                                    const double *__restrict__ geo, void *volume, float2 *comp)
 {
-    __shared__ double sg[12];
-    __shared__ AxisCoord sax[3];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 8, z = blockIdx.z;
-    const int nx = R.nx, ny = R.ny, nz = R.nz;
-    const int x = x0 + tx, y = y0 + ty;
-    const bool valid = x < nx && y < ny;
-    const int n[3] = {nx, ny, nz};
-    float2 s = make_float2(0.f, 0.f), cp = make_float2(0.f, 0.f);
-    const double o0 = (double)x, o1 = (double)(ny - 1 - y), o2 = (double)z;
-    for (int a = 0; a < R.nbatch_angles; ++a) {
-        if (threadIdx.x == 0) {
-            const double *g = geo + 12 * (size_t)a;
-            for (int k = 0; k < 12; ++k)
-                sg[k] = g[k];
-            const double b0 = (double)x0, b1 = (double)(ny - 1 - y0), b2 = (double)z;
-            for (int i = 0; i < 3; ++i) {
-                const double c = ((g[9 + i] + g[3 * i] * b0) + g[3 * i + 1] * b1) + g[3 * i + 2] * b2;
-                sax[i] = make_axis(c, g[3 * i], g[3 * i + 1]);
-            }
+    __shared__ AxisCoord3 srec[R3_CHUNK][3];
+    __shared__ int sflag[R3_CHUNK][3];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nx = R.nx, ny = R.ny, nz = R.nz, yp = R.ypitch;
+    const int x0 = blockIdx.x * R3_X, y0 = blockIdx.y * R3_Y, z0 = blockIdx.z * R3_Z;
+    const int x = x0 + w, y = y0 + lane;
+    const bool vxy = x < nx && y < ny;
+    const bool full = x0 + R3_X <= nx && y0 + R3_Y <= ny && z0 + R3_Z <= nz;
+    const int n3[3] = {nx, ny, nz};
+    const size_t aslab = (size_t)nz * nx * yp;
+    const size_t zstride = (size_t)nx * yp;
+    // frame offsets of this thread's outputs from the tile origin
+    const float d0 = (float)w, d1 = (float)(-lane);
+    const double o0 = (double)x, o1 = (double)(ny - 1 - y);
+    float2 s[R3_Z], cp[R3_Z], part[R3_Z];
+#pragma unroll
+    for (int q = 0; q < R3_Z; ++q) {
+        s[q] = make_float2(0.f, 0.f);
+        cp[q] = make_float2(0.f, 0.f);
+        part[q] = make_float2(0.f, 0.f);
+    }
+    const int nb = R.nbatch_angles;
+    for (int a0 = 0; a0 < nb; a0 += R3_CHUNK) {
+        const int na = min(R3_CHUNK, nb - a0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < na * 3; t += blockDim.x) {
+            const int aa = t / 3, i = t % 3;
+            const double *g = geo + 12 * (size_t)(a0 + aa);
+            const double m0 = g[3 * i], m1 = g[3 * i + 1], m2 = g[3 * i + 2];
+            const double c = ((g[9 + i] + m0 * (double)x0) + m1 * (double)(ny - 1 - y0)) + m2 * (double)z0;
+            srec[aa][i] = make_axis3(c, m0, m1, m2);
+            // coordinate range over the tile: o - o_origin in
+            // [0, X-1] x [-(Y-1), 0] x [0, Z-1]
+            const double e0 = m0 * (R3_X - 1), e1 = -m1 * (R3_Y - 1), e2 = m2 * (R3_Z - 1);
+            const double lo = c + fmin(e0, 0.0) + fmin(e1, 0.0) + fmin(e2, 0.0);
+            const double hi = c + fmax(e0, 0.0) + fmax(e1, 0.0) + fmax(e2, 0.0);
+            sflag[aa][i] = (full && lo >= 2.0 && hi <= n3[i] - 3.0) ? 1 : 0;
         }
         __syncthreads();
-        if (valid) {
-            const float d0 = (float)tx, d1 = (float)(-ty);
-            float l[3];
-            int Ib[3];
-            bool inside = true;
+        for (int aa = 0; aa < na; ++aa) {
+            const int a = a0 + aa;
+            const bool interior = sflag[aa][0] && sflag[aa][1] && sflag[aa][2];
+            const AxisCoord3 ax0 = srec[aa][0], ax1 = srec[aa][1], ax2 = srec[aa][2];
+            const float2 *sa = slab + (size_t)a * aslab;
+            const double *g = geo + 12 * (size_t)a;
 #pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                l[i] = eval_axis(sax[i], d0, d1, Ib[i]);
-                inside = inside && inside_axis(l[i], Ib[i], n[i], [&] {
-                    return __dadd_rn(__dadd_rn(__dadd_rn(sg[9 + i], __dmul_rn(sg[3 * i], o0)),
-                                               __dmul_rn(sg[3 * i + 1], o1)),
-                                     __dmul_rn(sg[3 * i + 2], o2));
-                });
-            }
-            if (inside) {
+            for (int q = 0; q < R3_Z; ++q) {
+                const int z = z0 + q;
+                if (!vxy || z >= nz)
+                    continue;
+                const float d2 = (float)q;
+                int Ib[3];
+                float l[3];
+                l[0] = eval_axis3(ax0, d0, d1, d2, Ib[0]);
+                l[1] = eval_axis3(ax1, d0, d1, d2, Ib[1]);
+                l[2] = eval_axis3(ax2, d0, d1, d2, Ib[2]);
+                const double o2 = (double)z;
+                auto exact = [&](int i) {
+                    return __dadd_rn(__dadd_rn(__dadd_rn(__ldg(g + 9 + i), __dmul_rn(__ldg(g + 3 * i), o0)),
+                                               __dmul_rn(__ldg(g + 3 * i + 1), o1)),
+                                     __dmul_rn(__ldg(g + 3 * i + 2), o2));
+                };
+                if (!interior) {
+                    bool in = true;
+#pragma unroll
+                    for (int i = 0; i < 3; ++i)
+                        in = in && inside_axis(l[i], Ib[i], n3[i], [&] { return exact(i); });
+                    if (!in)
+                        continue;
+                }
                 int t0[3];
-                float w[3][ORDER + 1];
+                float wt[3][ORDER + 1];
                 if (ORDER == 0) {
 #pragma unroll
                     for (int i = 0; i < 3; ++i) {
-                        const double c = __dadd_rn(__dadd_rn(__dadd_rn(sg[9 + i], __dmul_rn(sg[3 * i], o0)),
-                                                             __dmul_rn(sg[3 * i + 1], o1)),
-                                                   __dmul_rn(sg[3 * i + 2], o2));
-                        t0[i] = (int)floor(c + 0.5);
-                        w[i][0] = 1.f;
+                        t0[i] = (int)floor(exact(i) + 0.5);
+                        wt[i][0] = 1.f;
                     }
                 } else {
 #pragma unroll
                     for (int i = 0; i < 3; ++i)
-                        t0[i] = Ib[i] + Spline<ORDER>::weights(l[i], w[i]);
+                        t0[i] = Ib[i] + Spline<ORDER>::weights(l[i], wt[i]);
                 }
-                int ix[ORDER + 1], iy[ORDER + 1], iz[ORDER + 1];
+                float2 acc = part[q];
+                if (interior) {
+                    const float2 *base = sa + ((size_t)t0[2] * nx + t0[0]) * yp + (ny - 1 - t0[1]);
 #pragma unroll
-                for (int k = 0; k <= ORDER; ++k) {
-                    ix[k] = mirror_idx(t0[0] + k, nx);
-                    iy[k] = ny - 1 - mirror_idx(t0[1] + k, ny);
-                    iz[k] = mirror_idx(t0[2] + k, nz);
-                }
-                const float2 *base = slab + (size_t)a * nz * ny * nx;
-                float2 acc = make_float2(0.f, 0.f);
+                    for (int k2 = 0; k2 <= ORDER; ++k2) {
 #pragma unroll
-                for (int c2 = 0; c2 <= ORDER; ++c2) {
-                    float2 r1 = make_float2(0.f, 0.f);
+                        for (int k0 = 0; k0 <= ORDER; ++k0) {
+                            const float2 *col = base + k2 * zstride + (size_t)k0 * yp;
+                            float2 r = make_float2(0.f, 0.f);
 #pragma unroll
-                    for (int c1 = 0; c1 <= ORDER; ++c1) {
-                        const float2 *row = base + ((size_t)iz[c2] * ny + iy[c1]) * nx;
-                        float2 r0 = make_float2(0.f, 0.f);
-#pragma unroll
-                        for (int c0 = 0; c0 <= ORDER; ++c0) {
-                            const float2 b = __ldg(row + ix[c0]);
-                            r0.x = fmaf(w[0][c0], b.x, r0.x);
-                            r0.y = fmaf(w[0][c0], b.y, r0.y);
+                            for (int k1 = 0; k1 <= ORDER; ++k1)
+                                r = ffma2(make_float2(wt[1][k1], wt[1][k1]), __ldg(col - k1), r);
+                            const float w02 = wt[2][k2] * wt[0][k0];
+                            acc = ffma2(make_float2(w02, w02), r, acc);
                         }
-                        r1.x = fmaf(w[1][c1], r0.x, r1.x);
-                        r1.y = fmaf(w[1][c1], r0.y, r1.y);
                     }
-                    acc.x = fmaf(w[2][c2], r1.x, acc.x);
-                    acc.y = fmaf(w[2][c2], r1.y, acc.y);
+                } else {
+                    int ix[ORDER + 1], iy[ORDER + 1], iz[ORDER + 1];
+#pragma unroll
+                    for (int k = 0; k <= ORDER; ++k) {
+                        ix[k] = mirror_idx(t0[0] + k, nx);
+                        iy[k] = ny - 1 - mirror_idx(t0[1] + k, ny);
+                        iz[k] = mirror_idx(t0[2] + k, nz);
+                    }
+#pragma unroll
+                    for (int k2 = 0; k2 <= ORDER; ++k2) {
+#pragma unroll
+                        for (int k0 = 0; k0 <= ORDER; ++k0) {
+                            const float2 *col = sa + ((size_t)iz[k2] * nx + ix[k0]) * yp;
+                            float2 r = make_float2(0.f, 0.f);
+#pragma unroll
+                            for (int k1 = 0; k1 <= ORDER; ++k1)
+                                r = ffma2(make_float2(wt[1][k1], wt[1][k1]), __ldg(col + iy[k1]), r);
+                            const float w02 = wt[2][k2] * wt[0][k0];
+                            acc = ffma2(make_float2(w02, w02), r, acc);
+                        }
+                    }
                 }
-                kahan_add(s, cp, acc);
+                part[q] = acc;
+            }
+            if ((a % R3_KAHAN) == R3_KAHAN - 1 || a == nb - 1) {
+#pragma unroll
+                for (int q = 0; q < R3_Z; ++q) {
+                    kahan_add(s[q], cp[q], part[q]);
+                    part[q] = make_float2(0.f, 0.f);
+                }
             }
         }
-        __syncthreads();
     }
-    if (valid)
-        store_sum<ONLYREAL>(R, volume, comp, ((size_t)z * ny + y) * nx + x, s, cp);
+    if (vxy) {
+#pragma unroll
+        for (int q = 0; q < R3_Z; ++q) {
+            const int z = z0 + q;
+            if (z < nz)
+                store_sum<ONLYREAL>(R, volume, comp, ((size_t)z * ny + y) * nx + x, s[q], cp[q]);
+        }
+    }
 }
 
 template <int ORDER, bool ONLYREAL>
@@ -654,8 +752,8 @@ static cudaError_t rotate_impl(const RotParams &R, int tilted, const float2 *sla
         dim3 grid((R.nx + R2_T - 1) / R2_T, (R.nz + R2_T - 1) / R2_T, (R.ny + R2_Y - 1) / R2_Y);
         k_rotate_y<ORDER, ONLYREAL><<<grid, R2_THREADS, R2_SMEM, s>>>(R, slab, geo, tiles, volume, comp);
     } else {
-        dim3 grid((R.nx + 31) / 32, (R.ny + 7) / 8, R.nz);
-        k_rotate_3d<ORDER, ONLYREAL><<<grid, 256, 0, s>>>(R, slab, geo, volume, comp);
+        dim3 grid((R.nx + R3_X - 1) / R3_X, (R.ny + R3_Y - 1) / R3_Y, (R.nz + R3_Z - 1) / R3_Z);
+        k_rotate_3d<ORDER, ONLYREAL><<<grid, R3_X * 32, 0, s>>>(R, slab, geo, volume, comp);
     }
     return cudaGetLastError();
 }

@@ -257,11 +257,10 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
 // ---------------------------------------------------------------------------
 // (b2) rows: (+ z-boundary rows), backward FFT along x, x-prefilter boundary
 // terms, crop -> slab.
-// Tilted path: slab[a][z][y][x], one CTA line per (job, y) row.
-// y-axis path: slab[a][z][x][y] with the y pitch P.ypitch (a multiple of
-// LPC and of 16): the LPC lines of a CTA are consecutive y of one plane, the
-// cropped rows are transposed through shared memory and stored as runs of
-// LPC consecutive y per x (rows y >= ny are zero).
+// Slab layout [a][z][x][y] (both geometries) with the y pitch P.ypitch (a
+// multiple of LPC and of 16): the LPC lines of a CTA are consecutive y of
+// one plane, the cropped rows are transposed through shared memory and
+// stored as runs of LPC consecutive y per x (rows y >= ny are zero).
 template <class L, int LPC>
 __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L line, const float2 *T,
                                                                const float2 *Tab, float2 *slab, int q0, int qn)
@@ -274,8 +273,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
     const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl;
-    const bool yaxis = !P.tilted;
-    const int rows = yaxis ? P.ypitch : ny;  // rows per job in the grid
+    const int rows = P.ypitch;  // rows per job in the grid
     const long long rid = (long long)blockIdx.x * LPC + l;
     const int qrel = (int)(rid / rows);
     const int y = (int)(rid % rows);
@@ -339,19 +337,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
         }
         return o;
     };
-    if (!yaxis) {
-        if (!valid)
-            return;
-        float2 *dst = slab + (((size_t)a * nz + p) * ny + y) * nx;
-#pragma unroll
-        for (int r = 0; r < L::SLOTS; ++r) {
-            const int xx = j + r * L::TPL - padxl;
-            if (xx >= 0 && xx < nx)
-                __stcs(dst + xx, cropped(v[r], xx));  // streamed: keep L2 for the column stage output
-        }
-        return;
-    }
-    // y-axis: stage[x][l] (pitch LPC+1), then runs of LPC y per x
+    // stage[x][l] (pitch LPC+1), then runs of LPC y per x
     __syncthreads();  // every line is done with buf0
     float2 *stage = buf0;
     constexpr int SP = LPC + 1;
@@ -412,7 +398,7 @@ static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 
                                      float2 *slab, int q0, int qn, cudaStream_t s)
 {
     constexpr int LPC = Cfg<L>::LPC;
-    const long long lines = (long long)qn * (P.tilted ? P.ny : P.ypitch);
+    const long long lines = (long long)qn * P.ypitch;
     const unsigned grid = (unsigned)((lines + LPC - 1) / LPC);
     k_rows_inverse<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, Tab, slab, q0, qn);
     return cudaGetLastError();
