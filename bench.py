@@ -531,7 +531,7 @@ def run_ncu_case(rotate_case=False):
     sino, angles = sino[:k].copy(), angles[:k].copy()
     dev = torch.device("cuda", 0)
     rec = Backprop3D(tuple(sino.shape), angles, w["res"], w["nm"],
-                     lD=w["lD"], padfac=w["padfac"],
+                     lD=w["lD"], tilted_axis=w["axis"], padfac=w["padfac"],
                      intp_order=w["intp_order"],
                      save_memory=not rotate_case,
                      input_dtype="complex64", device=dev)

@@ -6,6 +6,22 @@
 
 namespace odt {
 
+// Asynchronous 16-byte global -> shared copies (cp.async, L2 only) and their
+// group bookkeeping.
+#ifdef __CUDACC__
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+#endif
+
 // Error bits recorded by kernels in the plan's device status word.
 enum : int {
     DEVCHK_BOX_OVERFLOW = 1,   // a rotation footprint did not fit its tile

@@ -303,14 +303,6 @@ __global__ void k_rotate_y_setup(RotParams R, const double *__restrict__ geo, Ti
     tiles[id] = tg;
 }
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 // Issue the footprint copy of one (angle, tile) for y values [y0, y0+16):
 // position p = (vz, vx) of the box holds 16 y at buf[p*16 .. p*16+15], read

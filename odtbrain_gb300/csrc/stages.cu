@@ -43,11 +43,11 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_forward(StageParams P, L 
     float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
-    const long long lid = (long long)blockIdx.x * LPC + l;
-    const long long nlines = (long long)nb * P.lNy;
+    const int lid = (int)blockIdx.x * LPC + l;
+    const int nlines = nb * P.lNy;
     const bool valid = lid < nlines;
-    const int a = valid ? (int)(lid / P.lNy) : 0;
-    const int y = valid ? (int)(lid % P.lNy) : 0;
+    const int a = valid ? lid / P.lNy : 0;
+    const int y = valid ? lid - a * P.lNy : 0;
     const double w = weights ? weights[a] : 1.0;
     const size_t arow = (size_t)a * P.ny * P.nx;
     float2 v[L::SLOTS];
@@ -274,9 +274,9 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
     const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl;
     const int rows = P.ypitch;  // rows per job in the grid
-    const long long rid = (long long)blockIdx.x * LPC + l;
-    const int qrel = (int)(rid / rows);
-    const int y = (int)(rid % rows);
+    const int rid = (int)blockIdx.x * LPC + l;  // < qn * ypitch
+    const int qrel = rid / rows;
+    const int y = rid - qrel * rows;
     const bool valid = qrel < qn && y < ny;
     const int qq = q0 + (qrel < qn ? qrel : qn - 1);
     const int yc = y < ny ? y : ny - 1;
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
     __syncthreads();
     if (qrel >= qn)
         return;
-    const int ybase = (int)(((long long)blockIdx.x * LPC) % rows);
+    const int ybase = ((int)blockIdx.x * LPC) % rows;
     float2 *dst = slab + ((size_t)a * nz + p) * nx * P.ypitch + ybase;
     for (int e = threadIdx.x; e < nx * LPC; e += LPC * L::TPL) {
         const int xx = e / LPC, ll = e % LPC;
