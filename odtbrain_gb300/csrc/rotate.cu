@@ -219,10 +219,11 @@ constexpr int R2_KAHAN = 8;     // angles summed plainly between Kahan steps
 constexpr int R2_BOXE = R2_BOX * R2_BOX * R2_Y;  // float2 per footprint buffer
 constexpr int R2_RING = 4;      // tile records in flight (angles a..a+3)
 // parameter record of an output: 4 words (box offset, in/out flag), then the
-// z and x weights, each duplicated into a (w, w) pair for packed FMAs
-template <int ORDER>
-constexpr int r2_words() { return 4 + 4 * (ORDER + 1); }
-constexpr size_t R2_SMEM = (size_t)2 * R2_BOXE * sizeof(float2) + (size_t)R2_T * R2_T * r2_words<3>() * sizeof(float) +
+// z and x weights, each duplicated into a (w, w) pair for packed FMAs.
+// Records are 20 words apart (80 bytes): the 16-byte stores of 8 consecutive
+// threads then hit disjoint banks.
+constexpr int R2_PW = 20;
+constexpr size_t R2_SMEM = (size_t)2 * R2_BOXE * sizeof(float2) + (size_t)R2_T * R2_T * R2_PW * sizeof(float) +
                            (size_t)R2_RING * 64;
 
 // d = a * b + c on (re, im) pairs: one packed FP32 FMA
@@ -418,14 +419,19 @@ __device__ __forceinline__ void output_params(const RotParams &R, const TileGeo 
             }
         }
     }
-    float4 *r4 = reinterpret_cast<float4 *>(rec);
-    r4[0] = make_float4(__int_as_float(off), __int_as_float(ok), 0.f, 0.f);
-    float2 *w2 = reinterpret_cast<float2 *>(rec + 4);
+    // 16-byte stores only: header, then the (w, w) pairs two per store
+    float w[2 * (ORDER + 1) + 1];
 #pragma unroll
     for (int k = 0; k <= ORDER; ++k) {
-        w2[k] = make_float2(wz[k], wz[k]);
-        w2[ORDER + 1 + k] = make_float2(wx[k], wx[k]);
+        w[k] = wz[k];
+        w[ORDER + 1 + k] = wx[k];
     }
+    w[2 * (ORDER + 1)] = 0.f;
+    float4 *r4 = reinterpret_cast<float4 *>(rec);
+    r4[0] = make_float4(__int_as_float(off), __int_as_float(ok), 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < ORDER + 1; ++k)
+        r4[1 + k] = make_float4(w[2 * k], w[2 * k], w[2 * k + 1], w[2 * k + 1]);
 }
 
 template <int ORDER, bool ONLYREAL>
@@ -436,9 +442,9 @@ __global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const f
 {
     extern __shared__ float4 r2_smem[];
     float2 *box = reinterpret_cast<float2 *>(r2_smem);       // [2][R2_BOXE]
-    constexpr int PW = r2_words<ORDER>();
+    constexpr int PW = R2_PW;
     float *prm = reinterpret_cast<float *>(box + 2 * R2_BOXE); // [256][PW]
-    TileGeo *ring = reinterpret_cast<TileGeo *>(prm + R2_T * R2_T * r2_words<3>());  // [R2_RING]
+    TileGeo *ring = reinterpret_cast<TileGeo *>(prm + R2_T * R2_T * R2_PW);  // [R2_RING]
     const int tid = threadIdx.x;
     const int hw = tid >> 4, yl = tid & 15;
     const int ntx = (R.nx + R2_T - 1) / R2_T, ntz = (R.nz + R2_T - 1) / R2_T;
@@ -542,7 +548,7 @@ __global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const f
 // same mapping: slab[a][mirror(t2)][mirror(t0)][ny-1-mirror(t1)] in the
 // layout [a][z][x][y] (y innermost, pitch R.ypitch).
 //
-// Work split: a CTA owns 32 y (the lanes) x 8 x (the warps) x 4 z (per
+// Work split: a CTA owns 32 y (the lanes) x 8 x (the warps) x 2 z (per
 // thread) outputs.  The rotation axis is close to y, so the frame point of
 // consecutive y moves almost along the slab's y axis: the 32 lanes of a tap
 // load read one nearly contiguous 256-byte run, served by L1 for the
@@ -550,7 +556,7 @@ __global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const f
 // splits of the tile origin (three axes) and an "interior" flag (every tap
 // of every output in range: no in/out decisions, no mirroring) are computed
 // once per CTA in FP64 and kept in shared memory for a chunk of angles.
-constexpr int R3_Y = 32, R3_X = 8, R3_Z = 4;
+constexpr int R3_Y = 32, R3_X = 8, R3_Z = 2;
 constexpr int R3_CHUNK = 64;
 constexpr int R3_KAHAN = 8;
 
@@ -587,7 +593,7 @@ __device__ __forceinline__ float eval_axis3(const AxisCoord3 &a, float d0, float
 }
 
 template <int ORDER, bool ONLYREAL>
-__global__ void __launch_bounds__(256, 2) k_rotate_3d(RotParams R, const float2 *__restrict__ slab,
+__global__ void __launch_bounds__(256, 3) k_rotate_3d(RotParams R, const float2 *__restrict__ slab,
                                                    const double *__restrict__ geo, void *volume, float2 *comp)
 {
     __shared__ AxisCoord3 srec[R3_CHUNK][3];
