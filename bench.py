@@ -204,18 +204,19 @@ def stage_flops(rec, A):
             "rows_inverse": planes * ny * f(lNx)}
 
 
-def profile_traffic(stage):
-    """Per-launch DRAM bytes of `stage` from the committed ncu summary, or
-    None."""
+def profile_traffic(stage, units_per_launch):
+    """DRAM bytes of one launch of `stage` from the committed ncu summary
+    (profiles/dram_traffic.md), scaled from the captured launch to a launch
+    of `units_per_launch` units; None if absent."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.md")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         for line in f:
             parts = [p.strip() for p in line.strip().strip("|").split("|")]
-            if len(parts) >= 2 and parts[0] == stage:
+            if len(parts) >= 3 and parts[0] == stage:
                 try:
-                    return float(parts[1])
+                    return float(parts[1]) / float(parts[2]) * units_per_launch
                 except ValueError:
                     return None
     return None
@@ -393,7 +394,16 @@ def run_ours(args):
     per_launch_s = ds["ms"] / ds["launches"] / 1e3
     peak, peak_kind = measured_peaks()
     achieved = per_launch_bytes / per_launch_s / 1e9
-    traffic = profile_traffic(dom)
+    # units of the captured launches: planes for the FFT stages, voxel-angle
+    # updates for the resampling
+    nz_ = n
+    units = {"columns_propagate": A * nz_ / max(1, stages["columns_propagate"]["launches"]),
+             "rows_inverse": A * nz_ / max(1, stages["rows_inverse"]["launches"]),
+             "rotate": U / max(1, stages["rotate"]["launches"]),
+             "rows_forward": None}
+    rot_key = "rotate" if w["axis"] is None else "rotate_tilted"
+    traffic = (profile_traffic(rot_key if dom == "rotate" else dom, units[dom])
+               if units.get(dom) else None)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
@@ -422,7 +432,7 @@ def run_ours(args):
     roofline_rotate = {"bound": "hbm", "kernel": "rotate",
                        "achieved": rot_achieved, "peak": peak, "unit": "GB/s",
                        "frac": rot_achieved / peak,
-                       "traffic": profile_traffic("rotate"),
+                       "traffic": profile_traffic(rot_key, units["rotate"]),
                        "algorithmic_bytes_per_launch":
                            rs["bytes"] / rs["launches"],
                        "launch_ms": rs["ms"] / rs["launches"]}
