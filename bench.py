@@ -70,6 +70,20 @@ WORKLOADS = {
                name="backpropagate_3d: A=60 x 64x64 -> 64^3, padfac 1.75 "
                     "(128^2 FFTs), intp_order 2"),
 }
+# differentiation and learned-filter configurations (single GPU; no
+# counterpart in the reference)
+WORKLOADS["c4"] = dict(
+    A=90, n=128, res=3.0, nm=1.333, seed=5, count_range=(2, 6),
+    semi_range=(6, 30), axis=None, padfac=1.75, intp_order=2, lD=0.0,
+    name="differentiation: forward + vector-Jacobian product (sinogram and "
+         "256x256 filter gain) through the autograd wrapper, A=90 x 128x128 "
+         "-> 128^3, intp_order 2")
+WORKLOADS["c5"] = dict(
+    A=40, n=128, res=3.0, nm=1.333, seed=0, axis=None, padfac=1.75,
+    intp_order=2, lD=0.0,
+    name="learned wedge filter: A=40 uniform over 120 deg, 128x128 -> 128^3, "
+         "shipped network (trained on 2000 phantoms); rel-L2 to the plain "
+         "A=400 full-circle reconstruction on held-out phantoms")
 WORKLOAD = WORKLOADS["c2"]
 WORKLOAD_NAME = WORKLOAD["name"]
 CPU_SAMPLE_ANGLES = 4
@@ -526,6 +540,195 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def _timed(fn, steps, warmup, flush, stream):
+    """Mean CUDA-event time (ms) of fn over `steps` calls after `warmup`,
+    L2 flushed before each call outside the events."""
+    import torch
+    for _ in range(max(warmup, 1)):
+        fn()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        a, b = (torch.cuda.Event(enable_timing=True),
+                torch.cuda.Event(enable_timing=True))
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    return statistics.mean(ms), ms
+
+
+def _base_line(args, w, value, ms, extra):
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": w["name"],
+                       "l2": "256 MiB flush before every timed step"}}
+    line.update(extra)
+    return line
+
+
+def run_diff(args):
+    """Forward + vector-Jacobian product of the y-axis reconstruction (the
+    differentiation configuration): one step = forward through the autograd
+    wrapper, then backward of a linear loss for the sinogram and the filter
+    gain."""
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    from odtbrain_gb300 import build as native_build
+    native_build.build()
+    from odtbrain_gb300._alg3d import Backprop3D
+    from odtbrain_gb300.autograd import backpropagate_3d_autograd
+    from sino_gen import ellipsoid_phantom_sinogram
+    w = WORKLOAD
+    sino, angles = ellipsoid_phantom_sinogram(
+        w["n"], w["A"], seed=w["seed"], count_range=w["count_range"],
+        semi_range=w["semi_range"])
+    A, n = w["A"], w["n"]
+    U = updates(A, n)
+    rec = Backprop3D(sino.shape, angles, w["res"], w["nm"],
+                     input_dtype="complex64", device=dev)
+    host = torch.from_numpy(sino.astype(np.complex64)).pin_memory()
+    dsino = host.to(dev)
+    rng = np.random.default_rng(1)
+    gain = torch.tensor(rng.uniform(0.8, 1.2, rec.gain_shape())
+                        .astype(np.float32), device=dev)
+    cot = torch.tensor((rng.normal(size=rec.volume_shape()) + 1j *
+                        rng.normal(size=rec.volume_shape()))
+                       .astype(np.complex64), device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, device=dev, dtype=torch.uint8)
+    stream = torch.cuda.current_stream(dev)
+    grads = {}
+
+    def step(src=None):
+        s = (dsino if src is None else src).clone().requires_grad_(True)
+        g = gain.clone().requires_grad_(True)
+        vol = backpropagate_3d_autograd(s, angles, w["res"], w["nm"], gain=g,
+                                        plan=rec)
+        loss = torch.vdot(cot.flatten(), vol.flatten()).real
+        loss.backward()
+        grads["s"], grads["g"] = s.grad, g.grad
+
+    def forward():
+        rec.forward_gain(dsino, gain, check=False)
+
+    if args.ncu_case:  # profiling case: two forward + VJP steps
+        for _ in range(2):
+            step()
+        torch.cuda.synchronize()
+        print("ncu case done")
+        return
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms, step_ms = _timed(step, args.steps, args.warmup, flush, stream)
+    clk = clocks.stop()
+    fwd_ms, _ = _timed(forward, args.steps, args.warmup, flush, stream)
+    torch.cuda.reset_peak_memory_stats(dev)
+    base = torch.cuda.memory_allocated(dev)
+    step()
+    torch.cuda.synchronize()
+    peak = torch.cuda.max_memory_allocated(dev)
+    # end to end: pinned host sinogram in, sinogram gradient out
+    out_host = torch.empty(sino.shape, dtype=torch.complex64).pin_memory()
+
+    def e2e():
+        step(host.to(dev, non_blocking=True))
+        out_host.copy_(grads["s"], non_blocking=True)
+    e2e_ms, _ = _timed(e2e, max(3, min(args.steps, 5)), 1, flush, stream)
+    line = _base_line(args, w, U / (ms / 1e3), ms, {
+        "step": "forward + VJP (sinogram and gain), slabs recomputed",
+        "forward_ms": fwd_ms, "backward_ms": ms - fwd_ms,
+        "peak_device_mib": (peak - base) / 2**20,
+        "peak_device_mib_incl_inputs": peak / 2**20,
+        "clocks": clk, "gpu_launches_forward": rec.launches_per_call,
+        "step_ms": step_ms,
+        "e2e": {"value": U / (e2e_ms / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": int(host.numel() * 8),
+                "d2h_bytes_per_step": int(host.numel() * 8),
+                "ms_per_step": e2e_ms},
+        "cpu_baseline": None,
+        "accuracy": {"checked_by": "tests/test_gpu_adjoint.py: central "
+                     "differences h=1e-3 over 64 directions and autograd "
+                     "through the dense FP64 model"}})
+    print(json.dumps(line), flush=True)
+
+
+def run_learned(args):
+    """Learned wedge filter: GPU time of the learned reconstruction against
+    the plain one, and the error cut of the shipped network on held-out
+    phantoms."""
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    from odtbrain_gb300 import build as native_build
+    native_build.build()
+    from odtbrain_gb300._alg3d import Backprop3D
+    from odtbrain_gb300.learned import (WEDGE_CONFIG, evaluate,
+                                        load_learned_filter, make_pairs,
+                                        wedge_angles)
+    w = WORKLOAD
+    c = dict(WEDGE_CONFIG)
+    A, n = c["num_angles"], c["n"]
+    U = updates(A, n)
+    sp = wedge_angles(A, c["span"])
+    de = np.linspace(0, 2 * np.pi, c["dense_angles"], endpoint=False)
+    rec = Backprop3D((A, n, n), sp, c["res"], c["nm"], device=dev)
+    rec_d = Backprop3D((c["dense_angles"], n, n), de, c["res"], c["nm"],
+                       device=dev)
+    n_eval = 32
+    seeds = 2_000_000 + np.arange(n_eval)  # the held-out seed range
+    sinos, targets = make_pairs(c, seeds, rec, rec_d, sp, de, dev)
+    lf = load_learned_filter(rec)
+    learned, plain = evaluate(lf, sinos, targets)
+    flush = torch.empty(L2_FLUSH_BYTES, device=dev, dtype=torch.uint8)
+    stream = torch.cuda.current_stream(dev)
+    vol = torch.empty(rec.volume_shape(), dtype=torch.complex64, device=dev)
+    s0 = sinos[0]
+    gain = lf.gains()
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms_l, step_ms = _timed(lambda: rec.forward_gain(s0, angle_gain=gain,
+                                                    out=vol, check=False),
+                           args.steps, args.warmup, flush, stream)
+    clk = clocks.stop()
+    ms_p, _ = _timed(lambda: rec(s0, out=vol, check=False), args.steps,
+                     args.warmup, flush, stream)
+
+    def with_inference():
+        lf.mlp.gains(lf.feat, *rec.gain_shape(), out=gain,
+                     positions=lf.positions)
+        rec.forward_gain(s0, angle_gain=gain, out=vol, check=False)
+    ms_i, _ = _timed(with_inference, args.steps, args.warmup, flush, stream)
+    host = sinos[0].cpu().pin_memory()
+    out_host = torch.empty(rec.volume_shape(),
+                           dtype=torch.complex64).pin_memory()
+
+    def e2e():
+        lf(host.to(dev, non_blocking=True), out=vol)
+        out_host.copy_(vol, non_blocking=True)
+    e2e_ms, _ = _timed(e2e, max(3, min(args.steps, 5)), 1, flush, stream)
+    line = _base_line(args, w, U / (ms_l / 1e3), ms_l, {
+        "step": "learned-gain reconstruction, gains cached per angle set",
+        "plain_ms": ms_p, "time_ratio_cached": ms_l / ms_p,
+        "learned_with_inference_ms": ms_i,
+        "time_ratio_with_inference": ms_i / ms_p,
+        "eval_phantoms": n_eval, "rel_l2_learned": learned,
+        "rel_l2_plain": plain, "reduction": 1.0 - learned / plain,
+        "clocks": clk, "gpu_launches": rec.launches_per_call,
+        "step_ms": step_ms,
+        "e2e": {"value": U / (e2e_ms / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": int(host.numel() * 8),
+                "d2h_bytes_per_step": int(out_host.numel() * 8),
+                "ms_per_step": e2e_ms},
+        "cpu_baseline": None})
+    print(json.dumps(line), flush=True)
+
+
 def run_ncu_case(rotate_case=False):
     """Small case for ncu captures: the workload's plane and volume sizes
     with 8 angles and the save_memory workspace, or (``rotate_case``) 16
@@ -558,7 +761,16 @@ def main():
     args = parse_args()
     WORKLOAD = WORKLOADS[args.config]
     WORKLOAD_NAME = WORKLOAD["name"]
-    if args.ncu_case or args.ncu_rotate_case:
+    if args.config in ("c4", "c5"):
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "no counterpart in the reference (it has no "
+                              "derivatives and a fixed filter)"}))
+        elif args.config == "c4":
+            run_diff(args)
+        else:
+            run_learned(args)
+    elif args.ncu_case or args.ncu_rotate_case:
         run_ncu_case(rotate_case=args.ncu_rotate_case)
     elif args.impl == "reference":
         run_reference(args)
