@@ -394,6 +394,8 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
         e = odt::configure_rotate_kernels();
     if (e == cudaSuccess && !tilted)
         e = odt::configure_adjoint_kernels(P);
+    if (e == cudaSuccess && !tilted)
+        e = odt::configure_rotate_adjoint_kernels();
     if (e != cudaSuccess) {
         cudaFree(p->d_tables);
         delete p;
@@ -633,7 +635,7 @@ odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const
         R.onlyreal = 0;
         R.status = plan->d_status;
         e = odt::launch_rotate_adjoint(R, d.intp_order, 0, (const float2 *)vol_grad, geometry + (size_t)a0 * 6, slab,
-                                       s);
+                                       ws + plan->off_rot, s);
         if (e != cudaSuccess)
             return cuda_fail(e, "rotate_adjoint launch");
         if (gain_grad || angle_gain_grad) {

@@ -97,8 +97,11 @@ cudaError_t configure_rotate_kernels();
 
 // Adjoint (adjoint.cu, rotate.cu).
 cudaError_t configure_adjoint_kernels(const StageParams &P);
+// Scratch: rotate_scratch_bytes(batch, ...) (one 64-byte record per angle and
+// 16 x 16 tile, like the forward).
 cudaError_t launch_rotate_adjoint(const RotParams &R, int order, int tilted, const float2 *vol_grad,
-                                  const double *geo, float2 *slab_grad, cudaStream_t s);
+                                  const double *geo, float2 *slab_grad, void *scratch, cudaStream_t s);
+cudaError_t configure_rotate_adjoint_kernels();
 cudaError_t launch_adj_rows(const StageParams &P, const float2 *sgrad, float2 *Tg, int q0, int qn, cudaStream_t s);
 cudaError_t launch_adj_columns(const StageParams &P, const float2 *Tg, float2 *Qg, int q0, int qn, cudaStream_t s);
 cudaError_t launch_adj_spectrum(const StageParams &P, const float2 *rowspec, const float2 *Qg, float *dgain,

@@ -20,6 +20,7 @@
 // registers; across launches (angle batches) the compensation is carried in
 // a side buffer.
 #include <float.h>
+#include <limits.h>
 #include "odt_fft.cuh"
 #include "odt_internal.cuh"
 
@@ -798,146 +799,260 @@ cudaError_t launch_rotate(const RotParams &R, int order, int tilted, const float
 }
 
 // ---------------------------------------------------------------------------
-// Transpose of the y-axis resampling (the backward pass): for every
-// coefficient (iz, ix) of plane y and every angle a of the batch,
-//   slab_grad[a][y][iz][ix] = sum_o beta(c_z(o) - tz) beta(c_x(o) - tx)
-//                                   * vol_grad[o_z][y][o_x]
-// over the outputs o whose coordinate c(o) is inside the domain and whose
-// (unmirrored) taps tz, tx mirror onto (iz, ix).  beta is the centred
-// B-spline of the order, so beta(c - t) is exactly the forward weight of tap
-// t (and zero for non-taps).  The outputs that can reach a tap lie in the
-// rotated support square around o* = R^T (t - off); they are enumerated and
-// tested.  In/out decisions use the forward's FP64 rule.
-template <int ORDER>
-__device__ __forceinline__ float bspline_weight(float u)
-{
-    const float a = fabsf(u);
-    if (ORDER == 1)
-        return a < 1.f ? 1.f - a : 0.f;
-    if (ORDER == 2) {
-        if (a < 0.5f)
-            return 0.75f - a * a;
-        if (a < 1.5f) {
-            const float b = 1.5f - a;
-            return 0.5f * b * b;
-        }
-        return 0.f;
-    }
-    if (ORDER == 3) {
-        if (a < 1.f)
-            return (2.f / 3.f) - a * a + 0.5f * a * a * a;
-        if (a < 2.f) {
-            const float b = 2.f - a;
-            return b * b * b * (1.f / 6.f);
-        }
-        return 0.f;
-    }
-    return 0.f;
-}
+// Transpose of the y-axis resampling (the backward pass):
+//   slab_grad[a][y][iz][ix] = sum over outputs o of angle a whose taps
+//       (mirrored) include (iz, ix): wz * wx * vol_grad[o_z][y][o_x]
+// with exactly the forward's in/out decisions, tap starts and weights.
+//
+// Work split (the transpose of k_rotate_y): a CTA owns a 16 x 16 tile of
+// coefficients (iz, ix) and 16 y (the lanes of a half-warp) and loops over
+// the batch's angles.  Per angle, k_rotate_y_adj_setup has found the box of
+// outputs whose coordinates come within reach of the tile's (virtual, for
+// mirrored edges) tap positions; one thread per output computes its
+// parameter record (in/out decision, tap start, weights) into shared memory,
+// then every half-warp pushes w * g of its outputs' taps that land in the
+// tile into a shared accumulator with shared-memory atomics (the 16 lanes
+// are 16 different y, so one instruction never collides with itself).  The
+// tile is written once per angle.
+constexpr int RA_T = 16, RA_Y = 16, RA_THREADS = 512;
+constexpr int RA_OBOX = 36;        // max output box per axis
+constexpr int RA_YP = RA_Y + 1;    // accumulator y pitch (conflict-free reads)
+constexpr size_t RA_SMEM = (size_t)RA_T * RA_T * RA_YP * sizeof(float2) + (size_t)RA_OBOX * RA_OBOX * 8 * sizeof(float);
 
-// Unmirrored tap positions that mirror onto index i (orders <= 3 reach one
-// position below 0 and up to two above n-1).
-template <int ORDER>
-__device__ __forceinline__ int virtual_taps(int i, int n, int *t)
+struct __align__(16) AdjTileGeo {
+    AxisCoord z, x;              // coordinates of output (oz0, ox0)
+    short oz0, ox0, ozn, oxn;    // box of candidate outputs; ozn == 0: none
+    short vz0, vz1, vx0, vx1;    // virtual tap range that can land in the tile
+};
+static_assert(sizeof(AdjTileGeo) == 64, "AdjTileGeo is one 64-byte record");
+
+// Virtual tap range [v0, v1] whose mirror images can fall in the real range
+// [t0, t1] of an axis of length n (taps reach at most two positions past
+// either edge for orders <= 3).
+__device__ __forceinline__ void virtual_range(int t0, int t1, int n, int &v0, int &v1)
 {
-    int k = 0;
-    t[k++] = i;
-    if (n >= 2) {
-        if (i == 1)
-            t[k++] = -1;
-        if (i == n - 2)
-            t[k++] = n;
-        if (ORDER == 3 && i == n - 3 && n >= 3)
-            t[k++] = n + 1;
-    }
-    return k;
+    v0 = t0;
+    v1 = t1;
+    if (t0 <= 2)
+        v0 = -2;
+    if (t1 >= n - 3)
+        v1 = n + 1;
 }
 
 template <int ORDER>
-__global__ void __launch_bounds__(256) k_rotate_y_adjoint(RotParams R, const float2 *__restrict__ vgrad,
-                                                          const double *__restrict__ geo, float2 *__restrict__ sgrad)
+__global__ void k_rotate_y_adj_setup(RotParams R, const double *__restrict__ geo, AdjTileGeo *__restrict__ tiles)
 {
-    const int ix = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int iz = blockIdx.y * 8 + (threadIdx.x >> 5);
-    const int y = blockIdx.z;
-    const int nx = R.nx, nz = R.nz, ny = R.ny;
-    if (ix >= nx || iz >= nz)
+    const int ntz = (R.nz + RA_T - 1) / RA_T, ntx = (R.nx + RA_T - 1) / RA_T;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= R.nbatch_angles * ntz * ntx)
         return;
-    int tzs[3], txs[3];
-    const int ntz = virtual_taps<ORDER>(iz, nz, tzs);
-    const int ntx = virtual_taps<ORDER>(ix, nx, txs);
-    const double supp = 0.5 * (ORDER + 1);
+    const int a = id / (ntz * ntx), t = id % (ntz * ntx);
+    const int cz0 = (t / ntx) * RA_T, cx0 = (t % ntx) * RA_T;
+    const int nz = R.nz, nx = R.nx;
+    const double *g = geo + 6 * (size_t)a;
+    const double m00 = g[0], m01 = g[1], m10 = g[2], m11 = g[3], f0 = g[4], f1 = g[5];
+    int vz0, vz1, vx0, vx1;
+    virtual_range(cz0, min(cz0 + RA_T, nz) - 1, nz, vz0, vz1);
+    virtual_range(cx0, min(cx0 + RA_T, nx) - 1, nx, vx0, vx1);
+    AdjTileGeo tg;
+    tg.vz0 = (short)vz0;
+    tg.vz1 = (short)vz1;
+    tg.vx0 = (short)vx0;
+    tg.vx1 = (short)vx1;
+    tg.oz0 = tg.ox0 = tg.ozn = tg.oxn = 0;
+    // outputs whose taps can reach the virtual range have coordinates within
+    // 2.5 of it (tap windows are at most 4 wide), and inside [0, n-1]
+    const double czl = fmax((double)vz0 - 2.5, 0.0), czh = fmin((double)vz1 + 2.5, (double)(nz - 1));
+    const double cxl = fmax((double)vx0 - 2.5, 0.0), cxh = fmin((double)vx1 + 2.5, (double)(nx - 1));
+    // o = M^T (c - f) (M is a rotation)
+    double ozl = 1e30, ozh = -1e30, oxl = 1e30, oxh = -1e30;
+    for (int k = 0; k < 4; ++k) {
+        const double cz = (k & 1) ? czh : czl, cx = (k & 2) ? cxh : cxl;
+        const double oz = m00 * (cz - f0) + m10 * (cx - f1), ox = m01 * (cz - f0) + m11 * (cx - f1);
+        ozl = fmin(ozl, oz);
+        ozh = fmax(ozh, oz);
+        oxl = fmin(oxl, ox);
+        oxh = fmax(oxh, ox);
+    }
+    const int oz0 = max(0, (int)floor(ozl) - 1), oz1 = min(nz - 1, (int)ceil(ozh) + 1);
+    const int ox0 = max(0, (int)floor(oxl) - 1), ox1 = min(nx - 1, (int)ceil(oxh) + 1);
+    if (oz0 <= oz1 && ox0 <= ox1) {
+        if (oz1 - oz0 + 1 > RA_OBOX || ox1 - ox0 + 1 > RA_OBOX) {
+            atomicOr(R.status, DEVCHK_BOX_OVERFLOW);
+        } else {
+            tg.oz0 = (short)oz0;
+            tg.ox0 = (short)ox0;
+            tg.ozn = (short)(oz1 - oz0 + 1);
+            tg.oxn = (short)(ox1 - ox0 + 1);
+        }
+    }
+    tg.z = make_axis((f0 + m00 * (double)tg.oz0) + m01 * (double)tg.ox0, m00, m01);
+    tg.x = make_axis((f1 + m10 * (double)tg.oz0) + m11 * (double)tg.ox0, m10, m11);
+    tiles[id] = tg;
+}
+
+template <int ORDER>
+__global__ void __launch_bounds__(RA_THREADS, 1) k_rotate_y_adjoint(RotParams R, const float2 *__restrict__ vgrad,
+                                                                    const double *__restrict__ geo,
+                                                                    const AdjTileGeo *__restrict__ tiles,
+                                                                    float2 *__restrict__ sgrad)
+{
+    extern __shared__ float4 ra_smem[];
+    float2 *acc = reinterpret_cast<float2 *>(ra_smem);              // [16 z][16 x][RA_YP]
+    float4 *rec = reinterpret_cast<float4 *>(acc + RA_T * RA_T * RA_YP);  // [box][2]
+    const int tid = threadIdx.x, hw = tid >> 4, yl = tid & 15;
+    const int nx = R.nx, nz = R.nz, ny = R.ny;
+    const int ntx = (nx + RA_T - 1) / RA_T, ntz = (nz + RA_T - 1) / RA_T;
+    const int tile = blockIdx.y * ntx + blockIdx.x;
+    const int cx0 = blockIdx.x * RA_T, cz0 = blockIdx.y * RA_T, y0 = blockIdx.z * RA_Y;
+    const int y = y0 + yl;
+    const bool yok = y < ny;
     for (int a = 0; a < R.nbatch_angles; ++a) {
+        const AdjTileGeo tg = tiles[(size_t)a * ntz * ntx + tile];
+        for (int i = tid; i < RA_T * RA_T * RA_YP; i += RA_THREADS)
+            acc[i] = make_float2(0.f, 0.f);
+        const int nbox = tg.ozn * tg.oxn;
         const double *g = geo + 6 * (size_t)a;
-        const double m00 = __ldg(g + 0), m01 = __ldg(g + 1), m10 = __ldg(g + 2), m11 = __ldg(g + 3);
-        const double f0 = __ldg(g + 4), f1 = __ldg(g + 5);
-        const float m00f = (float)m00, m01f = (float)m01, m10f = (float)m10, m11f = (float)m11;
-        const double rz = supp * (fabs(m00) + fabs(m01)), rx = supp * (fabs(m10) + fabs(m11));
-        float2 acc = make_float2(0.f, 0.f);
-        for (int u = 0; u < ntz; ++u) {
-            for (int v = 0; v < ntx; ++v) {
-                const double tz = (double)tzs[u], tx = (double)txs[v];
-                // o* = R^T (t - off)
-                const double dz = tz - f0, dx = tx - f1;
-                const double ozc = m00 * dz + m10 * dx, oxc = m01 * dz + m11 * dx;
-                const int oz_lo = max(0, (int)ceil(ozc - rz - 1e-9)), oz_hi = min(nz - 1, (int)floor(ozc + rz + 1e-9));
-                const int ox_lo = max(0, (int)ceil(oxc - rx - 1e-9)), ox_hi = min(nx - 1, (int)floor(oxc + rx + 1e-9));
-                for (int oz = oz_lo; oz <= oz_hi; ++oz) {
-                    for (int ox = ox_lo; ox <= ox_hi; ++ox) {
-                        float uz, ux;
-                        double cz = 0.0, cx = 0.0;
-                        bool exact = ORDER == 0;
-                        if (!exact) {
-                            // c(o) - t = R (o - o*)
-                            const float ez = (float)((double)oz - ozc), ex = (float)((double)ox - oxc);
-                            uz = fmaf(m01f, ex, m00f * ez);
-                            ux = fmaf(m11f, ex, m10f * ez);
-                            const float cze = (float)tz + uz, cxe = (float)tx + ux;
-                            exact = cze < kGuard || cze > (float)(nz - 1) - kGuard || cxe < kGuard ||
-                                    cxe > (float)(nx - 1) - kGuard;
-                        }
-                        if (exact) {
-                            cz = __dadd_rn(__dadd_rn(f0, __dmul_rn(m00, (double)oz)), __dmul_rn(m01, (double)ox));
-                            cx = __dadd_rn(__dadd_rn(f1, __dmul_rn(m10, (double)oz)), __dmul_rn(m11, (double)ox));
-                            if (cz < 0.0 || cz > (double)(nz - 1) || cx < 0.0 || cx > (double)(nx - 1))
-                                continue;
-                            if (ORDER == 0) {
-                                if (floor(cz + 0.5) != tz || floor(cx + 0.5) != tx)
-                                    continue;
-                                uz = ux = 0.f;
-                            } else {
-                                uz = (float)(cz - tz);
-                                ux = (float)(cx - tx);
-                            }
-                        }
-                        const float w = ORDER == 0 ? 1.f : bspline_weight<ORDER>(uz) * bspline_weight<ORDER>(ux);
-                        if (w == 0.f)
-                            continue;
-                        const float2 gv = __ldg(vgrad + ((size_t)oz * ny + y) * nx + ox);
-                        acc.x = fmaf(w, gv.x, acc.x);
-                        acc.y = fmaf(w, gv.y, acc.y);
-                    }
+        // parameter records: (tz0, tx0, wz0, wz1) (wz2, wx0, wx1, wx2), or
+        // tz0 = INT_MIN when the output is outside or cannot reach the tile
+        for (int o = tid; o < nbox; o += RA_THREADS) {
+            const int dz = o / tg.oxn, dx = o - dz * tg.oxn;
+            const int oz = tg.oz0 + dz, ox = tg.ox0 + dx;
+            int Iz, Ix;
+            const float lz = eval_axis(tg.z, (float)dz, (float)dx, Iz);
+            const float lx = eval_axis(tg.x, (float)dz, (float)dx, Ix);
+            bool in = inside_axis(lz, Iz, nz, [&] {
+                return __dadd_rn(__dadd_rn(__ldg(g + 4), __dmul_rn(__ldg(g + 0), (double)oz)),
+                                 __dmul_rn(__ldg(g + 1), (double)ox));
+            });
+            in = in && inside_axis(lx, Ix, nx, [&] {
+                return __dadd_rn(__dadd_rn(__ldg(g + 5), __dmul_rn(__ldg(g + 2), (double)oz)),
+                                 __dmul_rn(__ldg(g + 3), (double)ox));
+            });
+            int tz0 = INT_MIN, tx0 = 0;
+            float wz[4] = {0.f, 0.f, 0.f, 0.f}, wx[4] = {0.f, 0.f, 0.f, 0.f};
+            if (in) {
+                int sz, sx;
+                if (ORDER == 0) {
+                    const double cz = __dadd_rn(__dadd_rn(__ldg(g + 4), __dmul_rn(__ldg(g + 0), (double)oz)),
+                                                __dmul_rn(__ldg(g + 1), (double)ox));
+                    const double cx = __dadd_rn(__dadd_rn(__ldg(g + 5), __dmul_rn(__ldg(g + 2), (double)oz)),
+                                                __dmul_rn(__ldg(g + 3), (double)ox));
+                    sz = (int)floor(cz + 0.5);
+                    sx = (int)floor(cx + 0.5);
+                    wz[0] = 1.f;
+                    wx[0] = 1.f;
+                } else {
+                    float w[ORDER + 1];
+                    sz = Iz + Spline<ORDER>::weights(lz, w);
+#pragma unroll
+                    for (int k = 0; k <= ORDER; ++k)
+                        wz[k] = w[k];
+                    sx = Ix + Spline<ORDER>::weights(lx, w);
+#pragma unroll
+                    for (int k = 0; k <= ORDER; ++k)
+                        wx[k] = w[k];
+                }
+                if (sz + ORDER >= tg.vz0 && sz <= tg.vz1 && sx + ORDER >= tg.vx0 && sx <= tg.vx1) {
+                    tz0 = sz;
+                    tx0 = sx;
+                }
+            }
+            rec[2 * o] = make_float4(__int_as_float(tz0), __int_as_float(tx0), wz[0], wz[1]);
+            rec[2 * o + 1] = make_float4(wz[2], wx[0], wx[1], wx[2]);
+            if (ORDER == 3) {
+                // order 3 needs wz[3], wx[3]: the box holds at most
+                // RA_OBOX^2 records of 8 words; keep the fourth weights in
+                // the high half of the record array
+                float2 *w4 = reinterpret_cast<float2 *>(rec + 2 * RA_OBOX * RA_OBOX);
+                w4[o] = make_float2(wz[3], wx[3]);
+            }
+        }
+        __syncthreads();
+        // push: half-warp hw takes outputs hw, hw + 32, ...
+        for (int o = hw; o < nbox; o += RA_THREADS / 16) {
+            const float4 r0 = rec[2 * o];
+            const int tz0 = __float_as_int(r0.x);
+            if (tz0 == INT_MIN)
+                continue;
+            const float4 r1 = rec[2 * o + 1];
+            const int tx0 = __float_as_int(r0.y);
+            float wz[4] = {r0.z, r0.w, r1.x, 0.f}, wx[4] = {r1.y, r1.z, r1.w, 0.f};
+            if (ORDER == 3) {
+                const float2 w4 = reinterpret_cast<const float2 *>(rec + 2 * RA_OBOX * RA_OBOX)[o];
+                wz[3] = w4.x;
+                wx[3] = w4.y;
+            }
+            const int dz = o / tg.oxn, dx = o - dz * tg.oxn;
+            const int oz = tg.oz0 + dz, ox = tg.ox0 + dx;
+            const float2 gv = yok ? __ldg(vgrad + ((size_t)oz * ny + y) * nx + ox) : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i <= ORDER; ++i) {
+                const int zz = mirror_idx(tz0 + i, nz) - cz0;
+                if (zz < 0 || zz >= RA_T)
+                    continue;
+#pragma unroll
+                for (int k = 0; k <= ORDER; ++k) {
+                    const int xx = mirror_idx(tx0 + k, nx) - cx0;
+                    if (xx < 0 || xx >= RA_T)
+                        continue;
+                    const float w = wz[i] * wx[k];
+                    float2 *dst = acc + (zz * RA_T + xx) * RA_YP + yl;
+                    atomicAdd(&dst->x, w * gv.x);
+                    atomicAdd(&dst->y, w * gv.y);
                 }
             }
         }
-        sgrad[(((size_t)a * ny + y) * nz + iz) * nx + ix] = acc;
+        __syncthreads();
+        // write the tile: slab_grad[a][y][z][x], runs of 16 x
+        for (int e = tid; e < RA_T * RA_T * RA_Y; e += RA_THREADS) {
+            const int xx = e & 15, zz = (e >> 4) & 15, yy = e >> 8;
+            const int z = cz0 + zz, x = cx0 + xx, yv = y0 + yy;
+            if (z < nz && x < nx && yv < ny)
+                sgrad[(((size_t)a * ny + yv) * nz + z) * nx + x] = acc[(zz * RA_T + xx) * RA_YP + yy];
+        }
+        __syncthreads();
     }
 }
 
 cudaError_t launch_rotate_adjoint(const RotParams &R, int order, int tilted, const float2 *vol_grad,
-                                  const double *geo, float2 *slab_grad, cudaStream_t s)
+                                  const double *geo, float2 *slab_grad, void *scratch, cudaStream_t s)
 {
     if (tilted)
         return cudaErrorNotSupported;
-    dim3 grid((R.nx + 31) / 32, (R.nz + 7) / 8, R.ny);
+    const int ntiles = ((R.nx + RA_T - 1) / RA_T) * ((R.nz + RA_T - 1) / RA_T);
+    const int nset = R.nbatch_angles * ntiles;
+    AdjTileGeo *tiles = reinterpret_cast<AdjTileGeo *>(scratch);
+    dim3 grid((R.nx + RA_T - 1) / RA_T, (R.nz + RA_T - 1) / RA_T, (R.ny + RA_Y - 1) / RA_Y);
+    const size_t smem = RA_SMEM + (size_t)RA_OBOX * RA_OBOX * sizeof(float2);
     switch (order) {
-    case 0: k_rotate_y_adjoint<0><<<grid, 256, 0, s>>>(R, vol_grad, geo, slab_grad); break;
-    case 1: k_rotate_y_adjoint<1><<<grid, 256, 0, s>>>(R, vol_grad, geo, slab_grad); break;
-    case 2: k_rotate_y_adjoint<2><<<grid, 256, 0, s>>>(R, vol_grad, geo, slab_grad); break;
-    case 3: k_rotate_y_adjoint<3><<<grid, 256, 0, s>>>(R, vol_grad, geo, slab_grad); break;
-    default: return cudaErrorInvalidValue;
+#define ODT_ADJ_CASE(O)                                                                                      \
+    case O:                                                                                                  \
+        k_rotate_y_adj_setup<O><<<(nset + 127) / 128, 128, 0, s>>>(R, geo, tiles);                          \
+        k_rotate_y_adjoint<O><<<grid, RA_THREADS, smem, s>>>(R, vol_grad, geo, tiles, slab_grad);           \
+        break;
+        ODT_ADJ_CASE(0)
+        ODT_ADJ_CASE(1)
+        ODT_ADJ_CASE(2)
+        ODT_ADJ_CASE(3)
+#undef ODT_ADJ_CASE
+    default:
+        return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+cudaError_t configure_rotate_adjoint_kernels()
+{
+    const size_t smem = RA_SMEM + (size_t)RA_OBOX * RA_OBOX * sizeof(float2);
+    const void *fns[] = {(const void *)k_rotate_y_adjoint<0>, (const void *)k_rotate_y_adjoint<1>,
+                         (const void *)k_rotate_y_adjoint<2>, (const void *)k_rotate_y_adjoint<3>};
+    for (const void *f : fns) {
+        const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace odt
