@@ -89,6 +89,7 @@ struct odt_bpp3d_plan {
     size_t off_Qg, off_W, off_Pg, adj_ws_bytes;  // adjoint-only regions after ws_bytes
     double bx_ca, bx_cb, by_ca, by_cb;
     int kx_zero_lo, kx_zero_hi;  // all-zero spectrum columns [lo, hi)
+    int col_slots;               // resident column-stage CTAs (occupancy x SMs)
     // device tables (one allocation)
     void *d_tables;
     FilterTables tab;
@@ -121,6 +122,7 @@ StageParams stage_params(const odt_bpp3d_plan *p)
     P.by_ca = (float)p->by_ca;
     P.by_cb = (float)p->by_cb;
     P.ypitch = odt::yaxis_slab_pitch(d.ny);
+    P.col_slots = p->col_slots;
     P.tab = p->tab;
     P.gain = nullptr;
     P.again = nullptr;
@@ -388,8 +390,13 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
         p->adj_ws_bytes = w;
     }
 
+    p->col_slots = 0;
     StageParams P = stage_params(p);
     e = odt::configure_kernels(P);
+    if (e == cudaSuccess) {
+        p->col_slots = odt::columns_slots(P);
+        P.col_slots = p->col_slots;
+    }
     if (e == cudaSuccess && !tilted)
         e = odt::configure_rotate_kernels();
     if (e == cudaSuccess && !tilted)

@@ -57,6 +57,7 @@ struct StageParams {
     float by_ca, by_cb;  // y-prefilter boundary solve (n = ny)
     int ypitch;          // slab [a][z][x][y]: y pitch (ny rounded up to a
                          // multiple of 32)
+    int col_slots;       // resident CTAs of the column stage on the device
     FilterTables tab;
     const float *gain;   // optional real per-frequency gain [lNy*lNx] (NULL: 1)
     const float2 *again; // optional complex per-angle gain [A][lNy*lNx], this
@@ -93,6 +94,8 @@ size_t rotate_scratch_bytes(int nbatch_angles, int ny, int nx, int nz, int tilte
 cudaError_t launch_rotate(const RotParams &R, int order, int tilted, const float2 *slab, const double *geo,
                           void *volume, float2 *comp, void *scratch, cudaStream_t s);
 cudaError_t configure_kernels(const StageParams &P);
+// Resident CTAs (all SMs) of the column-stage kernel for these sizes.
+int columns_slots(const StageParams &P);
 cudaError_t configure_rotate_kernels();
 
 // Adjoint (adjoint.cu, rotate.cu).

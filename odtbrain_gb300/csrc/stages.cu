@@ -22,6 +22,7 @@
 // prefiltered axis (folded into the filter table G), z gets per-frequency
 // boundary terms (alpha, beta tables), and x (and y) get per-line boundary
 // terms computed from four samples just outside the crop.
+#include <algorithm>
 #include <type_traits>
 
 #include "odt_fft.cuh"
@@ -359,7 +360,22 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
 }
 
 // ---------------------------------------------------------------------------
-constexpr int kPlanesPerColumnBlock = 16;
+// Planes per column-stage CTA: enough CTAs for one full wave of the
+// resident slots over the active column groups (the forward column FFT of a
+// CTA is amortised over its planes, so fewer, longer CTAs are better as long
+// as every slot is busy), within [4, 32].
+template <int KX>
+static int planes_per_cta(const StageParams &P, int qn)
+{
+    const int groups = (P.lNx + KX - 1) / KX;
+    int active = 0;
+    for (int g = 0; g < groups; ++g)
+        if (!(g * KX >= P.kx_zero_lo && g * KX + KX <= P.kx_zero_hi))
+            ++active;
+    const int per = P.col_slots > 0 ? std::max(1, P.col_slots / std::max(1, active)) : 4;
+    const int ppc = (qn + per - 1) / per;
+    return std::min(32, std::max(4, ppc));
+}
 
 template <class L>
 static cudaError_t rows_forward_impl(const StageParams &P, L line, const void *sino, const double *w, int nb,
@@ -387,9 +403,10 @@ static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rows
                                 cudaStream_t s)
 {
     constexpr int KX = Cfg<L>::KX;
-    dim3 grid((P.lNx + KX - 1) / KX, (qn + kPlanesPerColumnBlock - 1) / kPlanesPerColumnBlock);
+    const int ppc = planes_per_cta<KX>(P, qn);
+    dim3 grid((P.lNx + KX - 1) / KX, (qn + ppc - 1) / ppc);
     k_columns_propagate<L, KX><<<grid, KX * L::TPL, smem_cols<L>(line.n), s>>>(P, line, rowspec, T, q0, qn,
-                                                                             kPlanesPerColumnBlock);
+                                                                             ppc);
     return cudaGetLastError();
 }
 
@@ -427,6 +444,21 @@ static cudaError_t set_smem_attrs(int n)
         return e;
     return cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_cols<L>(n));
+}
+
+int columns_slots(const StageParams &P)
+{
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    const cudaError_t e = with_line(P.lNy, [&](auto line) {
+        using L = decltype(line);
+        constexpr int KX = Cfg<L>::KX;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_columns_propagate<L, KX>, KX * L::TPL,
+                                                             smem_cols<L>(line.n));
+    });
+    return e == cudaSuccess ? per * sms : 0;
 }
 
 bool line_size_supported(int n)
