@@ -80,6 +80,11 @@ typedef struct odt_bpp3d_desc {
     const double *kz_phase;
     uint64_t workspace_limit;    /* bytes of scratch the plan may use; 0 =
                                     library default                         */
+    /* Position of plane p along the propagation axis: z_p = p - nz/2 +
+     * z_shift.  0 for the 3D functions (_alg3d_bpp.py:419-437); 0.5 for the
+     * 2D algorithm run as ny = 1 (rows yv = k - ln/2 + 0.5,
+     * _alg2d_bpp.py:295-300). */
+    double z_shift;
 } odt_bpp3d_desc;
 
 typedef struct odt_bpp3d_plan odt_bpp3d_plan;
@@ -248,6 +253,23 @@ odt_status odt_mlp_gain_backward(const odt_mlp_params *params,
                                  int32_t num_positions,
                                  const void *gain_grad, void *store,
                                  const odt_mlp_grads *grads, void *stream);
+
+/* ---- Object function -> refractive index --------------------------------
+ * Elementwise, stream-ordered, `n` elements of `dtype` at device `f` into
+ * device `ri` (same type; may alias).  FP32 for F32/C64, FP64 for F64/C128.
+ *   odt_odt_to_ri: ri = nm * sqrt(f / km^2 + 1), km = 2 pi nm / res;
+ *     principal root with non-negative real part for complex data, NaN
+ *     where f / km^2 + 1 < 0 for real data.  Replaces odtbrain.odt_to_ri
+ *     (odtbrain/_translate_ri.py:5-57).
+ *   odt_opt_to_ri: ri = nm + f / (2 pi) * res.  Replaces odtbrain.opt_to_ri
+ *     (odtbrain/_translate_ri.py:60-93). */
+enum odt_data_type {
+    ODT_DATA_F32 = 0, ODT_DATA_F64 = 1, ODT_DATA_C64 = 2, ODT_DATA_C128 = 3
+};
+odt_status odt_odt_to_ri(const void *f, void *ri, int64_t n, int32_t dtype,
+                         double res, double nm, void *stream);
+odt_status odt_opt_to_ri(const void *f, void *ri, int64_t n, int32_t dtype,
+                         double res, double nm, void *stream);
 
 /* Wait for `stream`, then return ODT_ERR_DEVICE_CHECK if any kernel of this
  * plan recorded a failed internal check since the last call (the status word

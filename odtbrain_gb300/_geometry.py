@@ -214,3 +214,49 @@ def tilted_geometry(angles, tilted_axis, weight_angles, shape_xyz):
         geo[i, :9] = dinv.reshape(-1)
         geo[i, 9:] = c - np.dot(dinv, c)
     return weights, geo, tilted_axis
+
+
+# ------------------------------------------------------------------ 2D path
+def padding_geometry_2d(ln, padding):
+    """Padded line length and left pad of the 2D algorithm
+    (odtbrain/_alg2d_bpp.py:175-187): the next power of two of 2.1*ln, at
+    least 64; left pad ceil(pad/2)."""
+    order = max(64., 2 ** np.ceil(np.log(ln * 2.1) / np.log(2)))
+    pad = order - ln if padding else 0
+    padl = int(np.ceil(pad / 2))
+    return dict(lN=int(ln + pad), padl=padl, padr=int(pad - padl))
+
+
+def filter_tables_2d(A, lN, res, nm, lD):
+    """(filter, kz_phase) of the 2D algorithm as (1, lN) FP64 arrays
+    (odtbrain/_alg2d_bpp.py:245-269): the prefactor divided by lN (the
+    reference's inverse FFT is normalised) and km*(M-1)."""
+    km = (2 * np.pi * nm) / res
+    kx = (2 * np.pi * np.fft.fftfreq(lN)).reshape(1, -1)
+    dphi0 = 2 * np.pi / A
+    klp = (kx ** 2 < km ** 2)
+    M = 1. / km * np.sqrt((km ** 2 - kx ** 2) * klp)
+    pre = -1j * km / (2 * np.pi)
+    pre *= dphi0
+    pre *= np.abs(kx) * klp
+    pre *= np.exp(-1j * km * (M - 1) * lD)
+    filt = np.ascontiguousarray(pre / lN, dtype=np.complex128)
+    phase = np.ascontiguousarray(km * (M - 1), dtype=np.float64)
+    return filt, phase
+
+
+def rotation_2d_geometry(angles, ln):
+    """Per angle the [m00, m01, m10, m11, off0, off1] that
+    ``scipy.ndimage.rotate(image, -angle*180/pi, reshape=False)`` builds
+    for an (ln, ln) image (odtbrain/_alg2d_bpp.py:312-321); the angle in
+    degrees is formed in the reference's operation order."""
+    angles = np.asarray(angles).reshape(-1)
+    out = np.empty((angles.size, 6), dtype=np.float64)
+    center = (np.asarray((ln, ln)) - 1) / 2
+    for i in range(angles.size):
+        deg = -angles[i] * 180 / np.pi
+        c, s = special.cosdg(deg), special.sindg(deg)
+        mat = np.array([[c, s], [-s, c]])
+        out[i, :4] = mat.reshape(-1)
+        out[i, 4:] = center - mat @ center
+    return out

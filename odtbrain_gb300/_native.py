@@ -20,6 +20,7 @@ ODT_ERR_DEVICE_CHECK = 5
 ODT_PAD_NONE, ODT_PAD_EDGE, ODT_PAD_RAMP = 0, 1, 2
 ODT_GEOM_Y_AXIS, ODT_GEOM_AFFINE3D = 0, 1
 ODT_INPUT_C64, ODT_INPUT_C128 = 0, 1
+ODT_DATA_F32, ODT_DATA_F64, ODT_DATA_C64, ODT_DATA_C128 = 0, 1, 2, 3
 # size of the static scratch of odt_bpp3d_execute_noalloc
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -40,6 +41,8 @@ EXPORTED_SYMBOLS = (
     "odt_mlp_gain_forward",
     "odt_mlp_store_size",
     "odt_mlp_gain_backward",
+    "odt_odt_to_ri",
+    "odt_opt_to_ri",
     "odt_status_string",
     "odt_last_error",
 )
@@ -72,6 +75,7 @@ class Bpp3dDesc(ctypes.Structure):
         ("filter", ctypes.POINTER(ctypes.c_double)),
         ("kz_phase", ctypes.POINTER(ctypes.c_double)),
         ("workspace_limit", ctypes.c_uint64),
+        ("z_shift", ctypes.c_double),
     ]
 
 
@@ -149,6 +153,10 @@ def lib():
         L.odt_bpp3d_adjoint.argtypes = [vp] * 12
         L.odt_bpp3d_read_status.argtypes = [vp, vp]
         L.odt_bpp3d_plan_destroy.argtypes = [vp]
+        for name in ("odt_odt_to_ri", "odt_opt_to_ri"):
+            getattr(L, name).argtypes = [vp, vp, ctypes.c_int64,
+                                         ctypes.c_int32, ctypes.c_double,
+                                         ctypes.c_double, vp]
         i32 = ctypes.c_int32
         L.odt_mlp_gain_forward.argtypes = [ctypes.POINTER(MlpParams), i32,
                                            i32, i32, vp, vp, i32, vp, vp]
@@ -164,7 +172,8 @@ def lib():
                      "odt_bpp3d_adjoint_workspace_size", "odt_bpp3d_adjoint",
                      "odt_bpp3d_read_status", "odt_bpp3d_plan_destroy",
                      "odt_mlp_gain_forward", "odt_mlp_store_size",
-                     "odt_mlp_gain_backward"):
+                     "odt_mlp_gain_backward", "odt_odt_to_ri",
+                     "odt_opt_to_ri"):
             getattr(L, name).restype = ctypes.c_int
         L.odt_status_string.argtypes = [ctypes.c_int]
         L.odt_status_string.restype = ctypes.c_char_p

@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_columns(StageParams P, L li
         if (a != cur_a) {
             if (cur_a >= 0)
                 flush(cur_a);
-            const float zp = (float)p - 0.5f * (float)nz;
+            const float zp = (float)p - 0.5f * (float)nz + P.zshift;
 #pragma unroll
             for (int r = 0; r < L::SLOTS; ++r) {
                 const int ky = j + r * L::TPL;

@@ -123,6 +123,7 @@ StageParams stage_params(const odt_bpp3d_plan *p)
     P.by_cb = (float)p->by_cb;
     P.ypitch = odt::yaxis_slab_pitch(d.ny);
     P.col_slots = p->col_slots;
+    P.zshift = (float)d.z_shift;
     P.tab = p->tab;
     P.gain = nullptr;
     P.again = nullptr;
@@ -151,6 +152,8 @@ odt_status validate(const odt_bpp3d_desc *d)
         return fail(ODT_ERR_INVALID_ARGUMENT, "intp_order must be in 0..5");
     if (d->intp_order > 3)
         return fail(ODT_ERR_UNSUPPORTED, "spline orders 4 and 5 are not implemented on the GPU");
+    if (!std::isfinite(d->z_shift) || std::fabs(d->z_shift) > 1.0 || 2.0 * d->z_shift != std::rint(2.0 * d->z_shift))
+        return fail(ODT_ERR_INVALID_ARGUMENT, "z_shift must be 0, +-0.5 or +-1");
     if (d->geometry == ODT_GEOM_AFFINE3D && d->intp_order >= 2 && d->ny < 2)
         return fail(ODT_ERR_UNSUPPORTED, "3D spline prefilter needs ny >= 2");
     if (!odt::line_size_supported(d->pad_nx) || !odt::line_size_supported(d->pad_ny))
@@ -218,7 +221,9 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
             zz *= z1;
         }
     }
-    const double z_first = 0.0 - 0.5 * nz, z_last = (double)(nz - 1) - 0.5 * nz;
+    // positions of the first and last planes (the z-prefilter boundary terms
+    // are per-frequency functions of them)
+    const double z_first = 0.0 - 0.5 * nz + d.z_shift, z_last = (double)(nz - 1) - 0.5 * nz + d.z_shift;
     for (int ky = 0; ky < lNy; ++ky) {
         const double iby = (pf && tilted) ? 1.0 / spline_bhat(order, fftfreq_rad(ky, lNy)) : 1.0;
         for (int kx = 0; kx < lNx; ++kx) {
@@ -396,6 +401,7 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     if (e == cudaSuccess) {
         p->col_slots = odt::columns_slots(P);
         P.col_slots = p->col_slots;
+    P.zshift = (float)d.z_shift;
     }
     if (e == cudaSuccess && !tilted)
         e = odt::configure_rotate_kernels();

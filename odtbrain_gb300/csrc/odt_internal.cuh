@@ -58,6 +58,7 @@ struct StageParams {
     int ypitch;          // slab [a][z][x][y]: y pitch (ny rounded up to a
                          // multiple of 32)
     int col_slots;       // resident CTAs of the column stage on the device
+    float zshift;        // plane p sits at z = p - nz/2 + zshift
     FilterTables tab;
     const float *gain;   // optional real per-frequency gain [lNy*lNx] (NULL: 1)
     const float2 *again; // optional complex per-angle gain [A][lNy*lNx], this

@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
         }
         if (a != cur_a) {
             column_spectrum<L, KX>(P, line, rowspec, a, kx, colok, c, j, buf0, buf1, tw, flip, V);
-            const float zp = (float)p - 0.5f * (float)nz;
+            const float zp = (float)p - 0.5f * (float)nz + P.zshift;
 #pragma unroll
             for (int r = 0; r < L::SLOTS; ++r) {
                 const int ky = j + r * L::TPL;

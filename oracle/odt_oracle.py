@@ -457,3 +457,65 @@ def backpropagate_3d_tilted(uSin, angles, res, nm, lD=0,
         return np.ascontiguousarray(out_re)
     return np.ascontiguousarray(out_re + 1j *
                                 acc_im.transpose(2, 1, 0)[:, ::-1, :])
+
+
+# ------------------------------------------------------------------ 2D path
+def backpropagate_2d(uSin, angles, res, nm, lD=0, weight_angles=True,
+                     onlyreal=False, padding=True, padval=0):
+    """FP64 restatement of ``odtbrain.backpropagate_2d``
+    (odtbrain/_alg2d_bpp.py:134-326): weight, pad along x (2.1x rule,
+    linear ramp to ``padval`` or edge values), FFT, filter, per-row
+    propagator exp(i km (M-1) yv) with yv = k - ln/2 + 0.5 and normalised
+    inverse FFT, crop to (ln, ln), rotate by -phi with scipy.ndimage's
+    cubic spline, sum."""
+    import scipy.ndimage
+    uSin = np.asarray(uSin)
+    angles = np.asarray(angles).reshape(-1)
+    A, ln = uSin.shape
+    sino = uSin * compute_angle_weights_1d(angles)[:, None] if weight_angles \
+        else np.array(uSin, dtype=complex)
+    lN = int(max(64., 2 ** np.ceil(np.log(ln * 2.1) / np.log(2)))) \
+        if padding else ln
+    pad = lN - ln
+    padl = int(np.ceil(pad / 2))
+    widths = ((0, 0), (padl, pad - padl))
+    if padval is None:
+        sino = np.pad(sino, widths, mode="edge")
+    else:
+        sino = np.pad(sino, widths, mode="linear_ramp", end_values=(padval,))
+    km = (2 * np.pi * nm) / res
+    kx = 2 * np.pi * np.fft.fftfreq(lN)
+    inside = kx ** 2 < km ** 2
+    M = np.sqrt((km ** 2 - kx ** 2) * inside) / km
+    pref = (-1j * km / (2 * np.pi)) * (2 * np.pi / A) * np.abs(kx) * inside
+    pref = pref * np.exp(-1j * km * (M - 1) * lD)
+    spec = scipy.fft.fft(sino, axis=-1) * pref                 # (A, lN)
+    yv = np.arange(ln) - ln / 2.0 + 0.5
+    prop = np.exp(1j * yv[:, None] * km * (M - 1)[None, :])    # (ln, lN)
+    out = np.zeros((ln, ln), dtype=float if onlyreal else complex)
+    for i in range(A):
+        img = scipy.fft.ifft(spec[i][None, :] * prop, axis=-1)[:, padl:padl + ln]
+        deg = -angles[i] * 180 / np.pi
+        out += scipy.ndimage.rotate(img.real, deg, reshape=False,
+                                    mode="constant", cval=0)
+        if not onlyreal:
+            out += 1j * scipy.ndimage.rotate(img.imag, deg, reshape=False,
+                                             mode="constant", cval=0)
+    return out
+
+
+def odt_to_ri(f, res, nm):
+    """FP64 restatement of ``odtbrain.odt_to_ri``
+    (odtbrain/_translate_ri.py:5-57): nm * sqrt(f / km^2 + 1), principal
+    root, real part made non-negative."""
+    km = (2 * np.pi * nm) / res
+    ri = nm * np.sqrt(np.asarray(f, dtype=complex) / km ** 2 + 1)
+    neg = ri.real < 0
+    ri[neg] *= -1
+    return ri
+
+
+def opt_to_ri(f, res, nm):
+    """FP64 restatement of ``odtbrain.opt_to_ri``
+    (odtbrain/_translate_ri.py:60-93): nm + f * res / (2 pi)."""
+    return nm + np.asarray(f) / (2 * np.pi) * res

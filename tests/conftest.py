@@ -38,12 +38,15 @@ def cuda_ready():
     return torch.device("cuda", 0)
 
 
-def reference_cases(golden):
+def reference_cases(golden, two_d=False):
+    """(name, sino, angles, kwargs, out) of the reference-made 3D cases, or
+    of the 2D cases (names b2d_*) with ``two_d``."""
     cases = golden["reference_cases"]
-    names = sorted({k.split("__")[0] for k in cases})
+    names = sorted({k.split("__")[0] for k in cases
+                    if k.startswith("b2d_") == two_d})
     for n in names:
         kw = json.loads(str(cases[n + "__kw"]))
-        if "padding" in kw:
+        if "padding" in kw and not two_d:
             kw["padding"] = tuple(kw["padding"])
         yield n, cases[n + "__sino"], cases[n + "__angles"], kw, \
             cases[n + "__out"]

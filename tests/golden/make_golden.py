@@ -7,11 +7,14 @@ $ODT_REFERENCE_ROOT):
     python tests/golden/make_golden.py
 
 Writes
-  reference_zips.npz   the reference's own golden vectors for the 3D path
+  reference_zips.npz   the reference's own golden vectors
                        (tests/data/alg3d_bpp__test_3d_backprop_phase.zip,
-                       ..._nopadreal.zip, ..._mprotate.zip), parsed
+                       ..._nopadreal.zip, ..._mprotate.zip,
+                       alg2d_bpp__test_2d_backprop_{phase,full}.zip,
+                       processing__test_{odt,opt}_to_ri.zip), parsed
   reference_cases.npz  inputs and FP64 outputs of backpropagate_3d /
-                       backpropagate_3d_tilted for small cases, produced by
+                       backpropagate_3d_tilted / backpropagate_2d for small
+                       cases, produced by
                        the reference itself (through the import shims of
                        refshim.py: scipy.fft for FFTW, NumPy for numexpr)
   reference_geometry.npz  FP64 host geometry of the reference (angle weights,
@@ -34,7 +37,7 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(HERE))
 
 import refshim  # noqa: E402
-from sino_gen import gauss_sino_3d, gauss_sino_3d_tilted, parameter_sets  # noqa: E402,E501
+from sino_gen import gauss_sino_2d, gauss_sino_3d, gauss_sino_3d_tilted, parameter_sets  # noqa: E402,E501
 
 
 def _read_zip(path):
@@ -52,6 +55,12 @@ def main():
                  "test_3d_mprotate"):
         zips[name] = _read_zip(os.path.join(data,
                                             "alg3d_bpp__%s.zip" % name))
+    for name in ("test_2d_backprop_phase", "test_2d_backprop_full"):
+        zips[name] = _read_zip(os.path.join(data,
+                                            "alg2d_bpp__%s.zip" % name))
+    for name in ("test_odt_to_ri", "test_opt_to_ri"):
+        zips[name] = _read_zip(os.path.join(data,
+                                            "processing__%s.zip" % name))
     np.savez_compressed(os.path.join(HERE, "reference_zips.npz"), **zips)
 
     cases = {}
@@ -100,6 +109,21 @@ def main():
     add("bppt_points3", odt.backpropagate_3d_tilted, st, pts,
         tilted_axis=[0, np.cos(0.4), np.sin(0.4)], weight_angles=False,
         dtype=float, **p1)
+    # 2D path
+    s2d, a2d = gauss_sino_2d()
+    s2f, _ = gauss_sino_2d(ampl_range=(0.9, 1.1))
+    add("b2d_p1", odt.backpropagate_2d, s2d, a2d, **p1)
+    add("b2d_full_p2", odt.backpropagate_2d, s2f, a2d, **p2)
+    add("b2d_edge_real", odt.backpropagate_2d, s2f, a2d, padval=None,
+        onlyreal=True, **p1)
+    rng = np.random.default_rng(11)
+    a_rand = np.sort(rng.uniform(0, 2 * np.pi, 13))
+    s_odd, _ = gauss_sino_2d(A=13, N=31, max_phase=3.0,
+                             ampl_range=(0.8, 1.2))
+    add("b2d_odd_nopad", odt.backpropagate_2d, s_odd, a_rand,
+        padding=False, **p2)
+    add("b2d_odd_noweight", odt.backpropagate_2d, s_odd, a_rand,
+        weight_angles=False, padval=1.5, **p1)
     np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **cases)
 
     geo = {}

@@ -1,8 +1,8 @@
 """Test inputs for the parity tests.
 
-* ``gauss_sino_3d`` / ``gauss_sino_3d_tilted`` / ``parameter_sets`` /
-  ``cutout`` restate the reference's test helpers
-  (tests/common_methods.py:63-118, 121-184, 231-243, 187-205) so the GPU
+* ``gauss_sino_2d`` / ``gauss_sino_3d`` / ``gauss_sino_3d_tilted`` /
+  ``parameter_sets`` / ``cutout`` restate the reference's test helpers
+  (tests/common_methods.py:10-60, 63-118, 121-184, 231-243, 187-205) so the GPU
   tests can rebuild the exact inputs of the reference's own tests and of the
   fixtures without the reference tree.  ``cutout`` keeps the reference's
   quirk (its z mask reuses the y axis, common_methods.py:200) because the
@@ -45,6 +45,29 @@ def _gauss_frames(A, Nx, Ny, max_phase, ampl_range):
         yield ii, angles, phase, ampl
 
 
+def gauss_sino_2d(A=9, N=22, max_phase=5.0, ampl_range=(1.0, 1.0)):
+    """2D variant: an off-centre Gaussian phase line per angle, amplitude 1
+    or a normalised double ring (tests/common_methods.py:10-60)."""
+    out = np.zeros((A, N), dtype=np.complex128)
+    angles = np.linspace(0, 2 * np.pi, A, endpoint=False)
+    x = np.linspace(-N / 2, N / 2, N, endpoint=True)
+    dev = np.sqrt(N / 2)
+    off = N / 7
+    for ii in range(A):
+        x0 = np.cos(angles[ii]) * off
+        phase = _normalize(np.exp(-(x - x0) ** 2 / dev ** 2), vmax=max_phase)
+        if ampl_range[0] == ampl_range[1]:
+            ampl = ampl_range[0]
+        else:
+            adev = dev / 5
+            aoff = off * .3
+            ring = (np.exp(-(x - x0 - aoff) ** 2 / adev ** 2)
+                    + np.exp(-(x - x0 + aoff) ** 2 / adev ** 2))
+            ampl = _normalize(ring, vmin=ampl_range[0], vmax=ampl_range[1])
+        out[ii] = ampl * np.exp(1j * phase)
+    return out, angles
+
+
 def gauss_sino_3d(A=9, Nx=22, Ny=22, max_phase=5.0, ampl_range=(1.0, 1.0)):
     """Off-centre Gaussian phase rotating about y; returns (sino, angles)."""
     out = np.zeros((A, Ny, Nx), dtype=np.complex128)
@@ -84,10 +107,16 @@ def parameter_sets(n=1):
 
 
 def cutout(a):
-    """Zero everything outside the reference test's mask (see module doc)."""
+    """Zero everything outside the reference test's mask (see module doc);
+    2D arrays get the disc mask."""
     a = np.array(a, copy=True)
     n = a.shape[0]
     c = n / 2
+    if a.ndim == 2:
+        x = np.arange(n).reshape(-1, 1)
+        y = x.reshape(1, -1)
+        a *= ((x - c) ** 2 + (y - c) ** 2) < c ** 2
+        return a
     x = np.arange(n).reshape(-1, 1, 1)
     y = x.reshape(1, -1, 1)
     mask = ((x - c) ** 2 + (y - c) ** 2 + (y - c) ** 2) < c ** 2
