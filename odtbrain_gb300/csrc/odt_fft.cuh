@@ -115,6 +115,13 @@ __device__ __forceinline__ void dft8(float2 *x)
 
 constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
+// Barrier over `nthreads` threads (a multiple of 32, whole warps) on named
+// barrier `id` (1..15; 0 is __syncthreads'), with shared-memory ordering.
+__device__ __forceinline__ void line_sync(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // Exchange-buffer slot of line position p.  The Stockham passes read
 // positions j + r*TPL and write positions 8*j' + r (first pass) or
 // blocks + 8*r (later passes).
@@ -153,9 +160,12 @@ struct Pow2Line {
     // element stride.  `flip` alternates the buffers across exchanges.
     // PAD selects the exchange layout (xslot): false for rows, true for
     // interleaved columns.
+    // bar > 0: the line's TPL threads are consecutive warps and sync on
+    // named barrier `bar` (only they share the line's buffers); 0: the whole
+    // CTA syncs.
     template <int DIR, bool PAD = false>
     __device__ __forceinline__ void run(float2 (&v)[8], int j, float2 *line0, float2 *line1, int es,
-                                        const float2 *tw, int &flip) const
+                                        const float2 *tw, int &flip, int bar = 0) const
     {
         int Ns = 1;
 #pragma unroll
@@ -176,7 +186,10 @@ struct Pow2Line {
 #pragma unroll
             for (int r = 0; r < 8; ++r)
                 b[xslot<PAD>(idxD + r * Ns) * es] = v[r];
-            __syncthreads();
+            if (bar > 0)
+                line_sync(bar, TPL);
+            else
+                __syncthreads();
 #pragma unroll
             for (int r = 0; r < 8; ++r)
                 v[r] = b[xslot<PAD>(j + r * TPL) * es];
@@ -218,7 +231,7 @@ struct GenericLine {
 
     template <int DIR, bool PAD = false>
     __device__ __forceinline__ void run(float2 (&v)[16], int j, float2 *line0, float2 *line1, int es,
-                                        const float2 *tw, int &flip) const
+                                        const float2 *tw, int &flip, int bar = 0) const
     {
         float2 *b = flip ? line1 : line0;
         flip ^= 1;

@@ -259,13 +259,24 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
 // (b2) rows: (+ z-boundary rows), backward FFT along x, x-prefilter boundary
 // terms, crop -> slab.
 // Slab layout [a][z][x][y] (both geometries) with the y pitch P.ypitch (a
-// multiple of LPC and of 16): the LPC lines of a CTA are consecutive y of
-// one plane, the cropped rows are transposed through shared memory and
-// stored as runs of LPC consecutive y per x (rows y >= ny are zero).
-template <class L, int LPC>
-__global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L line, const float2 *T,
-                                                               const float2 *Tab, float2 *slab, int q0, int qn)
+// multiple of 32).  A CTA owns RG consecutive y rows of one plane (job) and
+// transforms them in groups of LPC lines (one line per TPL threads); the T
+// values of the next group are loaded (evict-first) into registers while
+// the current group is transformed.  When a line is whole warps its FFT
+// exchanges sync only its own warps (named barrier).  The cropped rows of a
+// group are transposed through shared memory and stored as runs of LPC
+// consecutive y per x (rows y >= ny are zero).
+template <int LPC>
+constexpr int rows_per_cta()
 {
+    return LPC >= 8 ? LPC : 8;
+}
+
+template <class L, int LPC>
+__global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
+    k_rows_inverse(StageParams P, L line, const float2 *T, const float2 *Tab, float2 *slab, int q0, int qn)
+{
+    constexpr int RG = rows_per_cta<LPC>(), G = RG / LPC;
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNx
     const int ls = xslots<false>(n);
@@ -273,89 +284,103 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_rows_inverse(StageParams P, L 
     float2 *edge = tw + n;  // [LPC][4]
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
-    const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl;
-    const int rows = P.ypitch;  // rows per job in the grid
-    const int rid = (int)blockIdx.x * LPC + l;  // < qn * ypitch
-    const int qrel = rid / rows;
-    const int y = rid - qrel * rows;
-    const bool valid = qrel < qn && y < ny;
-    const int qq = q0 + (qrel < qn ? qrel : qn - 1);
-    const int yc = y < ny ? y : ny - 1;
-    const int a = qq / nz, p = qq % nz;
+    // lines of whole warps sync on named barrier 1 + l
+    const int bar = (L::TPL % 32 == 0 && LPC < 15) ? 1 + l : 0;
+    const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl, yp = P.ypitch;
+    const int cpj = yp / RG;  // CTAs per job
+    const int qrel = (int)blockIdx.x / cpj;
+    const int ybase = ((int)blockIdx.x - qrel * cpj) * RG;
+    const int qq = q0 + qrel;  // the grid covers exactly qn jobs
+    const int a = qq / nz, p = qq - a * nz;
     const bool pf = P.order >= 2;
     const float zl = (pf && p < ZPOW_N) ? P.tab.zpow[p] : 0.f;
     const float zh = (pf && nz - 1 - p < ZPOW_N) ? P.tab.zpow[nz - 1 - p] : 0.f;
-    const float2 *src = T + ((size_t)(qq - q0) * ny + yc) * n;
-    const float2 *ta = Tab + ((size_t)(a * 2 + 0) * ny + yc) * n;
-    const float2 *tb = Tab + ((size_t)(a * 2 + 1) * ny + yc) * n;
-    float2 v[L::SLOTS];
+    const float2 *Tq = T + (size_t)qrel * ny * n;
+    float2 *dst = slab + ((size_t)a * nz + p) * nx * yp + ybase;
+    // this thread's T values of row y (zeros for y >= ny or zero columns)
+    auto load_row = [&](int y, float2 (&v)[L::SLOTS]) {
+        const bool valid = y < ny;
+        const float2 *src = Tq + (size_t)(valid ? y : 0) * n;
 #pragma unroll
-    for (int r = 0; r < L::SLOTS; ++r) {
-        const int x = j + r * L::TPL;
-        float2 t = make_float2(0.f, 0.f);
-        if (valid && column_active(P, x)) {
-            t = __ldcs(src + x);  // read once: evict first
-            if (zl != 0.f) {
-                const float2 u = ta[x];
-                t = make_float2(fmaf(zl, u.x, t.x), fmaf(zl, u.y, t.y));
-            }
-            if (zh != 0.f) {
-                const float2 u = tb[x];
-                t = make_float2(fmaf(zh, u.x, t.x), fmaf(zh, u.y, t.y));
-            }
+        for (int r = 0; r < L::SLOTS; ++r) {
+            const int x = j + r * L::TPL;
+            v[r] = (valid && column_active(P, x)) ? __ldcs(src + x) : make_float2(0.f, 0.f);
         }
-        v[r] = t;
-    }
-    __syncthreads();
-    int flip = 0;
-    line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip);
-    float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
-    if (pf) {
-        const int e0 = (padxl - 1 + n) % n, e1 = (padxl + 1) % n;
-        const int e2 = (padxl + nx - 2 + n) % n, e3 = (padxl + nx) % n;
-        float2 t;
-        if (held<L>(v, j, e0, t)) edge[l * 4 + 0] = t;
-        if (held<L>(v, j, e1, t)) edge[l * 4 + 1] = t;
-        if (held<L>(v, j, e2, t)) edge[l * 4 + 2] = t;
-        if (held<L>(v, j, e3, t)) edge[l * 4 + 3] = t;
-        __syncthreads();
-        const float2 d0 = edge[l * 4 + 0] - edge[l * 4 + 1];
-        const float2 d1 = edge[l * 4 + 3] - edge[l * 4 + 2];
-        Acoef = make_float2(P.bx_ca * d0.x + P.bx_cb * d1.x, P.bx_ca * d0.y + P.bx_cb * d1.y);
-        Bcoef = make_float2(P.bx_ca * d1.x + P.bx_cb * d0.x, P.bx_ca * d1.y + P.bx_cb * d0.y);
-    }
-    // boundary-corrected value o of cropped sample xx of this line
-    auto cropped = [&](float2 o, int xx) {
-        if (pf) {
-            if (xx < ZPOW_N) {
-                const float zz = P.tab.zpow[xx];
-                o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
-            }
-            if (nx - 1 - xx < ZPOW_N) {
-                const float zz = P.tab.zpow[nx - 1 - xx];
-                o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
-            }
-        }
-        return o;
     };
-    // stage[x][l] (pitch LPC+1), then runs of LPC y per x
-    __syncthreads();  // every line is done with buf0
-    float2 *stage = buf0;
-    constexpr int SP = LPC + 1;
+    float2 v[L::SLOTS], vn[L::SLOTS];
+    load_row(ybase + l, v);
+    __syncthreads();  // twiddles
+#pragma unroll 1
+    for (int g = 0; g < G; ++g) {
+        const int y = ybase + g * LPC + l;
+        const bool valid = y < ny;
+        if (g + 1 < G)
+            load_row(y + LPC, vn);
+        if (valid && (zl != 0.f || zh != 0.f)) {
+            const float2 *ta = Tab + ((size_t)(a * 2 + 0) * ny + y) * n;
+            const float2 *tb = Tab + ((size_t)(a * 2 + 1) * ny + y) * n;
 #pragma unroll
-    for (int r = 0; r < L::SLOTS; ++r) {
-        const int xx = j + r * L::TPL - padxl;
-        if (xx >= 0 && xx < nx)
-            stage[xx * SP + l] = valid ? cropped(v[r], xx) : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    if (qrel >= qn)
-        return;
-    const int ybase = ((int)blockIdx.x * LPC) % rows;
-    float2 *dst = slab + ((size_t)a * nz + p) * nx * P.ypitch + ybase;
-    for (int e = threadIdx.x; e < nx * LPC; e += LPC * L::TPL) {
-        const int xx = e / LPC, ll = e % LPC;
-        __stcs(dst + (size_t)xx * P.ypitch + ll, stage[xx * SP + ll]);
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int x = j + r * L::TPL;
+                if (column_active(P, x)) {
+                    const float2 u = ta[x], w = tb[x];
+                    v[r] = make_float2(fmaf(zh, w.x, fmaf(zl, u.x, v[r].x)), fmaf(zh, w.y, fmaf(zl, u.y, v[r].y)));
+                }
+            }
+        }
+        int flip = 0;
+        line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
+        float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
+        if (pf) {
+            const int e0 = (padxl - 1 + n) % n, e1 = (padxl + 1) % n;
+            const int e2 = (padxl + nx - 2 + n) % n, e3 = (padxl + nx) % n;
+            float2 t;
+            if (held<L>(v, j, e0, t)) edge[l * 4 + 0] = t;
+            if (held<L>(v, j, e1, t)) edge[l * 4 + 1] = t;
+            if (held<L>(v, j, e2, t)) edge[l * 4 + 2] = t;
+            if (held<L>(v, j, e3, t)) edge[l * 4 + 3] = t;
+            if (bar > 0)
+                line_sync(bar, L::TPL);
+            else
+                __syncthreads();
+            const float2 d0 = edge[l * 4 + 0] - edge[l * 4 + 1];
+            const float2 d1 = edge[l * 4 + 3] - edge[l * 4 + 2];
+            Acoef = make_float2(P.bx_ca * d0.x + P.bx_cb * d1.x, P.bx_ca * d0.y + P.bx_cb * d1.y);
+            Bcoef = make_float2(P.bx_ca * d1.x + P.bx_cb * d0.x, P.bx_ca * d1.y + P.bx_cb * d0.y);
+        }
+        // stage[x][l] (pitch LPC+1) in buf0, then runs of LPC y per x
+        __syncthreads();  // every line is done with buf0
+        float2 *stage = buf0;
+        constexpr int SP = LPC + 1;
+#pragma unroll
+        for (int r = 0; r < L::SLOTS; ++r) {
+            const int xx = j + r * L::TPL - padxl;
+            if (xx >= 0 && xx < nx) {
+                float2 o = v[r];
+                if (pf) {
+                    if (xx < ZPOW_N) {
+                        const float zz = P.tab.zpow[xx];
+                        o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
+                    }
+                    if (nx - 1 - xx < ZPOW_N) {
+                        const float zz = P.tab.zpow[nx - 1 - xx];
+                        o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
+                    }
+                }
+                stage[xx * SP + l] = valid ? o : make_float2(0.f, 0.f);
+            }
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < nx * LPC; e += LPC * L::TPL) {
+            const int xx = e / LPC, ll = e - xx * LPC;
+            __stcs(dst + (size_t)xx * yp + g * LPC + ll, stage[xx * SP + ll]);
+        }
+        if (g + 1 < G) {
+            __syncthreads();  // stage reads done before buf0 is reused
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r)
+                v[r] = vn[r];
+        }
     }
 }
 
@@ -415,8 +440,7 @@ static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 
                                      float2 *slab, int q0, int qn, cudaStream_t s)
 {
     constexpr int LPC = Cfg<L>::LPC;
-    const long long lines = (long long)qn * P.ypitch;
-    const unsigned grid = (unsigned)((lines + LPC - 1) / LPC);
+    const unsigned grid = (unsigned)((long long)qn * (P.ypitch / rows_per_cta<LPC>()));
     k_rows_inverse<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, Tab, slab, q0, qn);
     return cudaGetLastError();
 }
