@@ -84,6 +84,14 @@ WORKLOADS["c5"] = dict(
     name="learned wedge filter: A=40 uniform over 120 deg, 128x128 -> 128^3, "
          "shipped network (trained on 2000 phantoms); rel-L2 to the plain "
          "A=400 full-circle reconstruction on held-out phantoms")
+# sinogram preparation of the headline sinogram (the step before the
+# reconstruction; the reference's sinogram_as_rytov)
+WORKLOADS["rytov"] = dict(
+    A=200, n=256, res=3.0, nm=1.333, seed=2024, count_range=(3, 12),
+    semi_range=(8, 60), axis=None,
+    name="sinogram_as_rytov: A=200 x 256x256 complex64 field exp(a + i*phi) "
+         "of the ellipsoid phantom -> Rytov sinogram, reliability-sorted 2D "
+         "unwrap per frame + align_unwrapped")
 WORKLOAD = WORKLOADS["c2"]
 WORKLOAD_NAME = WORKLOAD["name"]
 CPU_SAMPLE_ANGLES = 4
@@ -729,6 +737,96 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+def run_rytov(args):
+    """sinogram_as_rytov on the headline sinogram's field: one step = one
+    conversion of all 200 frames (phase, log-amplitude, per-frame unwrap,
+    alignment, composition)."""
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    from odtbrain_gb300 import build as native_build
+    native_build.build()
+    from odtbrain_gb300._prepare_sino import SinogramPrep
+    from sino_gen import ellipsoid_phantom_sinogram
+    w = WORKLOAD
+    ryt, _angles = ellipsoid_phantom_sinogram(
+        w["n"], w["A"], seed=w["seed"], count_range=w["count_range"],
+        semi_range=w["semi_range"], res=w["res"], nm=w["nm"])
+    field = np.exp(ryt).astype(np.complex64)
+    samples = field.size
+    metric = "sinogram_as_rytov samples/s on 1 GB300 (3D frames, FP32)"
+    unit = "sinogram samples/s"
+    prep = SinogramPrep(field.shape, "rytov", align=True, single=True,
+                        device=dev)
+    host = torch.from_numpy(field).pin_memory()
+    dfield = host.to(dev)
+    out = torch.empty(field.shape, dtype=torch.complex64, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, device=dev, dtype=torch.uint8)
+    stream = torch.cuda.current_stream(dev)
+    if args.ncu_case:
+        for _ in range(2):
+            prep(dfield, out=out)
+        torch.cuda.synchronize()
+        print("ncu case done")
+        return
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms, step_ms = _timed(lambda: prep(dfield, out=out, check=False),
+                         args.steps, args.warmup, flush, stream)
+    clk = clocks.stop()
+    prep(dfield, out=out, check=True)
+    out_host = torch.empty(field.shape, dtype=torch.complex64).pin_memory()
+
+    def e2e():
+        prep(host.to(dev, non_blocking=True), out=out, check=False)
+        out_host.copy_(out, non_blocking=True)
+    e2e_ms, _ = _timed(e2e, max(3, min(args.steps, 5)), 1, flush, stream)
+    # parity on a bounded sample: two frames against the oracle (FP64
+    # restatement of the reference, same anchor rule)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import unwrap_oracle
+        k = 2
+        t0 = time.perf_counter()
+        ref = unwrap_oracle.sinogram_as_rytov(field[:k].astype(np.complex128),
+                                              align=False,
+                                              anchor="first_edge")
+        cpu_s = time.perf_counter() - t0
+        sub = SinogramPrep((k,) + field.shape[1:], "rytov", align=False,
+                           single=True, device=dev)(dfield[:k].contiguous())
+        err = float(np.abs(sub.cpu().numpy() - ref).max())
+        cpu = {"value": k * field[0].size / cpu_s, "unit": unit, "cores": 1,
+               "kind": "port",
+               "sample": "%d of %d frames (oracle, FP64, align off)"
+                         % (k, field.shape[0]),
+               "max_abs_diff_vs_gpu": err}
+    algo = samples * 16  # complex64 field in, complex64 Rytov sinogram out
+    peak, peak_kind = measured_peaks()
+    achieved = algo / (ms / 1e3) / 1e9
+    line = {"metric": metric, "value": samples / (ms / 1e3), "unit": unit,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32 (reliabilities fp64)",
+            "data": "synthetic",
+            "config": {"workload": w["name"],
+                       "l2": "256 MiB flush before every timed step"},
+            "roofline": {"bound": "hbm", "achieved": achieved,
+                         "peak": peak, "peak_kind": peak_kind,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None,
+                         "note": "whole conversion against 16 B/sample "
+                                 "(field in, sinogram out); the spanning-"
+                                 "tree rounds re-read their state"},
+            "clocks": clk, "gpu_launches": prep.launches_per_call,
+            "step_ms": step_ms,
+            "e2e": {"value": samples / (e2e_ms / 1e3), "unit": unit,
+                    "h2d_bytes_per_step": int(field.nbytes),
+                    "d2h_bytes_per_step": int(field.nbytes),
+                    "ms_per_step": e2e_ms},
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
 def run_ncu_case(rotate_case=False):
     """Small case for ncu captures: the workload's plane and volume sizes
     with 8 angles and the save_memory workspace, or (``rotate_case``) 16
@@ -761,7 +859,15 @@ def main():
     args = parse_args()
     WORKLOAD = WORKLOADS[args.config]
     WORKLOAD_NAME = WORKLOAD["name"]
-    if args.config in ("c4", "c5"):
+    if args.config == "rytov":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference's 3D sinogram_as_rytov calls "
+                              "skimage.restoration.unwrap_phase; "
+                              "scikit-image is not installed"}))
+        else:
+            run_rytov(args)
+    elif args.config in ("c4", "c5"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":
                               "no counterpart in the reference (it has no "

@@ -271,6 +271,53 @@ odt_status odt_odt_to_ri(const void *f, void *ri, int64_t n, int32_t dtype,
 odt_status odt_opt_to_ri(const void *f, void *ri, int64_t n, int32_t dtype,
                          double res, double nm, void *stream);
 
+/* ---- Sinogram preparation ------------------------------------------------
+ * Replaces odtbrain.sinogram_as_rytov (odtbrain/_prepare_sino.py:105-182)
+ * and odtbrain.sinogram_as_radon (odtbrain/_prepare_sino.py:60-102),
+ * including align_unwrapped (odtbrain/_prepare_sino.py:7-46).
+ * The sinogram is (A, nx) (ny = 0, numpy.unwrap along each line) or
+ * (A, ny, nx) (ny > 0, reliability-sorted 2D unwrapping of every frame, the
+ * algorithm of skimage.restoration.unwrap_phase that the reference calls).
+ * The arithmetic type follows dtype: FP32 for complex64, FP64 for
+ * complex128.  Output (device): RYTOV complex of dtype,
+ * u0 * (log|u/u0| + 1j * unwrapped angle(u/u0)); RADON real (float32 /
+ * float64), the unwrapped angle(u).  u0 (RYTOV only): the scalar
+ * (u0_re, u0_im) when u0 == NULL, else a device array of dtype and the
+ * sinogram's shape.  seed: seed of the pseudo-random border reliabilities
+ * of the 3D unwrapping (the reference passes 47).
+ * ODT_SINO_ALIGN: align_unwrapped alone; the input is a real unwrapped
+ * phase sinogram (dtype ODT_DATA_F32 / F64, align = 1), the output its
+ * aligned copy (may alias the input).
+ * ODT_SINO_UNWRAP: the unwrapping alone (then alignment if `align`); the
+ * input is a real wrapped phase (F32 / F64) of lines (ny = 0) or frames,
+ * the output the unwrapped phase (may alias the input); for frames the
+ * counterpart of skimage.restoration.unwrap_phase on each 2D frame.
+ * Stream-ordered; the workspace (odt_sino_workspace_size bytes, 256-byte
+ * aligned) also holds the status word that odt_sino_read_status reads. */
+enum odt_sino_kind {
+    ODT_SINO_RYTOV = 0, ODT_SINO_RADON = 1, ODT_SINO_ALIGN = 2, ODT_SINO_UNWRAP = 3
+};
+typedef struct odt_sino_desc {
+    int64_t num_angles; /* A >= 1                                          */
+    int32_t ny;         /* frame rows (3D sinogram), 0 for a 2D sinogram   */
+    int32_t nx;         /* detector columns >= 1                           */
+    int32_t dtype;      /* ODT_DATA_C64 or ODT_DATA_C128                   */
+    int32_t kind;       /* odt_sino_kind                                   */
+    int32_t align;      /* apply align_unwrapped                           */
+    uint32_t seed;
+    const void *u0;
+    double u0_re, u0_im;
+} odt_sino_desc;
+odt_status odt_sino_workspace_size(const odt_sino_desc *desc, size_t *bytes);
+odt_status odt_sino_prepare(const odt_sino_desc *desc, const void *sino,
+                            void *out, void *workspace,
+                            size_t workspace_bytes, void *stream);
+/* Kernel launches one odt_sino_prepare call makes. */
+odt_status odt_sino_launch_count(const odt_sino_desc *desc, int32_t *count);
+/* Wait for `stream`; ODT_ERR_DEVICE_CHECK if a bounded loop of the unwrap
+ * gave up or a frame did not join into one tree. */
+odt_status odt_sino_read_status(const void *workspace, void *stream);
+
 /* Wait for `stream`, then return ODT_ERR_DEVICE_CHECK if any kernel of this
  * plan recorded a failed internal check since the last call (the status word
  * is cleared). */

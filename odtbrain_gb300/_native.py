@@ -21,6 +21,7 @@ ODT_PAD_NONE, ODT_PAD_EDGE, ODT_PAD_RAMP = 0, 1, 2
 ODT_GEOM_Y_AXIS, ODT_GEOM_AFFINE3D = 0, 1
 ODT_INPUT_C64, ODT_INPUT_C128 = 0, 1
 ODT_DATA_F32, ODT_DATA_F64, ODT_DATA_C64, ODT_DATA_C128 = 0, 1, 2, 3
+ODT_SINO_RYTOV, ODT_SINO_RADON, ODT_SINO_ALIGN, ODT_SINO_UNWRAP = 0, 1, 2, 3
 # size of the static scratch of odt_bpp3d_execute_noalloc
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -43,6 +44,10 @@ EXPORTED_SYMBOLS = (
     "odt_mlp_gain_backward",
     "odt_odt_to_ri",
     "odt_opt_to_ri",
+    "odt_sino_workspace_size",
+    "odt_sino_prepare",
+    "odt_sino_launch_count",
+    "odt_sino_read_status",
     "odt_status_string",
     "odt_last_error",
 )
@@ -95,6 +100,22 @@ class MlpGrads(ctypes.Structure):
 
 STAGE_NAMES = ("rows_forward", "columns_propagate", "rows_inverse",
                "rotate")
+
+
+class SinoDesc(ctypes.Structure):
+    """odt_sino_desc of include/odtbrain_gb300.h."""
+    _fields_ = [
+        ("num_angles", ctypes.c_int64),
+        ("ny", ctypes.c_int32),
+        ("nx", ctypes.c_int32),
+        ("dtype", ctypes.c_int32),
+        ("kind", ctypes.c_int32),
+        ("align", ctypes.c_int32),
+        ("seed", ctypes.c_uint32),
+        ("u0", ctypes.c_void_p),
+        ("u0_re", ctypes.c_double),
+        ("u0_im", ctypes.c_double),
+    ]
 
 
 class StageTiming(ctypes.Structure):
@@ -157,6 +178,13 @@ def lib():
             getattr(L, name).argtypes = [vp, vp, ctypes.c_int64,
                                          ctypes.c_int32, ctypes.c_double,
                                          ctypes.c_double, vp]
+        sd = ctypes.POINTER(SinoDesc)
+        L.odt_sino_workspace_size.argtypes = [
+            sd, ctypes.POINTER(ctypes.c_uint64)]
+        L.odt_sino_prepare.argtypes = [sd, vp, vp, vp, ctypes.c_uint64, vp]
+        L.odt_sino_launch_count.argtypes = [sd,
+                                            ctypes.POINTER(ctypes.c_int32)]
+        L.odt_sino_read_status.argtypes = [vp, vp]
         i32 = ctypes.c_int32
         L.odt_mlp_gain_forward.argtypes = [ctypes.POINTER(MlpParams), i32,
                                            i32, i32, vp, vp, i32, vp, vp]
@@ -173,7 +201,9 @@ def lib():
                      "odt_bpp3d_read_status", "odt_bpp3d_plan_destroy",
                      "odt_mlp_gain_forward", "odt_mlp_store_size",
                      "odt_mlp_gain_backward", "odt_odt_to_ri",
-                     "odt_opt_to_ri"):
+                     "odt_opt_to_ri", "odt_sino_workspace_size",
+                     "odt_sino_prepare", "odt_sino_launch_count",
+                     "odt_sino_read_status"):
             getattr(L, name).restype = ctypes.c_int
         L.odt_status_string.argtypes = [ctypes.c_int]
         L.odt_status_string.restype = ctypes.c_char_p

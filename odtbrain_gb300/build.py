@@ -17,7 +17,8 @@ LIBDIR = os.path.join(HERE, "_lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIBNAME = "libodtbrain_gb300.so"
 LIB = os.path.join(LIBDIR, LIBNAME)
-SOURCES = ["capi.cu", "stages.cu", "rotate.cu", "adjoint.cu", "mlp.cu", "translate.cu"]
+SOURCES = ["capi.cu", "stages.cu", "rotate.cu", "adjoint.cu", "mlp.cu", "translate.cu",
+           "unwrap.cu"]
 HEADERS = ["odt_fft.cuh", "odt_internal.cuh", "odt_stage_util.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

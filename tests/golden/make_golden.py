@@ -20,6 +20,12 @@ Writes
   reference_geometry.npz  FP64 host geometry of the reference (angle weights,
                        sphere points, rotation matrices, offsets) for
                        bit-exact comparison
+  reference_sino.npz   sinogram preparation: the reference's golden
+                       vectors (processing__test_sino_{rytov,radon}.zip,
+                       apple__test_correct_reproduce.zip) and outputs of its
+                       sinogram_as_rytov / sinogram_as_radon
+
+Parts can be chosen on the command line (backprop, sino); default all.
 The input sinogram generator below restates the reference's test helper
 (tests/common_methods.py:63-184) so that the GPU tests can regenerate the
 same inputs without the reference tree.
@@ -35,6 +41,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(HERE))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 import refshim  # noqa: E402
 from sino_gen import gauss_sino_2d, gauss_sino_3d, gauss_sino_3d_tilted, parameter_sets  # noqa: E402,E501
@@ -45,8 +52,16 @@ def _read_zip(path):
         return np.loadtxt(io.BytesIO(z.read("data.txt")))
 
 
-def main():
+def main(parts):
     odt = refshim.load_reference()
+    if "backprop" in parts:
+        make_backprop(odt)
+    if "sino" in parts:
+        make_sino(odt)
+    print("wrote fixtures to", HERE)
+
+
+def make_backprop(odt):
     from odtbrain import _alg3d_bppt as bppt
     root = refshim.REFERENCE_ROOT
     data = os.path.join(root, "tests", "data")
@@ -162,8 +177,64 @@ def main():
         geo["tilt%d__points" % i] = pts
         geo["tilt%d__geo" % i] = np.array(mats)
     np.savez_compressed(os.path.join(HERE, "reference_geometry.npz"), **geo)
-    print("wrote fixtures to", HERE)
+
+
+def make_sino(odt):
+    """reference_sino.npz: the reference's golden vectors of the sinogram
+    preparation and of apple.correct (tests/data/processing__test_sino_*.zip,
+    apple__test_correct_reproduce.zip), and outputs of the reference's own
+    sinogram_as_rytov / sinogram_as_radon.  2D sinograms run the reference
+    unmodified (numpy.unwrap); 3D sinograms run it with unwrap_phase
+    provided by the oracle's restatement (scikit-image is absent)."""
+    from oracle import unwrap_oracle
+    data = os.path.join(refshim.REFERENCE_ROOT, "tests", "data")
+    out = {}
+    for name in ("test_sino_rytov", "test_sino_radon"):
+        out["zip_" + name] = _read_zip(os.path.join(
+            data, "processing__%s.zip" % name))
+    out["zip_test_correct_reproduce"] = _read_zip(os.path.join(
+        data, "apple__test_correct_reproduce.zip"))
+    refshim.UNWRAP_PHASE[0] = unwrap_oracle.unwrap_2d
+
+    def add(name, kind, sino, u0=None, align=True):
+        if kind == "rytov":
+            res = (odt.sinogram_as_rytov(sino.copy(), align=align)
+                   if u0 is None else
+                   odt.sinogram_as_rytov(sino.copy(), u0=u0, align=align))
+        else:
+            res = odt.sinogram_as_radon(sino.copy(), align=align)
+        out[name + "__sino"] = sino
+        if u0 is not None:
+            out[name + "__u0"] = np.asarray(u0)
+        out[name + "__out"] = res
+        out[name + "__kw"] = np.array(json.dumps(
+            {"kind": kind, "align": bool(align)}))
+
+    s2, _ = gauss_sino_2d(A=13, N=40, max_phase=9.0, ampl_range=(0.7, 1.2))
+    add("r2_c128", "rytov", s2)
+    add("r2_c128_noalign", "rytov", s2, align=False)
+    add("r2_c64", "rytov", s2.astype(np.complex64))
+    add("r2_radon", "radon", s2)
+    # background phase near pi: the lines start on either side of the cut
+    rng = np.random.default_rng(21)
+    tilt = np.exp(1j * (np.pi - 0.05 + 0.1 * rng.standard_normal((13, 1))))
+    add("r2_nearpi", "rytov", s2 * tilt)
+    u0 = 0.9 * np.exp(1j * np.linspace(-0.4, 0.3, 40))
+    add("r2_u0_array", "rytov", s2 * u0, u0=u0)
+    add("r2_u0_scalar", "rytov", s2 * 2.0, u0=2.0)
+    s3, _ = gauss_sino_3d(A=9, Nx=22, Ny=18, max_phase=11.0,
+                          ampl_range=(0.8, 1.1))
+    add("r3_c128", "rytov", s3)
+    add("r3_c128_noalign", "rytov", s3, align=False)
+    add("r3_c64", "rytov", s3.astype(np.complex64))
+    add("r3_radon", "radon", s3)
+    tilt3 = np.exp(1j * (np.pi - 0.02 + 0.05 * rng.standard_normal((9, 1, 1))))
+    add("r3_nearpi", "rytov", s3 * tilt3)
+    u03 = 1.1 * np.exp(1j * np.linspace(0, 0.5, 22))[None, None, :]
+    add("r3_u0_array", "rytov", s3 * u03, u0=u03)
+    np.savez_compressed(os.path.join(HERE, "reference_sino.npz"), **out)
+    refshim.UNWRAP_PHASE[0] = None
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or ["backprop", "sino"])

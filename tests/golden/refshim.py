@@ -12,8 +12,11 @@ The stand-ins follow the behaviour the reference relies on:
   backward stand-in therefore uses ``scipy.fft.ifftn(..., norm="forward")``.
 * ``numexpr.evaluate(expr, local_dict, casting, out)`` -- evaluated with
   NumPy (``_alg3d_bpp.py:434-437, 518-523``).
-* ``skimage.restoration.unwrap_phase`` -- raises; it is only needed by
-  ``sinogram_as_rytov``, which is not on the backpropagation path.
+* ``skimage.restoration.unwrap_phase`` -- raises, unless a restatement is
+  installed in ``UNWRAP_PHASE`` (make_golden.py installs the oracle's, to
+  run the reference's 3D ``sinogram_as_rytov`` around it).
+* ``FFTW.N`` -- the number of transformed elements, which ``apple.correct``
+  divides by (odtbrain/apple.py:243).
 """
 import os
 import sys
@@ -39,6 +42,7 @@ def _make_pyfftw():
             self.output_array = output_array
             self.axes = tuple(axes)
             self.direction = direction
+            self.N = int(np.prod([input_array.shape[a] for a in self.axes]))
 
         def execute(self):
             if self.direction == "FFTW_FORWARD":
@@ -77,12 +81,21 @@ def _make_numexpr():
     return mod
 
 
+# Stand-in for skimage.restoration.unwrap_phase(image, rng=...): None
+# raises; make_golden.py installs the oracle's restatement
+# (oracle/unwrap_oracle.py:unwrap_2d) to run the reference's 3D
+# sinogram_as_rytov / sinogram_as_radon around it.
+UNWRAP_PHASE = [None]
+
+
 def _make_skimage():
     sk = types.ModuleType("skimage")
     rest = types.ModuleType("skimage.restoration")
 
-    def unwrap_phase(*args, **kwargs):
-        raise NotImplementedError("scikit-image is not installed")
+    def unwrap_phase(image, wrap_around=False, rng=None, **kwargs):
+        if UNWRAP_PHASE[0] is None:
+            raise NotImplementedError("scikit-image is not installed")
+        return UNWRAP_PHASE[0](np.asarray(image, dtype=np.float64))
 
     rest.unwrap_phase = unwrap_phase
     sk.restoration = rest
