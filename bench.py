@@ -92,6 +92,14 @@ WORKLOADS["rytov"] = dict(
     name="sinogram_as_rytov: A=200 x 256x256 complex64 field exp(a + i*phi) "
          "of the ellipsoid phantom -> Rytov sinogram, reliability-sorted 2D "
          "unwrap per frame + align_unwrapped")
+# missing-apple-core correction of the headline reconstruction (the step
+# after the reconstruction; the reference's apple.correct)
+WORKLOADS["apple"] = dict(
+    A=200, n=256, padfac=1.75, intp_order=2, res=3.0, nm=1.333, lD=0.0,
+    seed=2024, count_range=(3, 12), semi_range=(8, 60), axis=None,
+    name="apple.correct: 256^3 complex64 reconstruction of the headline "
+         "sinogram, method nn, enforce_envelope 0.95, max_iter 100, "
+         "min_diff 0.01 (single-precision 3D FFTs)")
 WORKLOAD = WORKLOADS["c2"]
 WORKLOAD_NAME = WORKLOAD["name"]
 CPU_SAMPLE_ANGLES = 4
@@ -827,6 +835,104 @@ def run_rytov(args):
     print(json.dumps(line), flush=True)
 
 
+def run_apple(args):
+    """apple.correct on the 256^3 reconstruction of the headline sinogram:
+    one step = one correction (iterations until the reference's stopping
+    test); the unit counts voxels times iterations."""
+    import ctypes
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    from odtbrain_gb300 import build as native_build
+    native_build.build()
+    from odtbrain_gb300 import _native
+    from odtbrain_gb300 import apple as gapple
+    from odtbrain_gb300._alg3d import Backprop3D
+    w = WORKLOAD
+    sino, angles = make_workload()
+    rec = Backprop3D(tuple(sino.shape), angles, w["res"], w["nm"],
+                     lD=w["lD"], padfac=w["padfac"],
+                     intp_order=w["intp_order"], input_dtype="complex64",
+                     device=dev)
+    vol = rec(torch.from_numpy(sino).to(dev))
+    shape = tuple(vol.shape)
+    N = int(np.prod(shape))
+    fr = vol.real.contiguous()
+    d = gapple._desc(shape, w["res"], w["nm"])
+    L = _native.lib()
+    nb = ctypes.c_uint64()
+    _native.check(L.odt_apple_workspace_size(ctypes.byref(d),
+                                             ctypes.byref(nb)))
+    ws = torch.empty(nb.value, dtype=torch.uint8, device=dev)
+    out = torch.empty(shape, dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    its = ctypes.c_int32()
+
+    def step():
+        _native.check(L.odt_apple_correct(
+            ctypes.byref(d), ctypes.c_void_p(fr.data_ptr()), None,
+            ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ws.data_ptr()),
+            nb.value, ctypes.byref(its), ctypes.c_void_p(stream.cuda_stream)))
+    flush = torch.empty(L2_FLUSH_BYTES, device=dev, dtype=torch.uint8)
+    if args.ncu_case:
+        d.max_iter = 3
+        step()
+        torch.cuda.synchronize()
+        print("ncu case done")
+        return
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms, step_ms = _timed(step, args.steps, args.warmup, flush, stream)
+    clk = clocks.stop()
+    iters = its.value
+    unit = "voxel-iterations/s"
+    value = N * iters / (ms / 1e3)
+    host = vol.cpu().numpy()
+
+    def e2e():
+        gapple.correct(host, w["res"], w["nm"])
+    e2e_ms, _ = _timed(e2e, max(3, min(args.steps, 3)), 1, flush, stream)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import apple_oracle
+        k = 2
+        t0 = time.perf_counter()
+        apple_oracle.correct(host, w["res"], w["nm"], max_iter=k,
+                             min_diff=0.0)
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": N * k / cpu_s, "unit": unit, "cores": 1,
+               "kind": "port",
+               "sample": "%d iterations (oracle, NumPy + scipy.fft, setup "
+                         "and envelope included)" % k}
+    # algorithmic bytes per voxel and iteration: the complex64 volume read
+    # and written once, the original spectrum (8 B) and envelope (4 B) read
+    algo = 28.0 * N * iters
+    peak, peak_kind = measured_peaks()
+    achieved = algo / (ms / 1e3) / 1e9
+    line = {"metric": "apple.correct voxel-iterations/s on 1 GB300 (FP32 "
+                      "FFTs)",
+            "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic",
+            "config": {"workload": w["name"], "iterations": iters,
+                       "l2": "256 MiB flush before every timed step"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "note": "28 B per voxel-iteration (volume read + "
+                                 "write, original spectrum and envelope "
+                                 "read); the five FFT passes per iteration "
+                                 "move about 85 B"},
+            "clocks": clk, "gpu_launches_per_iteration": 5,
+            "step_ms": step_ms,
+            "e2e": {"value": N * iters / (e2e_ms / 1e3), "unit": unit,
+                    "h2d_bytes_per_step": int(host.nbytes),
+                    "d2h_bytes_per_step": int(N * 8), "ms_per_step": e2e_ms},
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
 def run_ncu_case(rotate_case=False):
     """Small case for ncu captures: the workload's plane and volume sizes
     with 8 angles and the save_memory workspace, or (``rotate_case``) 16
@@ -859,7 +965,14 @@ def main():
     args = parse_args()
     WORKLOAD = WORKLOADS[args.config]
     WORKLOAD_NAME = WORKLOAD["name"]
-    if args.config == "rytov":
+    if args.config == "apple":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference's apple.correct needs pyFFTW, "
+                              "which is not installed"}))
+        else:
+            run_apple(args)
+    elif args.config == "rytov":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":
                               "the reference's 3D sinogram_as_rytov calls "

@@ -318,6 +318,47 @@ odt_status odt_sino_launch_count(const odt_sino_desc *desc, int32_t *count);
  * gave up or a frame did not join into one tree. */
 odt_status odt_sino_read_status(const void *workspace, void *stream);
 
+/* ---- Missing-apple-core correction ---------------------------------------
+ * Replaces odtbrain.apple.correct (odtbrain/apple.py:113-263): iterative
+ * filling of the apple core of the object function's spectrum with the
+ * non-negativity ("nn") or symmetric-histogram ("sh") constraint, single-
+ * precision 3D FFTs like the reference's pyFFTW plans.
+ *   volume (n0, n1, n2) = the reconstruction's (Nx, Ny, Nx); n0 == n2
+ *   f_real    device, n0*n1*n2 float32: the real part of f
+ *   mask      device, n0*n1*n2 bytes (nonzero = use voxel) or NULL
+ *   out       device, n0*n1*n2 complex64: the corrected object function
+ *   gauss_weights  host, 2*gauss_radius+1 doubles: the 1D Gaussian of
+ *             scipy.ndimage.gaussian_filter for sigma = max(shape)/100,
+ *             truncate 4 (needed when enforce_envelope != 0)
+ *   *iterations    iterations run before the stopping test ended the loop
+ * Synchronous: it waits for `stream` between chunks of iterations. */
+/* ODT_APPLE_NONE: no constraint (what the reference's loop does for any
+ * other method name) */
+enum odt_apple_method { ODT_APPLE_NN = 0, ODT_APPLE_SH = 1, ODT_APPLE_NONE = 2 };
+typedef struct odt_apple_desc {
+    int32_t n0, n1, n2;
+    double res, nm;
+    int32_t method;          /* odt_apple_method                           */
+    double enforce_envelope; /* in [0, 1]; 0 disables the envelope         */
+    int32_t max_iter;
+    double min_diff;
+    int32_t use_bg_shell;    /* background ellipsoid shell of width ...    */
+    double bg_shell_width;   /* ... bg_shell_width                         */
+    int32_t gauss_radius;
+    const double *gauss_weights;
+} odt_apple_desc;
+odt_status odt_apple_workspace_size(const odt_apple_desc *desc, size_t *bytes);
+/* Voxel flags of the correction (device, n0*n1*n2 bytes, stream-ordered):
+ * bit 0 apple core (apple_core_3d, odtbrain/apple.py:8-53), bit 1 outside
+ * the inscribed ellipsoid (spillover_region, :353-363), bit 2 background
+ * shell (ellipsoid_shell, :281-286, when use_bg_shell), bit 3 mask. */
+odt_status odt_apple_flags(const odt_apple_desc *desc, const uint8_t *mask,
+                           uint8_t *flags, void *stream);
+odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real,
+                             const uint8_t *mask, void *out, void *workspace,
+                             size_t workspace_bytes, int32_t *iterations,
+                             void *stream);
+
 /* Wait for `stream`, then return ODT_ERR_DEVICE_CHECK if any kernel of this
  * plan recorded a failed internal check since the last call (the status word
  * is cleared). */

@@ -22,6 +22,7 @@ ODT_GEOM_Y_AXIS, ODT_GEOM_AFFINE3D = 0, 1
 ODT_INPUT_C64, ODT_INPUT_C128 = 0, 1
 ODT_DATA_F32, ODT_DATA_F64, ODT_DATA_C64, ODT_DATA_C128 = 0, 1, 2, 3
 ODT_SINO_RYTOV, ODT_SINO_RADON, ODT_SINO_ALIGN, ODT_SINO_UNWRAP = 0, 1, 2, 3
+ODT_APPLE_NN, ODT_APPLE_SH, ODT_APPLE_NONE = 0, 1, 2
 # size of the static scratch of odt_bpp3d_execute_noalloc
 NOALLOC_SCRATCH_BYTES = 64 << 20
 
@@ -48,6 +49,9 @@ EXPORTED_SYMBOLS = (
     "odt_sino_prepare",
     "odt_sino_launch_count",
     "odt_sino_read_status",
+    "odt_apple_workspace_size",
+    "odt_apple_correct",
+    "odt_apple_flags",
     "odt_status_string",
     "odt_last_error",
 )
@@ -118,6 +122,25 @@ class SinoDesc(ctypes.Structure):
     ]
 
 
+class AppleDesc(ctypes.Structure):
+    """odt_apple_desc of include/odtbrain_gb300.h."""
+    _fields_ = [
+        ("n0", ctypes.c_int32),
+        ("n1", ctypes.c_int32),
+        ("n2", ctypes.c_int32),
+        ("res", ctypes.c_double),
+        ("nm", ctypes.c_double),
+        ("method", ctypes.c_int32),
+        ("enforce_envelope", ctypes.c_double),
+        ("max_iter", ctypes.c_int32),
+        ("min_diff", ctypes.c_double),
+        ("use_bg_shell", ctypes.c_int32),
+        ("bg_shell_width", ctypes.c_double),
+        ("gauss_radius", ctypes.c_int32),
+        ("gauss_weights", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
 class StageTiming(ctypes.Structure):
     _fields_ = [
         ("ms", ctypes.c_double * 4),
@@ -185,6 +208,12 @@ def lib():
         L.odt_sino_launch_count.argtypes = [sd,
                                             ctypes.POINTER(ctypes.c_int32)]
         L.odt_sino_read_status.argtypes = [vp, vp]
+        ad = ctypes.POINTER(AppleDesc)
+        L.odt_apple_workspace_size.argtypes = [
+            ad, ctypes.POINTER(ctypes.c_uint64)]
+        L.odt_apple_correct.argtypes = [ad, vp, vp, vp, vp, ctypes.c_uint64,
+                                        ctypes.POINTER(ctypes.c_int32), vp]
+        L.odt_apple_flags.argtypes = [ad, vp, vp, vp]
         i32 = ctypes.c_int32
         L.odt_mlp_gain_forward.argtypes = [ctypes.POINTER(MlpParams), i32,
                                            i32, i32, vp, vp, i32, vp, vp]
@@ -203,7 +232,8 @@ def lib():
                      "odt_mlp_gain_backward", "odt_odt_to_ri",
                      "odt_opt_to_ri", "odt_sino_workspace_size",
                      "odt_sino_prepare", "odt_sino_launch_count",
-                     "odt_sino_read_status"):
+                     "odt_sino_read_status", "odt_apple_workspace_size",
+                     "odt_apple_correct", "odt_apple_flags"):
             getattr(L, name).restype = ctypes.c_int
         L.odt_status_string.argtypes = [ctypes.c_int]
         L.odt_status_string.restype = ctypes.c_char_p

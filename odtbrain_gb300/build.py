@@ -18,7 +18,7 @@ OBJDIR = os.path.join(LIBDIR, "obj")
 LIBNAME = "libodtbrain_gb300.so"
 LIB = os.path.join(LIBDIR, LIBNAME)
 SOURCES = ["capi.cu", "stages.cu", "rotate.cu", "adjoint.cu", "mlp.cu", "translate.cu",
-           "unwrap.cu"]
+           "unwrap.cu", "apple.cu"]
 HEADERS = ["odt_fft.cuh", "odt_internal.cuh", "odt_stage_util.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

@@ -1,0 +1,1021 @@
+// Missing-apple-core correction on the GPU: odtbrain.apple.correct
+// (odtbrain/apple.py:113-263) with apple_core_3d (:8-53), the constraints
+// constraint_nn / constraint_sh (:56-110), envelope_gauss (:289-350) and
+// spillover_region / ellipsoid_shell (:281-286, 353-363).
+//
+// The volume (n0, n1, n2) = (Nx, Ny, Nx) stays in HBM as complex64; the
+// 3D FFTs (single precision, unnormalised, like the reference's pyFFTW
+// plans) are line transforms in registers (odt_fft.cuh), one kernel per
+// axis.  One iteration of the reference's loop is five kernels:
+//   k_apple_s (axis 1, forward)
+//   k_apple_s (axis 0, forward; then per voxel: envelope suppression,
+//              DC update (method "sh"), restore of the non-core spectrum,
+//              sum of |spectrum| over the core; then axis 0 inverse)
+//   k_apple_dec  stopping criterion, one thread, in float32 like the
+//              reference's NumPy scalars
+//   k_apple_s (axis 1, inverse)
+//   k_apple_x (axis 2 inverse, times fl32(1/N) -> result; for "nn" and a
+//              following iteration also the constraint and the axis 2
+//              forward transform of the next iteration)
+// Kernels of iterations after the stop return at once; the host enqueues
+// iterations in chunks and reads the stop word between chunks.  Method
+// "sh" needs the spatial histogram before its constraint: per iteration
+// k_sh_minmax, k_sh_hist (NumPy's bin assignment), and the host computes
+// the thresholds from the 100 counts exactly as the reference's NumPy code.
+//
+// Once per call: voxel flags (core, spillover, background shell, user mask)
+// from the reference's FP64 formulas (k_apple_flags), the initial forward
+// transform (the original spectrum), and the envelope: |spectrum| with the
+// core set to NaN, padded and fftshifted (k_env_pad), the core filled from
+// the x/y-swapped volume (k_env_swap), remaining NaNs from the nearest known
+// voxel (Maurer et al.'s exact Euclidean feature transform, the algorithm
+// scipy.ndimage.distance_transform_edt implements: k_edt_*), and scipy's
+// gaussian_filter (FP64 sums in its order, float32 after each axis,
+// k_env_gauss).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/odtbrain_gb300.h"
+#include "odt_fft.cuh"
+#include "odt_internal.cuh"
+#include "odt_stage_util.cuh"
+
+namespace odt {
+namespace {
+
+constexpr uint8_t F_CORE = 1, F_SPOV = 2, F_SHELL = 4, F_MASK = 8;
+constexpr int CHUNK = 8;      // iterations enqueued between stop checks
+constexpr int HIST_BINS = 100;
+
+struct AppleCtl {
+    float prev, norm;
+    int stop;   // iterations done when the loop stopped, 0 while running
+    int iters;  // iterations done
+    unsigned long long minkey, maxkey;  // ordered keys (method "sh")
+    float lo, hi, fmin, fmax;           // method "sh" thresholds
+    unsigned int nan_count;
+    unsigned int pad;
+};
+
+struct AP {
+    int n0, n1, n2;
+    long long N;
+    const float2 *tw0, *tw1, *tw2;
+    const uint8_t *flags;
+    const float *evlp;  // NULL: envelope off
+    float ee;
+    float2 *orig;
+    float2 *buf;
+    float2 *data;
+    const float *freal;
+    double *state;  // [max_iter + 1], FP64 sums of |spectrum| over the core
+    AppleCtl *ctl;
+    int method;  // 0 nn, 1 sh, 2 none
+    int max_iter;
+    float min_diff;
+    float scale;
+    int has_mask;
+    unsigned int *hist;  // [HIST_BINS] (method "sh")
+    const float *edges;  // [HIST_BINS + 1] (method "sh")
+};
+
+__device__ __forceinline__ bool ran_out(const AP &P, int it)
+{
+    const int s = *(volatile const int *)&P.ctl->stop;
+    return s != 0 && s <= it;
+}
+
+// Spatial constraint of the reference's loop on one voxel value.
+__device__ __forceinline__ float2 constrain(const AP &P, float2 d, uint8_t fl, float fmin, float fmax, float lo,
+                                            float hi)
+{
+    if (P.method == 2)  // neither constraint (apple.py:222-227 with another method)
+        return d;
+    float re = d.x;
+    if (P.method == 0) {  // constraint_nn, apple.py:56-72
+        if (fl & F_SHELL)
+            re = 0.f;
+        if (fl & F_SPOV)
+            re = 0.f;
+        bool low = re < 0.f;
+        if (P.has_mask)
+            low = low && (fl & F_MASK);
+        if (low)
+            re = 0.f;
+    } else {  // constraint_sh, apple.py:75-110
+        const bool below = re > fmin && re < lo;
+        const bool above = re > hi && re < fmax;
+        bool out = below || above;
+        if (P.has_mask)
+            out = out && (fl & F_MASK);
+        if (out)
+            re = __fmul_rn(re, 0.5f);
+        if (fl & F_SHELL)
+            re = __fmul_rn(re, 0.5f);
+    }
+    return make_float2(re, 0.f);
+}
+
+// ---- axis 2 (contiguous lines) --------------------------------------------
+// mode 0: f.real -> forward -> buf (the original spectrum's first axis)
+// mode 1: constrain(f.real) -> forward -> buf (iteration 0's first axis)
+// mode 2: buf -> inverse -> * scale -> data; for "nn" with a following
+//         iteration: constrain -> forward -> buf
+// mode 3: constrain(data) -> forward -> buf (method "sh")
+template <class L, int LPC>
+__global__ void __launch_bounds__(LPC *L::TPL) k_apple_x(AP P, L line, int mode, int it)
+{
+    if (mode >= 2 && ran_out(P, it))
+        return;
+    extern __shared__ float2 smem[];
+    const int n = line.size();
+    const int ls = xslots<false>(n);
+    float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
+    copy_twiddles<L>(tw, P.tw2, n);
+    const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
+    const long long lid = (long long)blockIdx.x * LPC + l;
+    const bool valid = lid < (long long)P.n0 * P.n1;
+    const long long base = valid ? lid * n : 0;
+    float fmin = 0.f, fmax = 0.f, lo = 0.f, hi = 0.f;
+    if (P.method == 1) {
+        fmin = P.ctl->fmin;
+        fmax = P.ctl->fmax;
+        lo = P.ctl->lo;
+        hi = P.ctl->hi;
+    }
+    float2 v[L::SLOTS];
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int x = j + r * L::TPL;
+        float2 a = make_float2(0.f, 0.f);
+        if (valid && x < n) {
+            if (mode <= 1)
+                a = make_float2(P.freal[base + x], 0.f);
+            else if (mode == 2)
+                a = P.buf[base + x];
+            else
+                a = P.data[base + x];
+            if (mode == 1 || mode == 3)
+                a = constrain(P, a, P.flags[base + x], fmin, fmax, lo, hi);
+        }
+        v[r] = a;
+    }
+    __syncthreads();
+    int flip = 0;
+    if (mode == 2) {
+        line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip);
+        const bool next = P.method != 1 && it + 1 < P.max_iter && !ran_out(P, it + 1);
+#pragma unroll
+        for (int r = 0; r < L::SLOTS; ++r) {
+            const int x = j + r * L::TPL;
+            v[r] = make_float2(__fmul_rn(v[r].x, P.scale), __fmul_rn(v[r].y, P.scale));
+            if (valid && x < n) {
+                P.data[base + x] = v[r];
+                if (next)
+                    v[r] = constrain(P, v[r], P.flags[base + x], 0.f, 0.f, 0.f, 0.f);
+            }
+        }
+        if (!next)
+            return;  // uniform over the CTA
+        __syncthreads();
+    }
+    line.template run<-1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip);
+    if (!valid)
+        return;
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int x = j + r * L::TPL;
+        if (x < n)
+            P.buf[base + x] = v[r];
+    }
+}
+
+// ---- axes 1 and 0 (strided lines, KX adjacent lines per CTA) --------------
+// mode 0: forward (axis 1) ; mode 1: inverse (axis 1)
+// mode 2: axis 0 forward -> orig (the original spectrum) + core sum
+// mode 3: axis 0 forward -> frequency-domain step -> inverse (iteration)
+template <class L, int KX>
+__global__ void __launch_bounds__(KX *L::TPL) k_apple_s(AP P, L line, int axis, int mode, int it)
+{
+    if (mode != 2 && ran_out(P, it))
+        return;
+    extern __shared__ float2 smem[];
+    __shared__ double red[32];
+    const int n = line.size();
+    const int ls = xslots<true>(n);
+    float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls;
+    copy_twiddles<L>(tw, axis == 0 ? P.tw0 : P.tw1, n);
+    const long long inner = axis == 0 ? (long long)P.n1 * P.n2 : P.n2;
+    const long long stride = inner;
+    const long long ostride = (long long)P.n1 * P.n2;
+    const long long gpo = (inner + KX - 1) / KX;
+    const long long o = (long long)blockIdx.x / gpo;
+    const long long q0 = ((long long)blockIdx.x - o * gpo) * KX;
+    const int c = threadIdx.x % KX, j = threadIdx.x / KX;
+    const long long q = q0 + c;
+    const bool colok = q < inner;
+    const long long base = (axis == 0 ? 0 : o * ostride) + (colok ? q : 0);
+    float2 v[L::SLOTS];
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int k = j + r * L::TPL;
+        v[r] = (colok && k < n) ? P.buf[base + k * stride] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    int flip = 0;
+    if (mode == 1)
+        line.template run<1, true>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+    else
+        line.template run<-1, true>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+    double part = 0.0;
+    if (mode >= 2) {
+#pragma unroll
+        for (int r = 0; r < L::SLOTS; ++r) {
+            const int k = j + r * L::TPL;
+            if (!(colok && k < n))
+                continue;
+            const long long vox = base + k * stride;
+            const uint8_t fl = P.flags[vox];
+            float2 ft = v[r];
+            if (mode == 2) {
+                P.orig[vox] = ft;
+            } else {
+                if (P.evlp && hypotf(ft.x, ft.y) > P.evlp[vox])
+                    ft = make_float2(__fmul_rn(ft.x, P.ee), __fmul_rn(ft.y, P.ee));
+                if (!(fl & F_CORE)) {
+                    float2 og = P.orig[vox];
+                    if (P.method == 1 && vox == 0) {  // (orig + ft) / 2 at the DC term
+                        og = make_float2(__fmul_rn(__fadd_rn(og.x, ft.x), 0.5f),
+                                         __fmul_rn(__fadd_rn(og.y, ft.y), 0.5f));
+                        P.orig[0] = og;
+                    }
+                    ft = og;
+                }
+            }
+            if (fl & F_CORE)
+                part += (double)hypotf(ft.x, ft.y);
+            v[r] = ft;
+        }
+        // block sum of the core magnitudes
+        for (int s = 16; s > 0; s >>= 1)
+            part += __shfl_xor_sync(0xffffffffu, part, s);
+        if ((threadIdx.x & 31) == 0)
+            red[threadIdx.x >> 5] = part;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+                t += red[w];
+            atomicAdd(P.state + (mode == 2 ? 0 : it + 1), t);
+        }
+        if (mode == 2)
+            return;
+        __syncthreads();
+        line.template run<1, true>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+    }
+    if (!colok)
+        return;
+#pragma unroll
+    for (int r = 0; r < L::SLOTS; ++r) {
+        const int k = j + r * L::TPL;
+        if (k < n)
+            P.buf[base + k * stride] = v[r];
+    }
+}
+
+// init_state (it < 0) or the stopping test of iteration `it`, in float32 as
+// the reference's NumPy scalars: state = sum / N, diff = state - prev,
+// norm = diff at iteration 0, stop when |diff / norm| < min_diff.
+__global__ void k_apple_dec(AP P, int it)
+{
+    AppleCtl *c = P.ctl;
+    if (it < 0) {
+        c->prev = __fdiv_rn((float)P.state[0], (float)P.N);
+        return;
+    }
+    if (c->stop != 0 && c->stop <= it)
+        return;
+    const float cur = __fdiv_rn((float)P.state[it + 1], (float)P.N);
+    const float diff = __fsub_rn(cur, c->prev);
+    c->iters = it + 1;
+    if (it == 0) {
+        c->norm = diff;
+    } else if (fabsf(__fdiv_rn(diff, c->norm)) < P.min_diff) {
+        c->stop = it + 1;
+        return;
+    }
+    c->prev = cur;
+}
+
+// data = f.real + 0i (the state before the loop)
+__global__ void k_apple_load(AP P)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < P.N;
+         v += (long long)gridDim.x * blockDim.x)
+        P.data[v] = make_float2(P.freal[v], 0.f);
+}
+
+// ---- voxel flags (FP64, the reference's formulas and operation order) ----
+__device__ __forceinline__ double fftfreq(int k, int n)
+{
+    // numpy.fft.fftfreq: integer frequency times 1.0 / n
+    const int kk = k < (n - 1) / 2 + 1 ? k : k - n;
+    return __dmul_rn((double)kk, __ddiv_rn(1.0, (double)n));
+}
+
+__device__ __forceinline__ bool outside_ellipsoid(int i0, int i1, int i2, int n0, int n1, int n2, double shell)
+{
+    const double cx = n0 / 2.0, cy = n1 / 2.0, cz = n2 / 2.0;
+    const double a = __ddiv_rn(__dsub_rn((double)i0, cx), __dsub_rn(cx, shell));
+    const double b = __ddiv_rn(__dsub_rn((double)i1, cy), __dsub_rn(cy, shell));
+    const double c = __ddiv_rn(__dsub_rn((double)i2, cz), __dsub_rn(cz, shell));
+    return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c)) > 1.0;
+}
+
+__global__ void k_apple_flags(int n0, int n1, int n2, double km, int use_shell, double shell_width,
+                              const uint8_t *mask, uint8_t *flags)
+{
+    const long long N = (long long)n0 * n1 * n2;
+    const double twopi = 6.283185307179586;
+    const double sqrt2km = __dmul_rn(1.4142135623730951, km);
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < N;
+         v += (long long)gridDim.x * blockDim.x) {
+        const int i0 = (int)(v / ((long long)n1 * n2));
+        const int i1 = (int)((v / n2) % n1);
+        const int i2 = (int)(v % n2);
+        const double fx = fftfreq(i0, n0), fy = fftfreq(i1, n1), fz = fftfreq(i2, n2);
+        const double ky = __dmul_rn(twopi, fy);
+        const double kxz = __dmul_rn(twopi, sqrt(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fz, fz))));
+        const double kr =
+            __dmul_rn(twopi, sqrt(__dadd_rn(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy)), __dmul_rn(fz, fz))));
+        double root = __dsub_rn(__dmul_rn(__dmul_rn(2.0, km), kxz), __dmul_rn(kxz, kxz));
+        if (root < 0.0)
+            root = 0.0;
+        bool core = fabs(ky) > sqrt(root);
+        if (kr > sqrt2km)
+            core = false;
+        uint8_t f = core ? F_CORE : 0;
+        if (outside_ellipsoid(i0, i1, i2, n0, n1, n2, 0.0))
+            f |= F_SPOV;
+        if (use_shell && (outside_ellipsoid(i0, i1, i2, n0, n1, n2, 0.0) !=
+                          outside_ellipsoid(i0, i1, i2, n0, n1, n2, shell_width)))
+            f |= F_SHELL;
+        if (mask && mask[v])
+            f |= F_MASK;
+        flags[v] = f;
+    }
+}
+
+// ---- envelope --------------------------------------------------------------
+struct EnvGeom {
+    int n0, n1, n2, msh;
+    int off0, off1, off2;  // where the volume sits in the padded cube
+};
+
+__device__ __forceinline__ int wrapi(int i, int n) { return ((i % n) + n) % n; }
+
+// hull_pad = fftshift(|orig|, core -> NaN) inside the slice, 0 outside;
+// cpad = fftshift(core) inside the slice
+__global__ void k_env_pad(EnvGeom G, const float2 *orig, const uint8_t *flags, double *hp, uint8_t *cpad)
+{
+    const long long M = (long long)G.msh * G.msh * G.msh;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < M;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int a = (int)(p / ((long long)G.msh * G.msh)), b = (int)((p / G.msh) % G.msh), c = (int)(p % G.msh);
+        const int i0 = a - G.off0, i1 = b - G.off1, i2 = c - G.off2;
+        double h = 0.0;
+        uint8_t cp = 0;
+        if (i0 >= 0 && i0 < G.n0 && i1 >= 0 && i1 < G.n1 && i2 >= 0 && i2 < G.n2) {
+            const int s0 = wrapi(i0 - G.n0 / 2, G.n0), s1 = wrapi(i1 - G.n1 / 2, G.n1),
+                      s2 = wrapi(i2 - G.n2 / 2, G.n2);
+            const long long v = ((long long)s0 * G.n1 + s1) * G.n2 + s2;
+            if (flags[v] & F_CORE) {
+                h = __longlong_as_double(0x7ff8000000000000ll);
+                cp = 1;
+            } else {
+                const float2 o = orig[v];
+                h = (double)hypotf(o.x, o.y);
+            }
+        }
+        hp[p] = h;
+        cpad[p] = cp;
+    }
+}
+
+// out = core ? in transposed over the first two axes : in; counts NaNs left
+__global__ void k_env_swap(EnvGeom G, const double *in, const uint8_t *cpad, double *out, unsigned int *nan_count)
+{
+    const long long M = (long long)G.msh * G.msh * G.msh;
+    unsigned int cnt = 0;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < M;
+         p += (long long)gridDim.x * blockDim.x) {
+        double h = in[p];
+        if (cpad[p]) {
+            const int a = (int)(p / ((long long)G.msh * G.msh)), b = (int)((p / G.msh) % G.msh),
+                      c = (int)(p % G.msh);
+            h = in[((long long)b * G.msh + a) * G.msh + c];
+        }
+        out[p] = h;
+        cnt += (h != h);
+    }
+    for (int s = 16; s > 0; s >>= 1)
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, s);
+    if ((threadIdx.x & 31) == 0 && cnt)
+        atomicAdd(nan_count, cnt);
+}
+
+// Exact Euclidean feature transform (Maurer, Qi, Raghavan, IEEE PAMI 25(2),
+// 2003): per axis, the lower envelope of the sites' distance parabolas along
+// every line; axes in order 0, 1, 2; a tie goes to the earlier site.
+// ft holds the linear index of the nearest known voxel, -1 for none yet.
+__global__ void k_edt_init(long long M, const double *hp, int *ft)
+{
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < M;
+         p += (long long)gridDim.x * blockDim.x)
+        ft[p] = (hp[p] != hp[p]) ? -1 : (int)p;
+}
+
+__global__ void k_edt_pass(int msh, int d, int *ft, int *scratch)
+{
+    const long long nl = (long long)msh * msh;
+    const long long line = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= nl)
+        return;
+    const long long m2 = (long long)msh * msh;
+    // fixed coordinates of the line
+    int co[3];
+    const int u = (int)(line / msh), w = (int)(line % msh);
+    if (d == 0) {
+        co[1] = u;
+        co[2] = w;
+    } else if (d == 1) {
+        co[0] = u;
+        co[2] = w;
+    } else {
+        co[0] = u;
+        co[1] = w;
+    }
+    const long long strides[3] = {m2, msh, 1};
+    co[d] = 0;
+    const long long base = (long long)co[0] * m2 + (long long)co[1] * msh + co[2];
+    const long long st = strides[d];
+    int *f = scratch + line * 2 * msh;  // copy of the line's features
+    int *g = f + msh;                   // site stack (positions)
+    auto coord = [&](int idx, int k) -> long long {
+        return k == 0 ? idx / m2 : (k == 1 ? (idx / msh) % msh : idx % msh);
+    };
+    for (int i = 0; i < msh; ++i)
+        f[i] = ft[base + i * st];
+    int l = -1;
+    for (int i = 0; i < msh; ++i) {
+        const int fi = f[i];
+        if (fi < 0)
+            continue;
+        long long wR = 0;
+        for (int k = 0; k < 3; ++k)
+            if (k != d) {
+                const long long t = coord(fi, k) - co[k];
+                wR += t * t;
+            }
+        const long long fd = coord(fi, d);
+        while (l >= 1) {
+            const int iu = f[g[l - 1]], iv = f[g[l]];
+            const long long a = coord(iv, d) - coord(iu, d);
+            const long long b = fd - coord(iv, d);
+            const long long c = a + b;
+            long long uR = 0, vR = 0;
+            for (int k = 0; k < 3; ++k)
+                if (k != d) {
+                    const long long tu = coord(iu, k) - co[k], tv = coord(iv, k) - co[k];
+                    uR += tu * tu;
+                    vR += tv * tv;
+                }
+            if (c * vR - b * uR - a * wR - a * b * c <= 0)
+                break;
+            --l;
+        }
+        g[++l] = i;
+    }
+    if (l < 0)
+        return;
+    const int maxl = l;
+    l = 0;
+    auto dist = [&](int idx, int i) -> long long {
+        long long s = 0;
+        for (int k = 0; k < 3; ++k) {
+            const long long t = coord(idx, k) - (k == d ? i : co[k]);
+            s += t * t;
+        }
+        return s;
+    };
+    for (int i = 0; i < msh; ++i) {
+        long long d1 = dist(f[g[l]], i);
+        while (l < maxl) {
+            const long long d2 = dist(f[g[l + 1]], i);
+            if (d1 <= d2)
+                break;
+            d1 = d2;
+            ++l;
+        }
+        ft[base + i * st] = f[g[l]];
+    }
+}
+
+__global__ void k_edt_gather(long long M, const int *ft, const double *in, double *out)
+{
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < M;
+         p += (long long)gridDim.x * blockDim.x)
+        out[p] = ft[p] >= 0 ? in[ft[p]] : in[p];
+}
+
+// scipy.ndimage.gaussian_filter (mode constant 0): per axis in order 0, 1,
+// 2, acc = x[i] w0 + sum_{j = r..1} (x[i+j] + x[i-j]) w_j in FP64, rounded
+// to float32 after each axis.  Axis 0 reads the padded cube's slice (the
+// fftshifted hull); the last axis writes ifftshift(result) (the envelope in
+// FFT order).
+__global__ void k_env_gauss(EnvGeom G, int axis, const double *hp, const float *in, float *out, const double *w,
+                            int r)
+{
+    const long long N = (long long)G.n0 * G.n1 * G.n2;
+    const int n[3] = {G.n0, G.n1, G.n2};
+    const long long st[3] = {(long long)G.n1 * G.n2, G.n2, 1};
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < N;
+         v += (long long)gridDim.x * blockDim.x) {
+        const int ii[3] = {(int)(v / st[0]), (int)((v / st[1]) % G.n1), (int)(v % G.n2)};
+        auto at = [&](int k) -> double {  // input at position k along the axis
+            if (k < 0 || k >= n[axis])
+                return 0.0;
+            if (axis == 0) {
+                const long long p = ((long long)(k + G.off0) * G.msh + (ii[1] + G.off1)) * G.msh + (ii[2] + G.off2);
+                return (double)(float)hp[p];
+            }
+            return (double)in[v + (long long)(k - ii[axis]) * st[axis]];
+        };
+        const int i = ii[axis];
+        double acc = __dmul_rn(at(i), w[r]);
+        for (int j = r; j >= 1; --j)
+            acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(at(i + j), at(i - j)), w[r + j]));
+        long long o = v;
+        if (axis == 2) {  // ifftshift: out[k] = g[(k + n/2) mod n]  =>  g[i] -> out[i - n/2]
+            const int s0 = wrapi(ii[0] - G.n0 / 2, G.n0), s1 = wrapi(ii[1] - G.n1 / 2, G.n1),
+                      s2 = wrapi(ii[2] - G.n2 / 2, G.n2);
+            o = ((long long)s0 * G.n1 + s1) * G.n2 + s2;
+        }
+        out[o] = (float)acc;
+    }
+}
+
+// ---- method "sh": min / max over the spillover (and shell) voxels and the
+// histogram of all values in [fmin, fmax] -----------------------------------
+__device__ __forceinline__ unsigned long long fkey(float f)
+{
+    const unsigned int b = __float_as_uint(f);
+    return (b >> 31) ? (unsigned long long)(~b) : (unsigned long long)(b | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float fkey_val(unsigned long long k)
+{
+    const unsigned int u = (unsigned int)k;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float((u >> 31) ? (u & 0x7fffffffu) : ~u);
+#else
+    const unsigned int b = (u >> 31) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+#endif
+}
+
+__global__ void k_sh_minmax(AP P, int it)
+{
+    if (ran_out(P, it))
+        return;
+    unsigned long long mn = ~0ull, mx = 0;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < P.N;
+         v += (long long)gridDim.x * blockDim.x) {
+        if (P.flags[v] & (F_SPOV | F_SHELL)) {
+            const unsigned long long k = fkey(P.data[v].x);
+            mn = min(mn, k);
+            mx = max(mx, k);
+        }
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+        mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, s));
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, s));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&P.ctl->minkey, mn);
+        atomicMax(&P.ctl->maxkey, mx);
+    }
+}
+
+// numpy.histogram's bin of x for equal bins (float32 arithmetic): index =
+// int(((x - first) / (last - first)) * bins), the last edge in the last bin,
+// then one-step corrections against the float32 edges.
+__global__ void k_sh_hist(AP P, int it)
+{
+    if (ran_out(P, it))
+        return;
+    __shared__ unsigned int h[HIST_BINS];
+    for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x)
+        h[i] = 0;
+    __syncthreads();
+    const float first = P.edges[0], last = P.edges[HIST_BINS];
+    const float denom = __fsub_rn(last, first);
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < P.N;
+         v += (long long)gridDim.x * blockDim.x) {
+        const float x = P.data[v].x;
+        if (!(x >= first && x <= last))
+            continue;
+        int idx = (int)__fmul_rn(__fdiv_rn(__fsub_rn(x, first), denom), (float)HIST_BINS);
+        idx = min(max(idx, 0), HIST_BINS);  // (a zero-width range gives no NaN index)
+        if (idx == HIST_BINS)
+            idx -= 1;
+        if (idx > 0 && x < P.edges[idx])
+            idx -= 1;
+        if (x >= P.edges[idx + 1] && idx != HIST_BINS - 1)
+            idx += 1;
+        idx = min(max(idx, 0), HIST_BINS - 1);
+        atomicAdd(&h[idx], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x)
+        if (h[i])
+            atomicAdd(&P.hist[i], h[i]);
+}
+
+// ---------------------------------------------------------------------------
+template <class L>
+size_t smem_x(int n)
+{
+    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + n) * sizeof(float2);
+}
+template <class L>
+size_t smem_s(int n)
+{
+    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + n) * sizeof(float2);
+}
+
+cudaError_t launch_x(const AP &P, int mode, int it, cudaStream_t s)
+{
+    return with_line(P.n2, [&](auto line) {
+        using L = decltype(line);
+        constexpr int LPC = Cfg<L>::LPC;
+        const size_t sm = smem_x<L>(P.n2);
+        cudaFuncSetAttribute(k_apple_x<L, LPC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        const long long lines = (long long)P.n0 * P.n1;
+        k_apple_x<L, LPC><<<(unsigned)((lines + LPC - 1) / LPC), LPC * L::TPL, sm, s>>>(P, line, mode, it);
+        return cudaGetLastError();
+    });
+}
+
+cudaError_t launch_s(const AP &P, int axis, int mode, int it, cudaStream_t s)
+{
+    const int n = axis == 0 ? P.n0 : P.n1;
+    return with_line(n, [&](auto line) {
+        using L = decltype(line);
+        constexpr int KX = Cfg<L>::KX;
+        const size_t sm = smem_s<L>(n);
+        cudaFuncSetAttribute(k_apple_s<L, KX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        const long long inner = axis == 0 ? (long long)P.n1 * P.n2 : P.n2;
+        const long long outer = axis == 0 ? 1 : P.n0;
+        const long long grid = outer * ((inner + KX - 1) / KX);
+        k_apple_s<L, KX><<<(unsigned)grid, KX * L::TPL, sm, s>>>(P, line, axis, mode, it);
+        return cudaGetLastError();
+    });
+}
+
+struct Layout {
+    size_t ctl, state, hist, edges, tw0, tw1, tw2, gw, flags, buf, orig, evlp, hp0, hp1, cpad, ft, scratch, g0, g1,
+        total;
+};
+
+Layout layout_of(const odt_apple_desc &d)
+{
+    const long long N = (long long)d.n0 * d.n1 * d.n2;
+    const long long msh = std::max(d.n0, d.n1);
+    const long long M = msh * msh * msh;
+    Layout L{};
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o += (bytes + 255) / 256 * 256;
+        return at;
+    };
+    L.ctl = take(sizeof(AppleCtl));
+    L.state = take((size_t)(std::max(d.max_iter, 0) + 1) * 8);
+    L.hist = take(HIST_BINS * 4);
+    L.edges = take((HIST_BINS + 1) * 4);
+    L.tw0 = take((size_t)d.n0 * 8);
+    L.tw1 = take((size_t)d.n1 * 8);
+    L.tw2 = take((size_t)d.n2 * 8);
+    L.gw = take((size_t)(2 * std::max(d.gauss_radius, 0) + 1) * 8);
+    L.flags = take((size_t)N);
+    L.buf = take((size_t)N * 8);
+    L.orig = take((size_t)N * 8);
+    if (d.enforce_envelope != 0.0) {
+        L.evlp = take((size_t)N * 4);
+        L.hp0 = take((size_t)M * 8);
+        L.hp1 = take((size_t)M * 8);
+        L.cpad = take((size_t)M);
+        L.ft = take((size_t)M * 4);
+        L.scratch = take((size_t)msh * msh * 2 * msh * 4);
+        L.g0 = take((size_t)N * 4);
+        L.g1 = take((size_t)N * 4);
+    }
+    L.total = o;
+    return L;
+}
+
+odt_status check_desc(const odt_apple_desc *d)
+{
+    if (!d)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL descriptor");
+    if (d->n0 < 1 || d->n1 < 1 || d->n2 < 1)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "volume sizes must be positive");
+    if (d->n0 != d->n2)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "`shape[0]` and `shape[2]` must be identical!");
+    for (int n : {d->n0, d->n1, d->n2})
+        if (!(n <= GenericLine::TPL * GenericLine::SLOTS || (n <= 4096 && (n & (n - 1)) == 0)))
+            return (odt_status)set_error(ODT_ERR_UNSUPPORTED,
+                                         "volume axes longer than 1024 must be powers of two up to 4096");
+    if (!(d->enforce_envelope >= 0.0 && d->enforce_envelope <= 1.0))
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "`enforce_envelope` must be in interval [0, 1]");
+    if (d->method != ODT_APPLE_NN && d->method != ODT_APPLE_SH && d->method != ODT_APPLE_NONE)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "unknown constraint method");
+    if (d->max_iter < 0)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "max_iter must not be negative");
+    if (d->enforce_envelope != 0.0 && (d->gauss_radius < 0 || !d->gauss_weights))
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "envelope needs the Gaussian weights");
+    if ((long long)d->n0 * d->n1 * d->n2 >= (1ll << 31))
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "volume too large (2^31 voxels or more)");
+    return ODT_OK;
+}
+
+odt_status cuda_fail(const char *what, cudaError_t e)
+{
+    return (odt_status)set_error(ODT_ERR_CUDA, (std::string(what) + ": " + cudaGetErrorString(e)).c_str());
+}
+
+std::vector<float2> twiddles(int n)
+{
+    std::vector<float2> t(n);
+    for (int m = 0; m < n; ++m)
+        t[m] = make_float2((float)std::cos(-2.0 * M_PI * m / n), (float)std::sin(-2.0 * M_PI * m / n));
+    return t;
+}
+
+// count_to_half of apple.py:266-278 on counts a[0..len)
+int count_to_half(const unsigned int *a, int len, int step)
+{
+    int num = 0;
+    for (int i = 1; i < len; ++i) {
+        if ((double)a[i * step] < (double)a[0] / 2.0)
+            break;
+        ++num;
+    }
+    return num;
+}
+
+}  // namespace
+}  // namespace odt
+
+using namespace odt;
+
+extern "C" {
+
+odt_status odt_apple_workspace_size(const odt_apple_desc *desc, size_t *bytes)
+{
+    const odt_status st = check_desc(desc);
+    if (st != ODT_OK)
+        return st;
+    if (!bytes)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL output pointer");
+    *bytes = layout_of(*desc).total;
+    return ODT_OK;
+}
+
+odt_status odt_apple_flags(const odt_apple_desc *desc, const uint8_t *mask, uint8_t *flags, void *stream)
+{
+    const odt_status st = check_desc(desc);
+    if (st != ODT_OK)
+        return st;
+    if (!flags)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL device pointer");
+    const odt_apple_desc &d = *desc;
+    const long long N = (long long)d.n0 * d.n1 * d.n2;
+    const unsigned eg = (unsigned)std::min<long long>((N + 255) / 256, 152ll * 16);
+    k_apple_flags<<<eg, 256, 0, (cudaStream_t)stream>>>(d.n0, d.n1, d.n2, (2.0 * M_PI * d.nm) / d.res,
+                                                         d.use_bg_shell, d.bg_shell_width, mask, flags);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? ODT_OK : cuda_fail("apple flags", e);
+}
+
+odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real, const uint8_t *mask, void *out,
+                             void *workspace, size_t workspace_bytes, int32_t *iterations, void *stream)
+{
+    const odt_status st = check_desc(desc);
+    if (st != ODT_OK)
+        return st;
+    if (!f_real || !out || !workspace)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL device pointer");
+    const Layout L = layout_of(*desc);
+    if (workspace_bytes < L.total)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "workspace too small");
+    if ((uintptr_t)workspace % 256 || (uintptr_t)out % 8 || (uintptr_t)f_real % 4)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "misaligned pointer");
+    const odt_apple_desc &d = *desc;
+    cudaStream_t s = (cudaStream_t)stream;
+    char *ws = (char *)workspace;
+    const long long N = (long long)d.n0 * d.n1 * d.n2;
+    AP P{};
+    P.n0 = d.n0;
+    P.n1 = d.n1;
+    P.n2 = d.n2;
+    P.N = N;
+    P.tw0 = (const float2 *)(ws + L.tw0);
+    P.tw1 = (const float2 *)(ws + L.tw1);
+    P.tw2 = (const float2 *)(ws + L.tw2);
+    P.flags = (const uint8_t *)(ws + L.flags);
+    P.evlp = d.enforce_envelope != 0.0 ? (const float *)(ws + L.evlp) : nullptr;
+    P.ee = (float)d.enforce_envelope;
+    P.orig = (float2 *)(ws + L.orig);
+    P.buf = (float2 *)(ws + L.buf);
+    P.data = (float2 *)out;
+    P.freal = f_real;
+    P.state = (double *)(ws + L.state);
+    P.ctl = (AppleCtl *)(ws + L.ctl);
+    P.method = d.method;
+    P.max_iter = d.max_iter;
+    P.min_diff = (float)d.min_diff;
+    P.scale = 1.0f / (float)N;
+    P.has_mask = mask != nullptr;
+    P.hist = (unsigned int *)(ws + L.hist);
+    P.edges = (const float *)(ws + L.edges);
+    cudaError_t e;
+    // tables
+    {
+        const std::vector<float2> t0 = twiddles(d.n0), t1 = twiddles(d.n1), t2 = twiddles(d.n2);
+        if ((e = cudaMemcpyAsync(ws + L.tw0, t0.data(), t0.size() * 8, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemcpyAsync(ws + L.tw1, t1.data(), t1.size() * 8, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemcpyAsync(ws + L.tw2, t2.data(), t2.size() * 8, cudaMemcpyHostToDevice, s)))
+            return cuda_fail("apple tables", e);
+        if (P.evlp &&
+            (e = cudaMemcpyAsync(ws + L.gw, d.gauss_weights, (size_t)(2 * d.gauss_radius + 1) * 8,
+                                 cudaMemcpyHostToDevice, s)))
+            return cuda_fail("apple tables", e);
+        if ((e = cudaMemsetAsync(ws + L.ctl, 0, sizeof(AppleCtl), s)) ||
+            (e = cudaMemsetAsync(ws + L.state, 0, (size_t)(std::max(d.max_iter, 0) + 1) * 8, s)))
+            return cuda_fail("apple reset", e);
+        // the tables must reach the device before the host vectors go
+        if ((e = cudaStreamSynchronize(s)))
+            return cuda_fail("apple tables", e);
+    }
+    const unsigned eg = (unsigned)std::min<long long>((N + 255) / 256, 152ll * 16);
+    const double km = (2.0 * M_PI * d.nm) / d.res;
+    k_apple_flags<<<eg, 256, 0, s>>>(d.n0, d.n1, d.n2, km, d.use_bg_shell, d.bg_shell_width, mask,
+                                     (uint8_t *)(ws + L.flags));
+    // original spectrum: axis 2, 1 from f.real into buf, axis 0 into orig
+    if ((e = launch_x(P, 0, -1, s)) || (e = launch_s(P, 1, 0, -1, s)) || (e = launch_s(P, 0, 2, -1, s)))
+        return cuda_fail("apple spectrum", e);
+    k_apple_dec<<<1, 1, 0, s>>>(P, -1);
+    if (P.evlp) {
+        EnvGeom G{};
+        G.n0 = d.n0;
+        G.n1 = d.n1;
+        G.n2 = d.n2;
+        G.msh = std::max(d.n0, d.n1);
+        const int dsh = std::abs(d.n1 - d.n0) / 2;
+        if (d.n0 > d.n1) {
+            G.off0 = 0;
+            G.off1 = dsh;
+            G.off2 = 0;
+        } else {
+            G.off0 = dsh;
+            G.off1 = 0;
+            G.off2 = dsh;
+        }
+        const long long M = (long long)G.msh * G.msh * G.msh;
+        const unsigned mg = (unsigned)std::min<long long>((M + 255) / 256, 152ll * 16);
+        double *hp0 = (double *)(ws + L.hp0), *hp1 = (double *)(ws + L.hp1);
+        k_env_pad<<<mg, 256, 0, s>>>(G, P.orig, P.flags, hp0, (uint8_t *)(ws + L.cpad));
+        k_env_swap<<<mg, 256, 0, s>>>(G, hp0, (const uint8_t *)(ws + L.cpad), hp1, &P.ctl->nan_count);
+        unsigned int nans = 0;
+        if ((e = cudaMemcpyAsync(&nans, &P.ctl->nan_count, 4, cudaMemcpyDeviceToHost, s)) ||
+            (e = cudaStreamSynchronize(s)))
+            return cuda_fail("apple envelope", e);
+        const double *hp = hp1;
+        if (nans) {
+            int *ft = (int *)(ws + L.ft);
+            k_edt_init<<<mg, 256, 0, s>>>(M, hp1, ft);
+            const long long nl = (long long)G.msh * G.msh;
+            for (int ax = 0; ax < 3; ++ax)
+                k_edt_pass<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(G.msh, ax, ft, (int *)(ws + L.scratch));
+            k_edt_gather<<<mg, 256, 0, s>>>(M, ft, hp1, hp0);
+            hp = hp0;
+        }
+        float *g0 = (float *)(ws + L.g0), *g1 = (float *)(ws + L.g1);
+        const double *gw = (const double *)(ws + L.gw);
+        k_env_gauss<<<eg, 256, 0, s>>>(G, 0, hp, nullptr, g0, gw, d.gauss_radius);
+        k_env_gauss<<<eg, 256, 0, s>>>(G, 1, hp, g0, g1, gw, d.gauss_radius);
+        k_env_gauss<<<eg, 256, 0, s>>>(G, 2, hp, g1, (float *)(ws + L.evlp), gw, d.gauss_radius);
+        if ((e = cudaGetLastError()))
+            return cuda_fail("apple envelope", e);
+    }
+    if (d.max_iter == 0 || d.method == ODT_APPLE_SH)
+        k_apple_load<<<eg, 256, 0, s>>>(P);  // data = f.real
+    int done = 0;
+    AppleCtl host_ctl{};
+    for (int it0 = 0; it0 < d.max_iter; it0 += CHUNK) {
+        const int it1 = std::min(d.max_iter, it0 + CHUNK);
+        for (int it = it0; it < it1; ++it) {
+            if (d.method != ODT_APPLE_SH) {
+                if (it == 0 && (e = launch_x(P, 1, 0, s)))
+                    return cuda_fail("apple iteration", e);
+            } else {
+                // constraint_sh: min / max over the spillover region, the
+                // histogram, and the thresholds (host, from 100 counts)
+                AppleCtl c0{};
+                c0.minkey = ~0ull;
+                c0.maxkey = 0;
+                if ((e = cudaMemcpyAsync(&P.ctl->minkey, &c0.minkey, 16, cudaMemcpyHostToDevice, s)) ||
+                    (e = cudaMemsetAsync(P.hist, 0, HIST_BINS * 4, s)))
+                    return cuda_fail("apple sh", e);
+                k_sh_minmax<<<eg, 256, 0, s>>>(P, it);
+                unsigned long long keys[2];
+                int stop = 0;
+                if ((e = cudaMemcpyAsync(keys, &P.ctl->minkey, 16, cudaMemcpyDeviceToHost, s)) ||
+                    (e = cudaMemcpyAsync(&stop, &P.ctl->stop, 4, cudaMemcpyDeviceToHost, s)) ||
+                    (e = cudaStreamSynchronize(s)))
+                    return cuda_fail("apple sh", e);
+                if (stop != 0 && stop <= it)
+                    break;
+                float fmin = fkey_val(keys[0]), fmax = fkey_val(keys[1]);
+                float first = fmin, last = fmax;
+                if (first == last) {
+                    first = first - 0.5f;
+                    last = last + 0.5f;
+                }
+                // numpy.linspace(first, last, 101) in float32
+                float edges[HIST_BINS + 1];
+                const float delta = last - first;
+                const float step = delta / (float)HIST_BINS;
+                for (int k = 0; k <= HIST_BINS; ++k) {
+                    volatile float y = (float)k * step;
+                    edges[k] = y + first;
+                }
+                edges[HIST_BINS] = last;
+                if ((e = cudaMemcpyAsync(ws + L.edges, edges, sizeof(edges), cudaMemcpyHostToDevice, s)))
+                    return cuda_fail("apple sh", e);
+                k_sh_hist<<<eg, 256, 0, s>>>(P, it);
+                unsigned int hist[HIST_BINS];
+                if ((e = cudaMemcpyAsync(hist, P.hist, sizeof(hist), cudaMemcpyDeviceToHost, s)) ||
+                    (e = cudaStreamSynchronize(s)))
+                    return cuda_fail("apple sh", e);
+                int idx_c = 0;
+                for (int k = 1; k < HIST_BINS; ++k)
+                    if (hist[k] > hist[idx_c])
+                        idx_c = k;
+                const int idx_start = idx_c - (idx_c > 0 ? count_to_half(hist + idx_c - 1, idx_c, -1) : 0);
+                const int idx_end = idx_c + count_to_half(hist + idx_c, HIST_BINS - idx_c, 1);
+                const float de = edges[1] - edges[0];
+                const float half = de / 2.0f;
+                float th[4];
+                th[0] = edges[idx_start + 1] - half;  // lo
+                th[1] = edges[idx_end + 1] - half;    // hi
+                th[2] = fmin;
+                th[3] = fmax;
+                if ((e = cudaMemcpyAsync(&P.ctl->lo, th, 16, cudaMemcpyHostToDevice, s)))
+                    return cuda_fail("apple sh", e);
+                if ((e = launch_x(P, 3, it, s)))
+                    return cuda_fail("apple iteration", e);
+                // keep the host arrays alive until the copies ran
+                if ((e = cudaStreamSynchronize(s)))
+                    return cuda_fail("apple sh", e);
+            }
+            if ((e = launch_s(P, 1, 0, it, s)) || (e = launch_s(P, 0, 3, it, s)))
+                return cuda_fail("apple iteration", e);
+            k_apple_dec<<<1, 1, 0, s>>>(P, it);
+            if ((e = launch_s(P, 1, 1, it, s)) || (e = launch_x(P, 2, it, s)))
+                return cuda_fail("apple iteration", e);
+        }
+        if ((e = cudaMemcpyAsync(&host_ctl, P.ctl, sizeof(AppleCtl), cudaMemcpyDeviceToHost, s)) ||
+            (e = cudaStreamSynchronize(s)))
+            return cuda_fail("apple iteration", e);
+        done = host_ctl.iters;
+        if (host_ctl.stop != 0)
+            break;
+    }
+    if ((e = cudaStreamSynchronize(s)))
+        return cuda_fail("apple", e);
+    if (iterations)
+        *iterations = done;
+    return ODT_OK;
+}
+
+}  // extern "C"

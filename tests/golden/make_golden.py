@@ -25,7 +25,10 @@ Writes
                        apple__test_correct_reproduce.zip) and outputs of its
                        sinogram_as_rytov / sinogram_as_radon
 
-Parts can be chosen on the command line (backprop, sino); default all.
+  reference_apple.npz  inputs and outputs of the reference's apple.correct
+
+Parts can be chosen on the command line (backprop, sino, apple); default
+all.
 The input sinogram generator below restates the reference's test helper
 (tests/common_methods.py:63-184) so that the GPU tests can regenerate the
 same inputs without the reference tree.
@@ -58,6 +61,8 @@ def main(parts):
         make_backprop(odt)
     if "sino" in parts:
         make_sino(odt)
+    if "apple" in parts:
+        make_apple(odt)
     print("wrote fixtures to", HERE)
 
 
@@ -236,5 +241,47 @@ def make_sino(odt):
     refshim.UNWRAP_PHASE[0] = None
 
 
+def make_apple(odt):
+    """reference_apple.npz: inputs and outputs of the reference's
+    apple.correct (odtbrain/apple.py:113-263) for small volumes, run
+    unmodified through the pyFFTW stand-in (scipy.fft on complex64 data)."""
+    out = {}
+    rng = np.random.default_rng(31)
+
+    def volume(A, nx, ny):
+        s, a = gauss_sino_3d(A=A, Nx=nx, Ny=ny, max_phase=2.5,
+                             ampl_range=(0.9, 1.0))
+        # Rytov data of a phase below pi: log of the field
+        return odt.backpropagate_3d(np.log(s), a, res=2.5, nm=1.333,
+                                    padval=0, dtype=float)
+
+    vols = {"cube": volume(12, 20, 20), "rect": volume(10, 18, 12)}
+    for k, v in vols.items():
+        out["vol_" + k] = v
+
+    def add(name, vol, **kw):
+        f = vols[vol]
+        res = odt.apple.correct(f=f.copy(), **kw)
+        out[name + "__vol"] = np.array(vol)
+        jkw = {k: v for k, v in kw.items() if k != "mask"}
+        if "mask" in kw:
+            out[name + "__mask"] = kw["mask"]
+        out[name + "__kw"] = np.array(json.dumps(jkw))
+        out[name + "__out"] = np.asarray(res)
+
+    base = dict(res=2.5, nm=1.333)
+    add("nn_default", "cube", **base)
+    add("nn_noenvelope", "cube", enforce_envelope=0, **base)
+    add("nn_iter5", "cube", max_iter=5, min_diff=0.0, **base)
+    add("nn_mask", "cube", mask=rng.random(vols["cube"].shape) > 0.3, **base)
+    add("nn_shell", "cube", bg_shell_width=3, **base)
+    add("sh_default", "cube", method="sh", **base)
+    add("sh_shell", "cube", method="sh", bg_shell_width=3, max_iter=20,
+        **base)
+    add("nn_rect", "rect", **base)
+    add("nn_env50", "cube", enforce_envelope=0.5, min_diff=0.001, **base)
+    np.savez_compressed(os.path.join(HERE, "reference_apple.npz"), **out)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["backprop", "sino"])
+    main(sys.argv[1:] or ["backprop", "sino", "apple"])
