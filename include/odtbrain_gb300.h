@@ -1,10 +1,15 @@
 /*
  * odtbrain_gb300 -- C ABI of the GB300 (sm_103a) 3D filtered backpropagation.
  *
- * The library replaces the compute of two reference entry points:
+ * The library replaces the compute of the reference's 3D backpropagation:
  *
  *   odtbrain.backpropagate_3d         odtbrain/_alg3d_bpp.py:84-555
  *   odtbrain.backpropagate_3d_tilted  odtbrain/_alg3d_bppt.py:374-949
+ *
+ * (also backpropagate_2d through a ny = 1 plan), and of the steps either
+ * side of it, declared further down: odt_to_ri / opt_to_ri, the sinogram
+ * preparation sinogram_as_rytov / sinogram_as_radon, and the
+ * missing-apple-core correction apple.correct.
  *
  * The reference is pure Python (NumPy + pyFFTW + numexpr + scipy.ndimage +
  * multiprocessing); it has no foreign-function interface of its own.  The
@@ -351,9 +356,12 @@ odt_status odt_apple_workspace_size(const odt_apple_desc *desc, size_t *bytes);
 /* Voxel flags of the correction (device, n0*n1*n2 bytes, stream-ordered):
  * bit 0 apple core (apple_core_3d, odtbrain/apple.py:8-53), bit 1 outside
  * the inscribed ellipsoid (spillover_region, :353-363), bit 2 background
- * shell (ellipsoid_shell, :281-286, when use_bg_shell), bit 3 mask. */
+ * shell (ellipsoid_shell, :281-286, when use_bg_shell), bit 3 mask.
+ * workspace: odt_apple_flags_workspace_size bytes, 256-byte aligned. */
+odt_status odt_apple_flags_workspace_size(const odt_apple_desc *desc,
+                                          size_t *bytes);
 odt_status odt_apple_flags(const odt_apple_desc *desc, const uint8_t *mask,
-                           uint8_t *flags, void *stream);
+                           uint8_t *flags, void *workspace, void *stream);
 odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real,
                              const uint8_t *mask, void *out, void *workspace,
                              size_t workspace_bytes, int32_t *iterations,

@@ -52,6 +52,7 @@ EXPORTED_SYMBOLS = (
     "odt_apple_workspace_size",
     "odt_apple_correct",
     "odt_apple_flags",
+    "odt_apple_flags_workspace_size",
     "odt_status_string",
     "odt_last_error",
 )
@@ -213,7 +214,9 @@ def lib():
             ad, ctypes.POINTER(ctypes.c_uint64)]
         L.odt_apple_correct.argtypes = [ad, vp, vp, vp, vp, ctypes.c_uint64,
                                         ctypes.POINTER(ctypes.c_int32), vp]
-        L.odt_apple_flags.argtypes = [ad, vp, vp, vp]
+        L.odt_apple_flags.argtypes = [ad, vp, vp, vp, vp]
+        L.odt_apple_flags_workspace_size.argtypes = [
+            ad, ctypes.POINTER(ctypes.c_uint64)]
         i32 = ctypes.c_int32
         L.odt_mlp_gain_forward.argtypes = [ctypes.POINTER(MlpParams), i32,
                                            i32, i32, vp, vp, i32, vp, vp]
@@ -233,7 +236,8 @@ def lib():
                      "odt_opt_to_ri", "odt_sino_workspace_size",
                      "odt_sino_prepare", "odt_sino_launch_count",
                      "odt_sino_read_status", "odt_apple_workspace_size",
-                     "odt_apple_correct", "odt_apple_flags"):
+                     "odt_apple_correct", "odt_apple_flags",
+                     "odt_apple_flags_workspace_size"):
             getattr(L, name).restype = ctypes.c_int
         L.odt_status_string.argtypes = [ctypes.c_int]
         L.odt_status_string.restype = ctypes.c_char_p

@@ -60,12 +60,18 @@ def _flags(shape, res=1.0, nm=1.0, bg_shell_width=None, device=None):
         raise ValueError("`shape[0]` and `shape[2]` must be identical!")
     dev = device or torch.device("cuda", torch.cuda.current_device())
     d = _desc(shape, res, nm, bg_shell_width=bg_shell_width)
+    L = _native.lib()
     with torch.cuda.device(dev):
         fl = torch.empty(tuple(int(v) for v in shape), dtype=torch.uint8,
                          device=dev)
+        nb = ctypes.c_uint64()
+        _native.check(L.odt_apple_flags_workspace_size(ctypes.byref(d),
+                                                       ctypes.byref(nb)))
+        ws = torch.empty(nb.value, dtype=torch.uint8, device=dev)
         stream = torch.cuda.current_stream(dev)
-        _native.check(_native.lib().odt_apple_flags(
+        _native.check(L.odt_apple_flags(
             ctypes.byref(d), None, ctypes.c_void_p(fl.data_ptr()),
+            ctypes.c_void_p(ws.data_ptr()),
             ctypes.c_void_p(stream.cuda_stream)))
         return fl.cpu().numpy()
 

@@ -322,6 +322,19 @@ __global__ void k_apple_load(AP P)
 }
 
 // ---- voxel flags (FP64, the reference's formulas and operation order) ----
+// The per-voxel formulas separate: per axis the fftfreq value, its square,
+// k = 2 pi f and the ellipsoid terms ((i - c) / (c - shell))^2; per (i0, i2)
+// sqrt(max(2 km kxz - kxz^2, 0)) with kxz = 2 pi sqrt(fx^2 + fz^2).  Every
+// value is the one NumPy computes (same operations, same order), so the
+// flags match the reference bit for bit.
+struct FlagTables {
+    double *sq[3];     // f^2 per axis
+    double *ky;        // 2 pi f, axis 1
+    double *eo[3];     // outer ellipsoid term per axis (shell 0)
+    double *ei[3];     // inner ellipsoid term per axis (shell width)
+    double *sroot;     // [n0 * n2]
+};
+
 __device__ __forceinline__ double fftfreq(int k, int n)
 {
     // numpy.fft.fftfreq: integer frequency times 1.0 / n
@@ -329,17 +342,40 @@ __device__ __forceinline__ double fftfreq(int k, int n)
     return __dmul_rn((double)kk, __ddiv_rn(1.0, (double)n));
 }
 
-__device__ __forceinline__ bool outside_ellipsoid(int i0, int i1, int i2, int n0, int n1, int n2, double shell)
+__device__ __forceinline__ double ell_term(int i, int n, double shell)
 {
-    const double cx = n0 / 2.0, cy = n1 / 2.0, cz = n2 / 2.0;
-    const double a = __ddiv_rn(__dsub_rn((double)i0, cx), __dsub_rn(cx, shell));
-    const double b = __ddiv_rn(__dsub_rn((double)i1, cy), __dsub_rn(cy, shell));
-    const double c = __ddiv_rn(__dsub_rn((double)i2, cz), __dsub_rn(cz, shell));
-    return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c)) > 1.0;
+    const double c = n / 2.0;
+    const double a = __ddiv_rn(__dsub_rn((double)i, c), __dsub_rn(c, shell));
+    return __dmul_rn(a, a);
 }
 
-__global__ void k_apple_flags(int n0, int n1, int n2, double km, int use_shell, double shell_width,
-                              const uint8_t *mask, uint8_t *flags)
+__global__ void k_apple_tables(int n0, int n1, int n2, double km, double shell_width, FlagTables T)
+{
+    const double twopi = 6.283185307179586;
+    const int n[3] = {n0, n1, n2};
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int ax = 0; ax < 3; ++ax)
+        if (t < n[ax]) {
+            const double f = fftfreq(t, n[ax]);
+            T.sq[ax][t] = __dmul_rn(f, f);
+            if (ax == 1)
+                T.ky[t] = __dmul_rn(twopi, f);
+            T.eo[ax][t] = ell_term(t, n[ax], 0.0);
+            T.ei[ax][t] = ell_term(t, n[ax], shell_width);
+        }
+    for (long long q = t; q < (long long)n0 * n2; q += (long long)gridDim.x * blockDim.x) {
+        const int i0 = (int)(q / n2), i2 = (int)(q % n2);
+        const double fx = fftfreq(i0, n0), fz = fftfreq(i2, n2);
+        const double kxz = __dmul_rn(twopi, sqrt(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fz, fz))));
+        double root = __dsub_rn(__dmul_rn(__dmul_rn(2.0, km), kxz), __dmul_rn(kxz, kxz));
+        if (root < 0.0)
+            root = 0.0;
+        T.sroot[q] = sqrt(root);
+    }
+}
+
+__global__ void k_apple_flags(int n0, int n1, int n2, double km, int use_shell, FlagTables T, const uint8_t *mask,
+                              uint8_t *flags)
 {
     const long long N = (long long)n0 * n1 * n2;
     const double twopi = 6.283185307179586;
@@ -349,27 +385,53 @@ __global__ void k_apple_flags(int n0, int n1, int n2, double km, int use_shell, 
         const int i0 = (int)(v / ((long long)n1 * n2));
         const int i1 = (int)((v / n2) % n1);
         const int i2 = (int)(v % n2);
-        const double fx = fftfreq(i0, n0), fy = fftfreq(i1, n1), fz = fftfreq(i2, n2);
-        const double ky = __dmul_rn(twopi, fy);
-        const double kxz = __dmul_rn(twopi, sqrt(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fz, fz))));
-        const double kr =
-            __dmul_rn(twopi, sqrt(__dadd_rn(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy)), __dmul_rn(fz, fz))));
-        double root = __dsub_rn(__dmul_rn(__dmul_rn(2.0, km), kxz), __dmul_rn(kxz, kxz));
-        if (root < 0.0)
-            root = 0.0;
-        bool core = fabs(ky) > sqrt(root);
+        bool core = fabs(T.ky[i1]) > T.sroot[(long long)i0 * n2 + i2];
+        const double kr = __dmul_rn(twopi, sqrt(__dadd_rn(__dadd_rn(T.sq[0][i0], T.sq[1][i1]), T.sq[2][i2])));
         if (kr > sqrt2km)
             core = false;
         uint8_t f = core ? F_CORE : 0;
-        if (outside_ellipsoid(i0, i1, i2, n0, n1, n2, 0.0))
+        const bool outer = __dadd_rn(__dadd_rn(T.eo[0][i0], T.eo[1][i1]), T.eo[2][i2]) > 1.0;
+        if (outer)
             f |= F_SPOV;
-        if (use_shell && (outside_ellipsoid(i0, i1, i2, n0, n1, n2, 0.0) !=
-                          outside_ellipsoid(i0, i1, i2, n0, n1, n2, shell_width)))
+        if (use_shell && outer != (__dadd_rn(__dadd_rn(T.ei[0][i0], T.ei[1][i1]), T.ei[2][i2]) > 1.0))
             f |= F_SHELL;
         if (mask && mask[v])
             f |= F_MASK;
         flags[v] = f;
     }
+}
+
+// Tables in a scratch block of flag_table_bytes() bytes; then the flags.
+size_t flag_table_bytes(int n0, int n1, int n2)
+{
+    return (size_t)(3 * (n0 + n1 + n2) + n1 + (long long)n0 * n2 + 8) * 8;
+}
+
+cudaError_t compute_flags(int n0, int n1, int n2, double km, int use_shell, double shell_width, const uint8_t *mask,
+                          uint8_t *flags, double *tab, cudaStream_t s)
+{
+    FlagTables T;
+    double *p = tab;
+    const int n[3] = {n0, n1, n2};
+    for (int ax = 0; ax < 3; ++ax) {
+        T.sq[ax] = p;
+        p += n[ax];
+        T.eo[ax] = p;
+        p += n[ax];
+        T.ei[ax] = p;
+        p += n[ax];
+    }
+    T.ky = p;
+    p += n1;
+    T.sroot = p;
+    const long long q = (long long)n0 * n2;
+    const int mx = std::max(n0, std::max(n1, n2));
+    const unsigned tg = (unsigned)std::max<long long>((mx + 255) / 256, std::min<long long>((q + 255) / 256, 1024));
+    k_apple_tables<<<tg, 256, 0, s>>>(n0, n1, n2, km, shell_width, T);
+    const long long N = (long long)n0 * n1 * n2;
+    const unsigned eg = (unsigned)std::min<long long>((N + 255) / 256, 152ll * 16);
+    k_apple_flags<<<eg, 256, 0, s>>>(n0, n1, n2, km, use_shell, T, mask, flags);
+    return cudaGetLastError();
 }
 
 // ---- envelope --------------------------------------------------------------
@@ -691,8 +753,8 @@ cudaError_t launch_s(const AP &P, int axis, int mode, int it, cudaStream_t s)
 }
 
 struct Layout {
-    size_t ctl, state, hist, edges, tw0, tw1, tw2, gw, flags, buf, orig, evlp, hp0, hp1, cpad, ft, scratch, g0, g1,
-        total;
+    size_t ctl, state, hist, edges, tw0, tw1, tw2, gw, ftab, flags, buf, orig, evlp, hp0, hp1, cpad, ft, scratch, g0,
+        g1, total;
 };
 
 Layout layout_of(const odt_apple_desc &d)
@@ -715,6 +777,7 @@ Layout layout_of(const odt_apple_desc &d)
     L.tw1 = take((size_t)d.n1 * 8);
     L.tw2 = take((size_t)d.n2 * 8);
     L.gw = take((size_t)(2 * std::max(d.gauss_radius, 0) + 1) * 8);
+    L.ftab = take(flag_table_bytes(d.n0, d.n1, d.n2));
     L.flags = take((size_t)N);
     L.buf = take((size_t)N * 8);
     L.orig = take((size_t)N * 8);
@@ -800,20 +863,31 @@ odt_status odt_apple_workspace_size(const odt_apple_desc *desc, size_t *bytes)
     return ODT_OK;
 }
 
-odt_status odt_apple_flags(const odt_apple_desc *desc, const uint8_t *mask, uint8_t *flags, void *stream)
+odt_status odt_apple_flags(const odt_apple_desc *desc, const uint8_t *mask, uint8_t *flags, void *workspace,
+                           void *stream)
 {
     const odt_status st = check_desc(desc);
     if (st != ODT_OK)
         return st;
-    if (!flags)
+    if (!flags || !workspace)
         return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL device pointer");
+    if ((uintptr_t)workspace % 256)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "misaligned pointer");
     const odt_apple_desc &d = *desc;
-    const long long N = (long long)d.n0 * d.n1 * d.n2;
-    const unsigned eg = (unsigned)std::min<long long>((N + 255) / 256, 152ll * 16);
-    k_apple_flags<<<eg, 256, 0, (cudaStream_t)stream>>>(d.n0, d.n1, d.n2, (2.0 * M_PI * d.nm) / d.res,
-                                                         d.use_bg_shell, d.bg_shell_width, mask, flags);
-    const cudaError_t e = cudaGetLastError();
+    const cudaError_t e = compute_flags(d.n0, d.n1, d.n2, (2.0 * M_PI * d.nm) / d.res, d.use_bg_shell,
+                                        d.bg_shell_width, mask, flags, (double *)workspace, (cudaStream_t)stream);
     return e == cudaSuccess ? ODT_OK : cuda_fail("apple flags", e);
+}
+
+odt_status odt_apple_flags_workspace_size(const odt_apple_desc *desc, size_t *bytes)
+{
+    const odt_status st = check_desc(desc);
+    if (st != ODT_OK)
+        return st;
+    if (!bytes)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL output pointer");
+    *bytes = flag_table_bytes(desc->n0, desc->n1, desc->n2);
+    return ODT_OK;
 }
 
 odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real, const uint8_t *mask, void *out,
@@ -878,8 +952,9 @@ odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real, co
     }
     const unsigned eg = (unsigned)std::min<long long>((N + 255) / 256, 152ll * 16);
     const double km = (2.0 * M_PI * d.nm) / d.res;
-    k_apple_flags<<<eg, 256, 0, s>>>(d.n0, d.n1, d.n2, km, d.use_bg_shell, d.bg_shell_width, mask,
-                                     (uint8_t *)(ws + L.flags));
+    if ((e = compute_flags(d.n0, d.n1, d.n2, km, d.use_bg_shell, d.bg_shell_width, mask, (uint8_t *)(ws + L.flags),
+                           (double *)(ws + L.ftab), s)))
+        return cuda_fail("apple flags", e);
     // original spectrum: axis 2, 1 from f.real into buf, axis 0 into orig
     if ((e = launch_x(P, 0, -1, s)) || (e = launch_s(P, 1, 0, -1, s)) || (e = launch_s(P, 0, 2, -1, s)))
         return cuda_fail("apple spectrum", e);
