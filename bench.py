@@ -849,12 +849,21 @@ def run_apple(args):
     from odtbrain_gb300 import apple as gapple
     from odtbrain_gb300._alg3d import Backprop3D
     w = WORKLOAD
-    sino, angles = make_workload()
-    rec = Backprop3D(tuple(sino.shape), angles, w["res"], w["nm"],
-                     lD=w["lD"], padfac=w["padfac"],
-                     intp_order=w["intp_order"], input_dtype="complex64",
-                     device=dev)
-    vol = rec(torch.from_numpy(sino).to(dev))
+    if args.ncu_case:
+        # profiling case: a 128^3 volume of smooth blobs (no
+        # reconstruction before it), three iterations
+        g = torch.arange(128, device=dev, dtype=torch.float32) - 64.0
+        z, y, x = torch.meshgrid(g, g, g, indexing="ij")
+        vol = (torch.exp(-(x * x + y * y + z * z) / 800.0)
+               + 0.3 * torch.exp(-((x - 20) ** 2 + y * y + z * z) / 60.0)
+               ).to(torch.complex64)
+    else:
+        sino, angles = make_workload()
+        rec = Backprop3D(tuple(sino.shape), angles, w["res"], w["nm"],
+                         lD=w["lD"], padfac=w["padfac"],
+                         intp_order=w["intp_order"], input_dtype="complex64",
+                         device=dev)
+        vol = rec(torch.from_numpy(sino).to(dev))
     shape = tuple(vol.shape)
     N = int(np.prod(shape))
     fr = vol.real.contiguous()

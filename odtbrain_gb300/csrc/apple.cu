@@ -214,9 +214,9 @@ __global__ void __launch_bounds__(KX *L::TPL) k_apple_s(AP P, L line, int axis, 
     const long long inner = axis == 0 ? (long long)P.n1 * P.n2 : P.n2;
     const long long stride = inner;
     const long long ostride = (long long)P.n1 * P.n2;
-    const long long gpo = (inner + KX - 1) / KX;
-    const long long o = (long long)blockIdx.x / gpo;
-    const long long q0 = ((long long)blockIdx.x - o * gpo) * KX;
+    const unsigned gpo = (unsigned)((inner + KX - 1) / KX);
+    const long long o = blockIdx.x / gpo;
+    const long long q0 = (long long)(blockIdx.x - (unsigned)o * gpo) * KX;
     const int c = threadIdx.x % KX, j = threadIdx.x / KX;
     const long long q = q0 + c;
     const bool colok = q < inner;
@@ -377,14 +377,15 @@ __global__ void k_apple_tables(int n0, int n1, int n2, double km, double shell_w
 __global__ void k_apple_flags(int n0, int n1, int n2, double km, int use_shell, FlagTables T, const uint8_t *mask,
                               uint8_t *flags)
 {
-    const long long N = (long long)n0 * n1 * n2;
+    // grid (ceil(n2/32), ceil(n1/8), n0), blocks of 32 x 8
     const double twopi = 6.283185307179586;
     const double sqrt2km = __dmul_rn(1.4142135623730951, km);
-    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < N;
-         v += (long long)gridDim.x * blockDim.x) {
-        const int i0 = (int)(v / ((long long)n1 * n2));
-        const int i1 = (int)((v / n2) % n1);
-        const int i2 = (int)(v % n2);
+    {
+        const int i2 = (int)(blockIdx.x * 32 + threadIdx.x), i1 = (int)(blockIdx.y * 8 + threadIdx.y);
+        const int i0 = (int)blockIdx.z;
+        if (i2 >= n2 || i1 >= n1)
+            return;
+        const long long v = ((long long)i0 * n1 + i1) * n2 + i2;
         bool core = fabs(T.ky[i1]) > T.sroot[(long long)i0 * n2 + i2];
         const double kr = __dmul_rn(twopi, sqrt(__dadd_rn(__dadd_rn(T.sq[0][i0], T.sq[1][i1]), T.sq[2][i2])));
         if (kr > sqrt2km)
@@ -428,9 +429,8 @@ cudaError_t compute_flags(int n0, int n1, int n2, double km, int use_shell, doub
     const int mx = std::max(n0, std::max(n1, n2));
     const unsigned tg = (unsigned)std::max<long long>((mx + 255) / 256, std::min<long long>((q + 255) / 256, 1024));
     k_apple_tables<<<tg, 256, 0, s>>>(n0, n1, n2, km, shell_width, T);
-    const long long N = (long long)n0 * n1 * n2;
-    const unsigned eg = (unsigned)std::min<long long>((N + 255) / 256, 152ll * 16);
-    k_apple_flags<<<eg, 256, 0, s>>>(n0, n1, n2, km, use_shell, T, mask, flags);
+    const dim3 fg((unsigned)((n2 + 31) / 32), (unsigned)((n1 + 7) / 8), (unsigned)n0), fb(32, 8);
+    k_apple_flags<<<fg, fb, 0, s>>>(n0, n1, n2, km, use_shell, T, mask, flags);
     return cudaGetLastError();
 }
 
@@ -446,10 +446,13 @@ __device__ __forceinline__ int wrapi(int i, int n) { return ((i % n) + n) % n; }
 // cpad = fftshift(core) inside the slice
 __global__ void k_env_pad(EnvGeom G, const float2 *orig, const uint8_t *flags, double *hp, uint8_t *cpad)
 {
-    const long long M = (long long)G.msh * G.msh * G.msh;
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < M;
-         p += (long long)gridDim.x * blockDim.x) {
-        const int a = (int)(p / ((long long)G.msh * G.msh)), b = (int)((p / G.msh) % G.msh), c = (int)(p % G.msh);
+    // grid (ceil(msh/32), ceil(msh/8), msh), blocks of 32 x 8
+    {
+        const int c = (int)(blockIdx.x * 32 + threadIdx.x), b = (int)(blockIdx.y * 8 + threadIdx.y);
+        const int a = (int)blockIdx.z;
+        if (c >= G.msh || b >= G.msh)
+            return;
+        const long long p = ((long long)a * G.msh + b) * G.msh + c;
         const int i0 = a - G.off0, i1 = b - G.off1, i2 = c - G.off2;
         double h = 0.0;
         uint8_t cp = 0;
@@ -473,18 +476,18 @@ __global__ void k_env_pad(EnvGeom G, const float2 *orig, const uint8_t *flags, d
 // out = core ? in transposed over the first two axes : in; counts NaNs left
 __global__ void k_env_swap(EnvGeom G, const double *in, const uint8_t *cpad, double *out, unsigned int *nan_count)
 {
-    const long long M = (long long)G.msh * G.msh * G.msh;
+    // grid (ceil(msh/32), ceil(msh/8), msh), blocks of 32 x 8; every lane
+    // reaches the warp sum
     unsigned int cnt = 0;
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < M;
-         p += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(blockIdx.x * 32 + threadIdx.x), b = (int)(blockIdx.y * 8 + threadIdx.y);
+    const int a = (int)blockIdx.z;
+    if (c < G.msh && b < G.msh) {
+        const long long p = ((long long)a * G.msh + b) * G.msh + c;
         double h = in[p];
-        if (cpad[p]) {
-            const int a = (int)(p / ((long long)G.msh * G.msh)), b = (int)((p / G.msh) % G.msh),
-                      c = (int)(p % G.msh);
+        if (cpad[p])
             h = in[((long long)b * G.msh + a) * G.msh + c];
-        }
         out[p] = h;
-        cnt += (h != h);
+        cnt = (h != h);
     }
     for (int s = 16; s > 0; s >>= 1)
         cnt += __shfl_xor_sync(0xffffffffu, cnt, s);
@@ -604,12 +607,14 @@ __global__ void k_edt_gather(long long M, const int *ft, const double *in, doubl
 __global__ void k_env_gauss(EnvGeom G, int axis, const double *hp, const float *in, float *out, const double *w,
                             int r)
 {
-    const long long N = (long long)G.n0 * G.n1 * G.n2;
+    // grid (ceil(n2/32), ceil(n1/8), n0), blocks of 32 x 8
     const int n[3] = {G.n0, G.n1, G.n2};
     const long long st[3] = {(long long)G.n1 * G.n2, G.n2, 1};
-    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < N;
-         v += (long long)gridDim.x * blockDim.x) {
-        const int ii[3] = {(int)(v / st[0]), (int)((v / st[1]) % G.n1), (int)(v % G.n2)};
+    {
+        const int ii[3] = {(int)blockIdx.z, (int)(blockIdx.y * 8 + threadIdx.y), (int)(blockIdx.x * 32 + threadIdx.x)};
+        if (ii[1] >= G.n1 || ii[2] >= G.n2)
+            return;
+        const long long v = ((long long)ii[0] * G.n1 + ii[1]) * G.n2 + ii[2];
         auto at = [&](int k) -> double {  // input at position k along the axis
             if (k < 0 || k >= n[axis])
                 return 0.0;
@@ -978,8 +983,9 @@ odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real, co
         const long long M = (long long)G.msh * G.msh * G.msh;
         const unsigned mg = (unsigned)std::min<long long>((M + 255) / 256, 152ll * 16);
         double *hp0 = (double *)(ws + L.hp0), *hp1 = (double *)(ws + L.hp1);
-        k_env_pad<<<mg, 256, 0, s>>>(G, P.orig, P.flags, hp0, (uint8_t *)(ws + L.cpad));
-        k_env_swap<<<mg, 256, 0, s>>>(G, hp0, (const uint8_t *)(ws + L.cpad), hp1, &P.ctl->nan_count);
+        const dim3 cg((unsigned)((G.msh + 31) / 32), (unsigned)((G.msh + 7) / 8), (unsigned)G.msh), cb(32, 8);
+        k_env_pad<<<cg, cb, 0, s>>>(G, P.orig, P.flags, hp0, (uint8_t *)(ws + L.cpad));
+        k_env_swap<<<cg, cb, 0, s>>>(G, hp0, (const uint8_t *)(ws + L.cpad), hp1, &P.ctl->nan_count);
         unsigned int nans = 0;
         if ((e = cudaMemcpyAsync(&nans, &P.ctl->nan_count, 4, cudaMemcpyDeviceToHost, s)) ||
             (e = cudaStreamSynchronize(s)))
@@ -996,9 +1002,10 @@ odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real, co
         }
         float *g0 = (float *)(ws + L.g0), *g1 = (float *)(ws + L.g1);
         const double *gw = (const double *)(ws + L.gw);
-        k_env_gauss<<<eg, 256, 0, s>>>(G, 0, hp, nullptr, g0, gw, d.gauss_radius);
-        k_env_gauss<<<eg, 256, 0, s>>>(G, 1, hp, g0, g1, gw, d.gauss_radius);
-        k_env_gauss<<<eg, 256, 0, s>>>(G, 2, hp, g1, (float *)(ws + L.evlp), gw, d.gauss_radius);
+        const dim3 vg((unsigned)((d.n2 + 31) / 32), (unsigned)((d.n1 + 7) / 8), (unsigned)d.n0), vb(32, 8);
+        k_env_gauss<<<vg, vb, 0, s>>>(G, 0, hp, nullptr, g0, gw, d.gauss_radius);
+        k_env_gauss<<<vg, vb, 0, s>>>(G, 1, hp, g0, g1, gw, d.gauss_radius);
+        k_env_gauss<<<vg, vb, 0, s>>>(G, 2, hp, g1, (float *)(ws + L.evlp), gw, d.gauss_radius);
         if ((e = cudaGetLastError()))
             return cuda_fail("apple envelope", e);
     }

@@ -192,16 +192,35 @@ struct Frames {
     long long N;  // A * P
 };
 
-__device__ __forceinline__ void edge_ends(const Frames &F, long long base, uint32_t le, uint32_t &u, uint32_t &v)
+// The per-pixel kernels run on blocks of 32 x 8 pixels over a grid
+// (ceil(W/32), ceil(H/8), frames): frame, row and column come from the
+// block and thread indices (no divisions); p = (a*H + i)*W + j < 2^31.
+struct Px {
+    int a, i, j;
+    uint32_t p;
+    bool ok;
+};
+__device__ __forceinline__ Px pixel(const Frames &F)
+{
+    Px x;
+    x.j = (int)(blockIdx.x * 32 + threadIdx.x);
+    x.i = (int)(blockIdx.y * 8 + threadIdx.y);
+    x.a = (int)blockIdx.z;
+    x.ok = x.i < F.H && x.j < F.W;
+    x.p = ((uint32_t)x.a * (uint32_t)F.H + (uint32_t)x.i) * (uint32_t)F.W + (uint32_t)x.j;
+    return x;
+}
+
+__device__ __forceinline__ void edge_ends(const Frames &F, uint32_t base, uint32_t le, uint32_t &u, uint32_t &v)
 {
     const uint32_t nh = (uint32_t)F.H * (uint32_t)(F.W - 1);
     if (le < nh) {
         const uint32_t i = le / (uint32_t)(F.W - 1), j = le - i * (uint32_t)(F.W - 1);
-        u = (uint32_t)(base + (long long)i * F.W + j);
+        u = base + i * (uint32_t)F.W + j;
         v = u + 1;
     } else {
         const uint32_t l2 = le - nh;
-        u = (uint32_t)(base + l2);
+        u = base + l2;
         v = u + (uint32_t)F.W;
     }
 }
@@ -266,11 +285,12 @@ template <class T>
 __global__ void k_uw_init(const T *phi, Frames F, uint32_t seed, double *rel, unsigned long long *word,
                           unsigned long long *bw, uint32_t *be)
 {
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= F.N)
+    const Px x = pixel(F);
+    if (!x.ok)
         return;
-    const long long lp = p % F.P;
-    const int i = (int)(lp / F.W), j = (int)(lp - (long long)i * F.W);
+    const uint32_t p = x.p;
+    const int i = x.i, j = x.j;
+    const uint32_t lp = (uint32_t)i * (uint32_t)F.W + (uint32_t)j;
     double r;
     if (i >= 1 && i <= F.H - 2 && j >= 1 && j <= F.W - 2) {
         const T *c = phi + p;
@@ -298,18 +318,18 @@ __global__ void k_uw_minw(Frames F, const double *rel, const unsigned long long 
 {
     if (round > 0 && flags[round - 1] == 0)
         return;
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= F.N)
+    const Px x = pixel(F);
+    if (!x.ok)
         return;
-    const long long lp = p % F.P;
-    const int i = (int)(lp / F.W), j = (int)(lp - (long long)i * F.W);
+    const uint32_t p = x.p;
+    const int i = x.i, j = x.j;
     const uint32_t rp = par_of(word[p]);
     const double relp = rel[p];
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
         if (d == 0 ? (j + 1 >= F.W) : (i + 1 >= F.H))
             continue;
-        const long long q = p + (d == 0 ? 1 : F.W);
+        const uint32_t q = p + (d == 0 ? 1u : (uint32_t)F.W);
         const uint32_t rq = par_of(word[q]);
         if (rp == rq)
             continue;
@@ -327,23 +347,24 @@ __global__ void k_uw_mine(Frames F, const double *rel, const unsigned long long 
 {
     if (round > 0 && flags[round - 1] == 0)
         return;
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= F.N)
+    const Px x = pixel(F);
+    if (!x.ok)
         return;
-    const long long lp = p % F.P;
-    const int i = (int)(lp / F.W), j = (int)(lp - (long long)i * F.W);
+    const uint32_t p = x.p;
+    const int i = x.i, j = x.j;
+    const uint32_t lp = (uint32_t)i * (uint32_t)F.W + (uint32_t)j;
     const uint32_t rp = par_of(word[p]);
     const double relp = rel[p];
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
         if (d == 0 ? (j + 1 >= F.W) : (i + 1 >= F.H))
             continue;
-        const long long q = p + (d == 0 ? 1 : F.W);
+        const uint32_t q = p + (d == 0 ? 1u : (uint32_t)F.W);
         const uint32_t rq = par_of(word[q]);
         if (rp == rq)
             continue;
         const unsigned long long wb = dbits(__dadd_rn(relp, rel[q]));
-        const uint32_t le = d == 0 ? (uint32_t)(i * (F.W - 1) + j) : (uint32_t)(F.H * (F.W - 1) + lp);
+        const uint32_t le = d == 0 ? (uint32_t)(i * (F.W - 1) + j) : (uint32_t)(F.H * (F.W - 1)) + lp;
         if (wb == bw[rp])
             atomicMin(be + rp, le);
         if (wb == bw[rq])
@@ -360,18 +381,18 @@ __global__ void k_uw_hook(Frames F, const T *phi, const unsigned long long *word
 {
     if (round > 0 && flags[round - 1] == 0)
         return;
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= F.N)
+    const Px x = pixel(F);
+    if (!x.ok)
         return;
-    const uint32_t r = (uint32_t)p;
-    if (par_of(word[p]) != r)
+    const uint32_t r = x.p;
+    if (par_of(word[r]) != r)
         return;
     const uint32_t le = be[r];
     if (le == NONE32) {
         rw[r] = pack(r, 0);
         return;
     }
-    const long long base = p - p % F.P;
+    const uint32_t base = (uint32_t)x.a * (uint32_t)F.P;
     uint32_t u, v;
     edge_ends(F, base, le, u, v);
     const unsigned long long wu = word[u], wv = word[v];
@@ -396,11 +417,11 @@ __global__ void k_uw_jump(Frames F, const unsigned long long *word, unsigned lon
 {
     if (flags[round] == 0)
         return;
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= F.N)
+    const Px x = pixel(F);
+    if (!x.ok)
         return;
-    const uint32_t r = (uint32_t)p;
-    if (par_of(word[p]) != r)
+    const uint32_t r = x.p;
+    if (par_of(word[r]) != r)
         return;
     unsigned long long w = __ldcg(rw + r);
     for (int it = 0;; ++it) {
@@ -424,9 +445,10 @@ __global__ void k_uw_flatten(Frames F, unsigned long long *word, const unsigned 
 {
     if (flags[round] == 0)
         return;
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= F.N)
+    const Px x = pixel(F);
+    if (!x.ok)
         return;
+    const uint32_t p = x.p;
     const unsigned long long w = word[p];
     const unsigned long long wr = rw[par_of(w)];
     word[p] = pack(par_of(wr), off_of(w) + off_of(wr));
@@ -482,15 +504,16 @@ __global__ void __launch_bounds__(1024) k_uw_anchor(Frames F, const unsigned lon
 template <class T>
 __global__ void k_uw_finish(Frames F, T *phi, const unsigned long long *word, const uint32_t *fe, uint32_t *status)
 {
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= F.N)
+    const Px x = pixel(F);
+    if (!x.ok)
         return;
-    const long long a = p / F.P;
+    const uint32_t p = x.p;
+    const int a = x.a;
     const unsigned long long w = word[p];
     int32_t ka = 0;
     if (fe[a] != NONE32) {
         uint32_t u, v;
-        edge_ends(F, a * F.P, fe[a], u, v);
+        edge_ends(F, (uint32_t)a * (uint32_t)F.P, fe[a], u, v);
         const unsigned long long wa = word[u];
         if (par_of(wa) != par_of(w)) {
             atomicOr(status, STATUS_SPLIT);
@@ -596,15 +619,19 @@ __global__ void k_align(const T *phi, long long A, int ny, int nx, int three_d, 
     }
 }
 
+// grid (x, angle): the angle is blockIdx.y, no division per sample
 template <class T>
 __global__ void k_compose(const T *phi, const double *remove, long long per_angle, long long n, int rytov,
                           const C2<T> *u0arr, C2<T> u0s, C2<T> *outc, T *outr)
 {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
+    const long long a = blockIdx.y;
+    const double rm = remove ? remove[a] : 0.0;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < per_angle;
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long i = a * per_angle + k;
         T ph = phi[i];
         if (remove)
-            ph = (T)__dsub_rn((double)ph, remove[i / per_angle]);
+            ph = (T)__dsub_rn((double)ph, rm);
         if (!rytov) {
             outr[i] = ph;
             continue;
@@ -683,6 +710,8 @@ odt_status check_desc(const odt_sino_desc *d)
     const long long P = d->ny > 0 ? (long long)d->ny * d->nx : (long long)d->nx;
     if (d->num_angles > (1ll << 31) / P)
         return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "sinogram too large (more than 2^31 samples)");
+    if (d->num_angles > 65535)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "more than 65535 angles");
     if (d->align && d->ny == 0 && d->nx < 3)
         return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "alignment needs at least 3 detector columns");
     if (d->align && d->ny > 0 && d->nx < 2)
@@ -741,18 +770,18 @@ odt_status run(const odt_sino_desc &d, const void *sino, void *out, char *ws, cu
         const int rounds = num_rounds(P);
         if (cudaMemsetAsync(flags, 0, (size_t)(rounds + 1) * 4, s) != cudaSuccess)
             return launched("unwrap workspace reset");
-        const unsigned pg = (unsigned)((N + 255) / 256);
-        k_uw_init<T><<<pg, 256, 0, s>>>(phi, F, d.seed, rel, word, bw, be);
+        const dim3 pg((unsigned)((d.nx + 31) / 32), (unsigned)((d.ny + 7) / 8), (unsigned)A), pb(32, 8);
+        k_uw_init<T><<<pg, pb, 0, s>>>(phi, F, d.seed, rel, word, bw, be);
         for (int r = 0; r < rounds; ++r) {
-            k_uw_minw<<<pg, 256, 0, s>>>(F, rel, word, bw, flags, r);
-            k_uw_mine<<<pg, 256, 0, s>>>(F, rel, word, bw, be, flags, r);
+            k_uw_minw<<<pg, pb, 0, s>>>(F, rel, word, bw, flags, r);
+            k_uw_mine<<<pg, pb, 0, s>>>(F, rel, word, bw, be, flags, r);
             if (r == 0)
                 k_uw_anchor<<<(unsigned)A, 1024, 0, s>>>(F, bw, be, fe);
-            k_uw_hook<T><<<pg, 256, 0, s>>>(F, phi, word, be, rw, flags, r);
-            k_uw_jump<<<pg, 256, 0, s>>>(F, word, rw, flags, r, status);
-            k_uw_flatten<<<pg, 256, 0, s>>>(F, word, rw, bw, be, flags, r);
+            k_uw_hook<T><<<pg, pb, 0, s>>>(F, phi, word, be, rw, flags, r);
+            k_uw_jump<<<pg, pb, 0, s>>>(F, word, rw, flags, r, status);
+            k_uw_flatten<<<pg, pb, 0, s>>>(F, word, rw, bw, be, flags, r);
         }
-        k_uw_finish<T><<<pg, 256, 0, s>>>(F, phi, word, fe, status);
+        k_uw_finish<T><<<pg, pb, 0, s>>>(F, phi, word, fe, status);
     }
     double *remove = nullptr;
     if (d.align) {
@@ -765,7 +794,8 @@ odt_status run(const odt_sino_desc &d, const void *sino, void *out, char *ws, cu
         k_align<T><<<1, 256, 0, s>>>(phi, A, d.ny, d.nx, three_d ? 1 : 0, minkey, nan_seen,
                                      (double *)(ws + L.steps), remove);
     }
-    k_compose<T><<<eg, 256, 0, s>>>(phi, remove, P, N, rytov ? 1 : 0, u0arr, u0s, outc, outr);
+    const dim3 cg((unsigned)std::min<long long>((P + 255) / 256, 64), (unsigned)A);
+    k_compose<T><<<cg, 256, 0, s>>>(phi, remove, P, N, rytov ? 1 : 0, u0arr, u0s, outc, outr);
     return launched("sinogram preparation");
 }
 
