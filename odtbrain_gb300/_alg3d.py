@@ -29,7 +29,7 @@ from . import _native
 ncores = mp.cpu_count()
 
 # workspace the plan may use; save_memory trades batch size for memory
-_WS_DEFAULT = 8 << 30
+_WS_DEFAULT = 16 << 30
 _WS_SAVE_MEMORY = 1 << 30
 
 _PLAN_CACHE = collections.OrderedDict()
