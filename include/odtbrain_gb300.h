@@ -84,7 +84,7 @@ typedef struct odt_bpp3d_desc {
     const double *filter;
     const double *kz_phase;
     uint64_t workspace_limit;    /* bytes of scratch the plan may use; 0 =
-                                    library default                         */
+                                    library default (16 GiB)                */
     /* Position of plane p along the propagation axis: z_p = p - nz/2 +
      * z_shift.  0 for the 3D functions (_alg3d_bpp.py:419-437); 0.5 for the
      * 2D algorithm run as ny = 1 (rows yv = k - ln/2 + 0.5,
@@ -112,7 +112,11 @@ odt_status odt_bpp3d_angle_batch(const odt_bpp3d_plan *plan, int32_t *batch);
  *   geometry  device, A*6 (Y_AXIS) or A*12 (AFFINE3D) doubles
  *   volume    device, (nx, ny, nx) complex64, or float32 when onlyreal;
  *             fully overwritten
- *   workspace device, odt_bpp3d_workspace_size bytes, 256-byte aligned */
+ *   workspace device, odt_bpp3d_workspace_size bytes, 256-byte aligned
+ * The row stage runs on a second stream that the plan owns, forked from and
+ * joined back into `stream` with events (so the call also works inside
+ * stream capture); a plan must not be executed by two host threads at
+ * once. */
 odt_status odt_bpp3d_execute(const odt_bpp3d_plan *plan, const void *sino,
                              const double *weights, const double *geometry,
                              void *volume, void *workspace, void *stream);
