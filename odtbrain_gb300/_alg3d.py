@@ -391,13 +391,24 @@ def _device_for(uSin):
     return torch.device("cuda", torch.cuda.current_device())
 
 
+def _to_host(t):
+    """Device tensor -> NumPy array through pinned host memory (torch's
+    caching host allocator: the copy runs at full link speed, and the block
+    is reused once the returned array is dropped)."""
+    torch = _torch()
+    host = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    host.copy_(t, non_blocking=True)
+    torch.cuda.current_stream(t.device).synchronize()
+    return host.numpy()
+
+
 def _finish(vol, uSin, dtype, onlyreal):
     torch = _torch()
     if _is_tensor(uSin):
         if onlyreal:
             return vol if dtype == np.float32 else vol.to(torch.float64)
         return vol if dtype == np.float32 else vol.to(torch.complex128)
-    out = vol.cpu().numpy()
+    out = _to_host(vol)
     if onlyreal:
         return out if dtype == np.float32 else out.astype(np.float64)
     return out if dtype == np.float32 else out.astype(np.complex128)

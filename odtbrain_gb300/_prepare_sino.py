@@ -27,7 +27,7 @@ import ctypes
 import numpy as np
 
 from . import _native
-from ._alg3d import _device_for, _is_tensor, _torch
+from ._alg3d import _device_for, _is_tensor, _to_host, _torch
 
 SEED = 47  # the rng the reference passes to unwrap_phase
 
@@ -208,7 +208,7 @@ def _run(kind, uSin, u0, align):
         out = prep(sino)
     if is_t:
         return out
-    return out.cpu().numpy()
+    return _to_host(out)
 
 
 def _real_inplace(kind, phase, align):

@@ -16,7 +16,7 @@ import ctypes
 import numpy as np
 
 from . import _native
-from ._alg3d import _device_for, _is_tensor, _torch
+from ._alg3d import _device_for, _is_tensor, _to_host, _torch
 
 _CODES = {"float32": _native.ODT_DATA_F32, "float64": _native.ODT_DATA_F64,
           "complex64": _native.ODT_DATA_C64,
@@ -52,7 +52,7 @@ def _apply(fn_name, f, res, nm):
             t.numel(), code, float(res), float(nm),
             ctypes.c_void_p(stream.cuda_stream)))
     if host is not None:
-        return out.cpu().numpy()
+        return _to_host(out)
     return out
 
 

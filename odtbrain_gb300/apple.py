@@ -17,7 +17,7 @@ import ctypes
 import numpy as np
 
 from . import _native
-from ._alg3d import _device_for, _is_tensor, _torch
+from ._alg3d import _device_for, _is_tensor, _to_host, _torch
 
 _METHODS = {"nn": _native.ODT_APPLE_NN, "sh": _native.ODT_APPLE_SH}
 
@@ -172,4 +172,4 @@ def correct(f, res, nm, method="nn", mask=None, bg_shell_width=None,
             count.value += 1 + iters.value + (max_iter - iters.value)
     if is_t:
         return out
-    return out.cpu().numpy()
+    return _to_host(out)
