@@ -264,9 +264,12 @@ def check(status):
 
 
 class Plan:
-    """Owns an ``odt_bpp3d_plan``."""
+    """Owns an ``odt_bpp3d_plan``.  A plan's executions fork onto the plan's
+    own second stream, so enqueueing them is serialised per plan (the C ABI
+    forbids concurrent execution of one plan from several host threads)."""
 
     def __init__(self, desc):
+        self._lock = threading.Lock()
         L = lib()
         handle = ctypes.c_void_p()
         check(L.odt_bpp3d_plan_create(ctypes.byref(desc),
@@ -284,24 +287,26 @@ class Plan:
 
     def execute(self, sino_ptr, weights_ptr, geometry_ptr, volume_ptr,
                 workspace_ptr, stream_handle):
-        check(lib().odt_bpp3d_execute(self._h, sino_ptr, weights_ptr,
-                                      geometry_ptr, volume_ptr,
-                                      workspace_ptr, stream_handle))
+        with self._lock:
+            check(lib().odt_bpp3d_execute(self._h, sino_ptr, weights_ptr,
+                                          geometry_ptr, volume_ptr,
+                                          workspace_ptr, stream_handle))
 
     def execute_timed(self, sino_ptr, weights_ptr, geometry_ptr, volume_ptr,
                       workspace_ptr, stream_handle):
         t = StageTiming()
-        check(lib().odt_bpp3d_execute_timed(
-            self._h, sino_ptr, weights_ptr, geometry_ptr, volume_ptr,
-            workspace_ptr, stream_handle, ctypes.byref(t)))
+        with self._lock:
+            check(lib().odt_bpp3d_execute_timed(
+                self._h, sino_ptr, weights_ptr, geometry_ptr, volume_ptr,
+                workspace_ptr, stream_handle, ctypes.byref(t)))
         return t.as_dict()
 
     def execute_gain(self, sino_ptr, weights_ptr, geometry_ptr, gain_ptr,
                      again_ptr, volume_ptr, workspace_ptr, stream_handle):
-        check(lib().odt_bpp3d_execute_gain(self._h, sino_ptr, weights_ptr,
-                                           geometry_ptr, gain_ptr, again_ptr,
-                                           volume_ptr, workspace_ptr,
-                                           stream_handle))
+        with self._lock:
+            check(lib().odt_bpp3d_execute_gain(
+                self._h, sino_ptr, weights_ptr, geometry_ptr, gain_ptr,
+                again_ptr, volume_ptr, workspace_ptr, stream_handle))
 
     def adjoint_workspace_bytes(self):
         ws = ctypes.c_uint64()
@@ -312,11 +317,12 @@ class Plan:
     def adjoint(self, sino_ptr, weights_ptr, geometry_ptr, gain_ptr,
                 again_ptr, vgrad_ptr, sgrad_ptr, ggrad_ptr, aggrad_ptr,
                 workspace_ptr, stream_handle):
-        check(lib().odt_bpp3d_adjoint(self._h, sino_ptr, weights_ptr,
-                                      geometry_ptr, gain_ptr, again_ptr,
-                                      vgrad_ptr, sgrad_ptr, ggrad_ptr,
-                                      aggrad_ptr, workspace_ptr,
-                                      stream_handle))
+        with self._lock:
+            check(lib().odt_bpp3d_adjoint(self._h, sino_ptr, weights_ptr,
+                                          geometry_ptr, gain_ptr, again_ptr,
+                                          vgrad_ptr, sgrad_ptr, ggrad_ptr,
+                                          aggrad_ptr, workspace_ptr,
+                                          stream_handle))
 
     def read_status(self, stream_handle):
         check(lib().odt_bpp3d_read_status(self._h, stream_handle))
