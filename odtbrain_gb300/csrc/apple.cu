@@ -603,39 +603,75 @@ __global__ void k_edt_gather(long long M, const int *ft, const double *in, doubl
 // 2, acc = x[i] w0 + sum_{j = r..1} (x[i+j] + x[i-j]) w_j in FP64, rounded
 // to float32 after each axis.  Axis 0 reads the padded cube's slice (the
 // fftshifted hull); the last axis writes ifftshift(result) (the envelope in
-// FFT order).
-__global__ void k_env_gauss(EnvGeom G, int axis, const double *hp, const float *in, float *out, const double *w,
-                            int r)
+// FFT order).  A 32 x 8 block stages its inputs as doubles in shared memory
+// (one conversion per input): for axes 0 and 1 the block covers 32 x2
+// positions and 8 consecutive positions along the filtered axis, for axis 2
+// 32 consecutive x2 positions (the filtered axis) and 8 x1 rows.
+constexpr int GAUSS_RMAX = 64;  // radius limit (sigma <= 15.9, volumes <= 1590)
+
+__global__ void __launch_bounds__(256) k_env_gauss(EnvGeom G, int axis, const double *hp, const float *in, float *out,
+                                                   const double *w, int r)
 {
-    // grid (ceil(n2/32), ceil(n1/8), n0), blocks of 32 x 8
+    extern __shared__ double gx[];  // the staged inputs with halo
     const int n[3] = {G.n0, G.n1, G.n2};
-    const long long st[3] = {(long long)G.n1 * G.n2, G.n2, 1};
-    {
-        const int ii[3] = {(int)blockIdx.z, (int)(blockIdx.y * 8 + threadIdx.y), (int)(blockIdx.x * 32 + threadIdx.x)};
-        if (ii[1] >= G.n1 || ii[2] >= G.n2)
-            return;
-        const long long v = ((long long)ii[0] * G.n1 + ii[1]) * G.n2 + ii[2];
-        auto at = [&](int k) -> double {  // input at position k along the axis
-            if (k < 0 || k >= n[axis])
-                return 0.0;
-            if (axis == 0) {
-                const long long p = ((long long)(k + G.off0) * G.msh + (ii[1] + G.off1)) * G.msh + (ii[2] + G.off2);
-                return (double)(float)hp[p];
-            }
-            return (double)in[v + (long long)(k - ii[axis]) * st[axis]];
-        };
-        const int i = ii[axis];
-        double acc = __dmul_rn(at(i), w[r]);
-        for (int j = r; j >= 1; --j)
-            acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(at(i + j), at(i - j)), w[r + j]));
-        long long o = v;
-        if (axis == 2) {  // ifftshift: out[k] = g[(k + n/2) mod n]  =>  g[i] -> out[i - n/2]
-            const int s0 = wrapi(ii[0] - G.n0 / 2, G.n0), s1 = wrapi(ii[1] - G.n1 / 2, G.n1),
-                      s2 = wrapi(ii[2] - G.n2 / 2, G.n2);
-            o = ((long long)s0 * G.n1 + s1) * G.n2 + s2;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+    int ii[3];
+    auto input = [&](int a0, int a1, int a2) -> double {
+        if (a0 < 0 || a0 >= G.n0 || a1 < 0 || a1 >= G.n1 || a2 < 0 || a2 >= G.n2)
+            return 0.0;
+        if (axis == 0)
+            return (double)(float)hp[((long long)(a0 + G.off0) * G.msh + (a1 + G.off1)) * G.msh + (a2 + G.off2)];
+        return (double)in[((long long)a0 * G.n1 + a1) * G.n2 + a2];
+    };
+    double acc;
+    if (axis < 2) {
+        // grid (ceil(n2/32), ceil(n_axis/8), n_other); smem [(8 + 2r)][32]
+        const int a2 = (int)blockIdx.x * 32 + tx;
+        const int s0 = (int)blockIdx.y * 8 - r;  // first staged position along the axis
+        const int other = (int)blockIdx.z;
+        const int rows = 8 + 2 * r;
+        for (int t = tid; t < rows * 32; t += 256) {
+            const int k = s0 + t / 32, c = (int)blockIdx.x * 32 + (t & 31);
+            gx[t] = axis == 0 ? input(k, other, c) : input(other, k, c);
         }
-        out[o] = (float)acc;
+        __syncthreads();
+        const int k = (int)blockIdx.y * 8 + ty;
+        if (k >= n[axis] || a2 >= G.n2)
+            return;
+        ii[axis] = k;
+        ii[axis == 0 ? 1 : 0] = other;
+        ii[2] = a2;
+        const double *col = gx + (ty + r) * 32 + tx;
+        acc = __dmul_rn(col[0], w[r]);
+        for (int j = r; j >= 1; --j)
+            acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(col[j * 32], col[-j * 32]), w[r + j]));
+    } else {
+        // grid (ceil(n2/32), ceil(n1/8), n0); smem [8][32 + 2r]
+        const int wdt = 32 + 2 * r;
+        const int s2 = (int)blockIdx.x * 32 - r;
+        for (int t = tid; t < 8 * wdt; t += 256) {
+            const int row = t / wdt, c = t - row * wdt;
+            gx[t] = input((int)blockIdx.z, (int)blockIdx.y * 8 + row, s2 + c);
+        }
+        __syncthreads();
+        const int a1 = (int)blockIdx.y * 8 + ty, a2 = (int)blockIdx.x * 32 + tx;
+        if (a1 >= G.n1 || a2 >= G.n2)
+            return;
+        ii[0] = (int)blockIdx.z;
+        ii[1] = a1;
+        ii[2] = a2;
+        const double *row = gx + ty * wdt + tx + r;
+        acc = __dmul_rn(row[0], w[r]);
+        for (int j = r; j >= 1; --j)
+            acc = __dadd_rn(acc, __dmul_rn(__dadd_rn(row[j], row[-j]), w[r + j]));
     }
+    long long o = ((long long)ii[0] * G.n1 + ii[1]) * G.n2 + ii[2];
+    if (axis == 2) {  // ifftshift: out[k] = g[(k + n/2) mod n]  =>  g[i] -> out[i - n/2]
+        const int s0 = wrapi(ii[0] - G.n0 / 2, G.n0), s1 = wrapi(ii[1] - G.n1 / 2, G.n1),
+                  s2 = wrapi(ii[2] - G.n2 / 2, G.n2);
+        o = ((long long)s0 * G.n1 + s1) * G.n2 + s2;
+    }
+    out[o] = (float)acc;
 }
 
 // ---- method "sh": min / max over the spillover (and shell) voxels and the
@@ -820,6 +856,8 @@ odt_status check_desc(const odt_apple_desc *d)
         return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "max_iter must not be negative");
     if (d->enforce_envelope != 0.0 && (d->gauss_radius < 0 || !d->gauss_weights))
         return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "envelope needs the Gaussian weights");
+    if (d->enforce_envelope != 0.0 && d->gauss_radius > GAUSS_RMAX)
+        return (odt_status)set_error(ODT_ERR_UNSUPPORTED, "envelope Gaussian radius above 64 (volume axes above 1590)");
     if ((long long)d->n0 * d->n1 * d->n2 >= (1ll << 31))
         return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "volume too large (2^31 voxels or more)");
     return ODT_OK;
@@ -1002,10 +1040,17 @@ odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real, co
         }
         float *g0 = (float *)(ws + L.g0), *g1 = (float *)(ws + L.g1);
         const double *gw = (const double *)(ws + L.gw);
-        const dim3 vg((unsigned)((d.n2 + 31) / 32), (unsigned)((d.n1 + 7) / 8), (unsigned)d.n0), vb(32, 8);
-        k_env_gauss<<<vg, vb, 0, s>>>(G, 0, hp, nullptr, g0, gw, d.gauss_radius);
-        k_env_gauss<<<vg, vb, 0, s>>>(G, 1, hp, g0, g1, gw, d.gauss_radius);
-        k_env_gauss<<<vg, vb, 0, s>>>(G, 2, hp, g1, (float *)(ws + L.evlp), gw, d.gauss_radius);
+        const int gr = d.gauss_radius;
+        const dim3 vb(32, 8);
+        const dim3 g0g((unsigned)((d.n2 + 31) / 32), (unsigned)((d.n0 + 7) / 8), (unsigned)d.n1);
+        const dim3 g1g((unsigned)((d.n2 + 31) / 32), (unsigned)((d.n1 + 7) / 8), (unsigned)d.n0);
+        const size_t sm01 = (size_t)(8 + 2 * gr) * 32 * 8, sm2 = (size_t)8 * (32 + 2 * gr) * 8;
+        const size_t smx = std::max(sm01, sm2);
+        if (smx > 48 * 1024)
+            cudaFuncSetAttribute(k_env_gauss, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        k_env_gauss<<<g0g, vb, sm01, s>>>(G, 0, hp, nullptr, g0, gw, gr);
+        k_env_gauss<<<g1g, vb, sm01, s>>>(G, 1, hp, g0, g1, gw, gr);
+        k_env_gauss<<<g1g, vb, sm2, s>>>(G, 2, hp, g1, (float *)(ws + L.evlp), gw, gr);
         if ((e = cudaGetLastError()))
             return cuda_fail("apple envelope", e);
     }

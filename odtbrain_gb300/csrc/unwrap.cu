@@ -281,63 +281,151 @@ __global__ void k_unwrap_rows(T *phi, long long rows, int len)
 }
 
 // ---- 3D frames: reliability-sorted unwrapping as a Boruvka MST ------------
-template <class T>
-__global__ void k_uw_init(const T *phi, Frames F, uint32_t seed, double *rel, unsigned long long *word,
-                          unsigned long long *bw, uint32_t *be)
+// Warp-aggregated append to a list: every lane of the warp must call it (with
+// want = false where it has nothing to add); returns the slot of a wanting
+// lane.
+__device__ __forceinline__ uint32_t append_slot(uint32_t *cnt, bool want)
 {
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (mask) {
+        const int leader = __ffs(mask) - 1;
+        if (lane == leader)
+            base = atomicAdd(cnt, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+// Root of pixel p and p's turns relative to it: follow the (parent, offset)
+// words until a root (a word pointing to itself); then store the result in
+// p's word (path compression; the words of pixels only ever move to a root
+// of the same component).  Bounded: gives up with STATUS_JUMP.
+__device__ __forceinline__ uint32_t resolve(unsigned long long *word, uint32_t p, int32_t &off, uint32_t *status)
+{
+    const unsigned long long w = __ldcg(word + p);
+    uint32_t x = par_of(w);
+    int32_t acc = off_of(w);
+    int hops = 0;
+    for (;;) {
+        const unsigned long long wx = __ldcg(word + x);
+        if (par_of(wx) == x)
+            break;
+        acc += off_of(wx);
+        x = par_of(wx);
+        if (++hops > JUMP_LIMIT) {
+            atomicOr(status, STATUS_JUMP);
+            break;
+        }
+    }
+    if (hops > 0)
+        __stcg(word + p, pack(x, acc));
+    off = acc;
+    return x;
+}
+
+// Pixel reliabilities.  A 32 x 8 block stages its tile of phases (plus a
+// one-pixel halo) as doubles in shared memory and forms each wrapped first
+// difference once -- right, down, down-right and down-left of every tile
+// position -- so an interior pixel's second differences
+//   H = wrap(l - c) - wrap(c - r), V (up/down), D1 (up-left/down-right),
+//   D2 (up-right/down-left)
+// are differences of those (the same FP64 operands and operations as the
+// direct formula, so the values are identical).  Border pixels get
+// 9999999 + border_noise.
+constexpr int UI_TW = 34, UI_TH = 10;  // tile with halo
+
+template <class T>
+__global__ void __launch_bounds__(256) k_uw_init(const T *phi, Frames F, uint32_t seed, double *rel,
+                                                 unsigned long long *word, unsigned long long *bw, uint32_t *be)
+{
+    __shared__ double ph[UI_TH][UI_TW];
+    __shared__ double dR[UI_TH][UI_TW], dD[UI_TH][UI_TW], dDR[UI_TH][UI_TW], dDL[UI_TH][UI_TW];
     const Px x = pixel(F);
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    const int i0 = (int)blockIdx.y * 8 - 1, j0 = (int)blockIdx.x * 32 - 1;
+    const T *frame = phi + (size_t)x.a * (size_t)F.P;
+    for (int t = tid; t < UI_TH * UI_TW; t += 256) {
+        const int ti = t / UI_TW, tj = t - ti * UI_TW;
+        const int gi = i0 + ti, gj = j0 + tj;
+        ph[ti][tj] = (gi >= 0 && gi < F.H && gj >= 0 && gj < F.W) ? (double)frame[(size_t)gi * F.W + gj] : 0.0;
+    }
+    __syncthreads();
+    for (int t = tid; t < UI_TH * UI_TW; t += 256) {
+        const int ti = t / UI_TW, tj = t - ti * UI_TW;
+        const double c = ph[ti][tj];
+        if (tj + 1 < UI_TW)
+            dR[ti][tj] = wrapd(__dsub_rn(c, ph[ti][tj + 1]));
+        if (ti + 1 < UI_TH) {
+            dD[ti][tj] = wrapd(__dsub_rn(c, ph[ti + 1][tj]));
+            if (tj + 1 < UI_TW)
+                dDR[ti][tj] = wrapd(__dsub_rn(c, ph[ti + 1][tj + 1]));
+            if (tj >= 1)
+                dDL[ti][tj] = wrapd(__dsub_rn(c, ph[ti + 1][tj - 1]));
+        }
+    }
+    __syncthreads();
     if (!x.ok)
         return;
     const uint32_t p = x.p;
     const int i = x.i, j = x.j;
-    const uint32_t lp = (uint32_t)i * (uint32_t)F.W + (uint32_t)j;
     double r;
     if (i >= 1 && i <= F.H - 2 && j >= 1 && j <= F.W - 2) {
-        const T *c = phi + p;
-        const double pc = (double)c[0];
-        const double h = __dsub_rn(wrapd(__dsub_rn((double)c[-1], pc)), wrapd(__dsub_rn(pc, (double)c[1])));
-        const double v = __dsub_rn(wrapd(__dsub_rn((double)c[-F.W], pc)), wrapd(__dsub_rn(pc, (double)c[F.W])));
-        const double d1 =
-            __dsub_rn(wrapd(__dsub_rn((double)c[-F.W - 1], pc)), wrapd(__dsub_rn(pc, (double)c[F.W + 1])));
-        const double d2 =
-            __dsub_rn(wrapd(__dsub_rn((double)c[-F.W + 1], pc)), wrapd(__dsub_rn(pc, (double)c[F.W - 1])));
+        const int ti = threadIdx.y + 1, tj = threadIdx.x + 1;
+        const double h = __dsub_rn(dR[ti][tj - 1], dR[ti][tj]);         // wrap(l - c) - wrap(c - r)
+        const double v = __dsub_rn(dD[ti - 1][tj], dD[ti][tj]);         // wrap(u - c) - wrap(c - d)
+        const double d1 = __dsub_rn(dDR[ti - 1][tj - 1], dDR[ti][tj]);  // wrap(ul - c) - wrap(c - dr)
+        const double d2 = __dsub_rn(dDL[ti - 1][tj + 1], dDL[ti][tj]);  // wrap(ur - c) - wrap(c - dl)
         r = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(h, h), __dmul_rn(v, v)), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
     } else {
-        r = __dadd_rn(BORDER_BASE, border_noise(seed, (unsigned long long)lp));
+        r = __dadd_rn(BORDER_BASE, border_noise(seed, (unsigned long long)((uint32_t)i * (uint32_t)F.W + j)));
     }
     rel[p] = r;
-    word[p] = pack((uint32_t)p, 0);
+    word[p] = pack(p, 0);
     bw[p] = NONE64;
     be[p] = NONE32;
 }
 
 // Lightest outgoing edge weight of every component root (edges handled by
 // their pixel 1: right and down neighbours).
+// Lightest outgoing edge weight of every component root (edges handled by
+// their pixel 1: right and down neighbours).  With `elist`, the crossing
+// edges are also appended to it as (pixel 1, frame-local edge index).
 __global__ void k_uw_minw(Frames F, const double *rel, const unsigned long long *word, unsigned long long *bw,
-                          const uint32_t *flags, int round)
+                          const uint32_t *flags, int round, uint2 *elist, uint32_t *ecnt)
 {
     if (round > 0 && flags[round - 1] == 0)
         return;
     const Px x = pixel(F);
-    if (!x.ok)
-        return;
     const uint32_t p = x.p;
     const int i = x.i, j = x.j;
-    const uint32_t rp = par_of(word[p]);
-    const double relp = rel[p];
+    const uint32_t rp = x.ok ? par_of(word[p]) : 0u;
+    const double relp = x.ok ? rel[p] : 0.0;
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
-        if (d == 0 ? (j + 1 >= F.W) : (i + 1 >= F.H))
-            continue;
-        const uint32_t q = p + (d == 0 ? 1u : (uint32_t)F.W);
-        const uint32_t rq = par_of(word[q]);
-        if (rp == rq)
-            continue;
-        const unsigned long long wb = dbits(__dadd_rn(relp, rel[q]));
-        if (wb < bw[rp])
-            atomicMin(bw + rp, wb);
-        if (wb < bw[rq])
-            atomicMin(bw + rq, wb);
+        bool cross = false;
+        uint32_t le = 0;
+        if (x.ok && (d == 0 ? (j + 1 < F.W) : (i + 1 < F.H))) {
+            const uint32_t q = p + (d == 0 ? 1u : (uint32_t)F.W);
+            const uint32_t rq = par_of(word[q]);
+            if (rp != rq) {
+                cross = true;
+                le = d == 0 ? (uint32_t)(i * (F.W - 1) + j)
+                            : (uint32_t)(F.H * (F.W - 1)) + (uint32_t)i * (uint32_t)F.W + (uint32_t)j;
+                const unsigned long long wb = dbits(__dadd_rn(relp, rel[q]));
+                if (wb < bw[rp])
+                    atomicMin(bw + rp, wb);
+                if (wb < bw[rq])
+                    atomicMin(bw + rq, wb);
+            }
+        }
+        if (elist) {
+            // list entry: (pixel 1, local edge index | vertical flag)
+            const uint32_t slot = append_slot(ecnt, cross);
+            if (cross)
+                elist[slot] = make_uint2(p, d == 0 ? le : (le | 0x80000000u));
+        }
     }
 }
 
@@ -377,39 +465,44 @@ __global__ void k_uw_mine(Frames F, const double *rel, const unsigned long long 
 // relative to it); written for every root.
 template <class T>
 __global__ void k_uw_hook(Frames F, const T *phi, const unsigned long long *word, const uint32_t *be,
-                          unsigned long long *rw, uint32_t *flags, int round)
+                          unsigned long long *rw, uint32_t *flags, int round, uint32_t *rlist, uint32_t *rcnt)
 {
     if (round > 0 && flags[round - 1] == 0)
         return;
     const Px x = pixel(F);
-    if (!x.ok)
-        return;
     const uint32_t r = x.p;
-    if (par_of(word[r]) != r)
-        return;
-    const uint32_t le = be[r];
-    if (le == NONE32) {
-        rw[r] = pack(r, 0);
-        return;
+    bool keep = false;  // a root after this round with an outgoing edge left
+    if (x.ok && par_of(word[r]) == r) {
+        const uint32_t le = be[r];
+        if (le == NONE32) {
+            rw[r] = pack(r, 0);
+        } else {
+            const uint32_t base = (uint32_t)x.a * (uint32_t)F.P;
+            uint32_t u, v;
+            edge_ends(F, base, le, u, v);
+            const unsigned long long wu = word[u], wv = word[v];
+            const bool u_in_r = par_of(wu) == r;
+            const uint32_t s = u_in_r ? par_of(wv) : par_of(wu);
+            if (be[s] == le && r < s) {
+                rw[r] = pack(r, 0);
+                keep = true;
+            } else {
+                // turns: k(v) - k(u) = -e with e = +1 / -1 / 0 as
+                // phi[u] - phi[v] is below -pi / above pi / neither (the
+                // reference's find_wrap)
+                const double d = (double)phi[u] - (double)phi[v];
+                const int e = d > PI_D ? -1 : (d < -PI_D ? 1 : 0);
+                const int32_t ou = off_of(wu), ov = off_of(wv);
+                rw[r] = pack(s, u_in_r ? (e + ov - ou) : (-e + ou - ov));
+                flags[round] = 1;
+            }
+        }
     }
-    const uint32_t base = (uint32_t)x.a * (uint32_t)F.P;
-    uint32_t u, v;
-    edge_ends(F, base, le, u, v);
-    const unsigned long long wu = word[u], wv = word[v];
-    const bool u_in_r = par_of(wu) == r;
-    const uint32_t s = u_in_r ? par_of(wv) : par_of(wu);
-    if (be[s] == le && r < s) {
-        rw[r] = pack(r, 0);
-        return;
+    if (rlist) {
+        const uint32_t slot = append_slot(rcnt, keep);
+        if (keep)
+            rlist[slot] = r;
     }
-    // turns: k(v) - k(u) = -e with e = +1 / -1 / 0 as phi[u] - phi[v] is
-    // below -pi / above pi / neither (the reference's find_wrap)
-    const double d = (double)phi[u] - (double)phi[v];
-    const int e = d > PI_D ? -1 : (d < -PI_D ? 1 : 0);
-    const int32_t ou = off_of(wu), ov = off_of(wv);
-    const int32_t off = u_in_r ? (e + ov - ou) : (-e + ou - ov);
-    rw[r] = pack(s, off);
-    flags[round] = 1;
 }
 
 __global__ void k_uw_jump(Frames F, const unsigned long long *word, unsigned long long *rw, uint32_t *flags,
@@ -454,6 +547,157 @@ __global__ void k_uw_flatten(Frames F, unsigned long long *word, const unsigned 
     word[p] = pack(par_of(wr), off_of(w) + off_of(wr));
     bw[p] = NONE64;
     be[p] = NONE32;
+}
+
+// ---- rounds >= 2 on lists ---------------------------------------------------
+// From round 2 on, only the edges that crossed components in the previous
+// round and the roots that are left are visited (lists compacted every
+// round); pixel roots are found by following the (parent, offset) words,
+// which only the roots update (k_ul_update), with path compression.  Grids
+// are fixed; the kernels stride over the device-side counts.
+constexpr int UL_GRID = 152 * 8, UL_BLOCK = 256;
+
+__global__ void __launch_bounds__(UL_BLOCK) k_ul_edges_w(const double *rel, unsigned long long *word,
+                                                         unsigned long long *bw, const uint2 *ein,
+                                                         const uint32_t *ecnt_in, uint2 *eout, uint32_t *ecnt_out,
+                                                         int W, const uint32_t *flags, int round, uint32_t *status)
+{
+    if (flags[round - 1] == 0)
+        return;
+    const uint32_t n = *ecnt_in;
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+        const uint32_t k = b + threadIdx.x;
+        bool cross = false;
+        uint2 e = make_uint2(0, 0);
+        if (k < n) {
+            e = ein[k];
+            const uint32_t u = e.x;
+            const uint32_t v = u + ((e.y & 0x80000000u) ? (uint32_t)W : 1u);
+            int32_t ou, ov;
+            const uint32_t ru = resolve(word, u, ou, status), rv = resolve(word, v, ov, status);
+            if (ru != rv) {
+                cross = true;
+                const unsigned long long wb = dbits(__dadd_rn(rel[u], rel[v]));
+                if (wb < bw[ru])
+                    atomicMin(bw + ru, wb);
+                if (wb < bw[rv])
+                    atomicMin(bw + rv, wb);
+            }
+        }
+        const uint32_t slot = append_slot(ecnt_out, cross);
+        if (cross)
+            eout[slot] = e;
+    }
+}
+
+__global__ void __launch_bounds__(UL_BLOCK) k_ul_edges_e(const double *rel, unsigned long long *word,
+                                                         const unsigned long long *bw, uint32_t *be, const uint2 *el,
+                                                         const uint32_t *ecnt, int W, const uint32_t *flags,
+                                                         int round, uint32_t *status)
+{
+    if (flags[round - 1] == 0)
+        return;
+    const uint32_t n = *ecnt;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint2 e = el[k];
+        const uint32_t u = e.x;
+        const uint32_t v = u + ((e.y & 0x80000000u) ? (uint32_t)W : 1u);
+        const uint32_t le = e.y & 0x7fffffffu;
+        int32_t ou, ov;
+        const uint32_t ru = resolve(word, u, ou, status), rv = resolve(word, v, ov, status);
+        if (ru == rv)
+            continue;
+        const unsigned long long wb = dbits(__dadd_rn(rel[u], rel[v]));
+        if (wb == bw[ru])
+            atomicMin(be + ru, le);
+        if (wb == bw[rv])
+            atomicMin(be + rv, le);
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(UL_BLOCK) k_ul_hook(Frames F, const T *phi, unsigned long long *word,
+                                                      const uint32_t *be, unsigned long long *rw, const uint32_t *rin,
+                                                      const uint32_t *rcnt_in, uint32_t *rout, uint32_t *rcnt_out,
+                                                      uint32_t *flags, int round, uint32_t *status)
+{
+    if (flags[round - 1] == 0)
+        return;
+    const uint32_t n = *rcnt_in;
+    for (uint32_t b = blockIdx.x * blockDim.x; b < n; b += gridDim.x * blockDim.x) {
+        const uint32_t k = b + threadIdx.x;
+        bool keep = false;
+        uint32_t r = 0;
+        if (k < n) {
+            r = rin[k];
+            const uint32_t le = be[r];
+            if (le == NONE32) {
+                rw[r] = pack(r, 0);
+            } else {
+                const uint32_t base = r / (uint32_t)F.P * (uint32_t)F.P;
+                uint32_t u, v;
+                edge_ends(F, base, le, u, v);
+                int32_t ou, ov;
+                const uint32_t ru = resolve(word, u, ou, status), rv = resolve(word, v, ov, status);
+                const bool u_in_r = ru == r;
+                const uint32_t s = u_in_r ? rv : ru;
+                if (be[s] == le && r < s) {
+                    rw[r] = pack(r, 0);
+                    keep = true;
+                } else {
+                    const double d = (double)phi[u] - (double)phi[v];
+                    const int e = d > PI_D ? -1 : (d < -PI_D ? 1 : 0);
+                    rw[r] = pack(s, u_in_r ? (e + ov - ou) : (-e + ou - ov));
+                    flags[round] = 1;
+                }
+            }
+        }
+        const uint32_t slot = append_slot(rcnt_out, keep);
+        if (keep)
+            rout[slot] = r;
+    }
+}
+
+__global__ void __launch_bounds__(UL_BLOCK) k_ul_jump(unsigned long long *rw, const uint32_t *rl, const uint32_t *rcnt,
+                                                      const uint32_t *flags, int round, uint32_t *status)
+{
+    if (flags[round] == 0)
+        return;
+    const uint32_t n = *rcnt;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint32_t r = rl[k];
+        unsigned long long w = __ldcg(rw + r);
+        for (int it = 0;; ++it) {
+            const uint32_t pp = par_of(w);
+            if (pp == r)
+                break;
+            const unsigned long long wp = __ldcg(rw + pp);
+            if (par_of(wp) == pp)
+                break;
+            w = pack(par_of(wp), off_of(w) + off_of(wp));
+            __stcg(rw + r, w);
+            if (it >= JUMP_LIMIT) {
+                atomicOr(status, STATUS_JUMP);
+                break;
+            }
+        }
+    }
+}
+
+// the roots of this round take their new parent word; per-root minima reset
+__global__ void __launch_bounds__(UL_BLOCK) k_ul_update(unsigned long long *word, const unsigned long long *rw,
+                                                        unsigned long long *bw, uint32_t *be, const uint32_t *rl,
+                                                        const uint32_t *rcnt, const uint32_t *flags, int round)
+{
+    if (flags[round] == 0)
+        return;
+    const uint32_t n = *rcnt;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint32_t r = rl[k];
+        word[r] = rw[r];
+        bw[r] = NONE64;
+        be[r] = NONE32;
+    }
 }
 
 // First edge of each frame in (weight, index) order, whose pixel 1 starts
@@ -502,26 +746,26 @@ __global__ void __launch_bounds__(1024) k_uw_anchor(Frames F, const unsigned lon
 }
 
 template <class T>
-__global__ void k_uw_finish(Frames F, T *phi, const unsigned long long *word, const uint32_t *fe, uint32_t *status)
+__global__ void k_uw_finish(Frames F, T *phi, unsigned long long *word, const uint32_t *fe, uint32_t *status)
 {
     const Px x = pixel(F);
     if (!x.ok)
         return;
     const uint32_t p = x.p;
     const int a = x.a;
-    const unsigned long long w = word[p];
+    int32_t op;
+    const uint32_t rp = resolve(word, p, op, status);
     int32_t ka = 0;
     if (fe[a] != NONE32) {
         uint32_t u, v;
         edge_ends(F, (uint32_t)a * (uint32_t)F.P, fe[a], u, v);
-        const unsigned long long wa = word[u];
-        if (par_of(wa) != par_of(w)) {
+        const uint32_t ra = resolve(word, u, ka, status);
+        if (ra != rp) {
             atomicOr(status, STATUS_SPLIT);
             return;
         }
-        ka = off_of(wa);
     }
-    const int32_t k = off_of(w) - ka;
+    const int32_t k = op - ka;
     if (k != 0)
         phi[p] = (T)__dadd_rn((double)phi[p], __dmul_rn(TWOPI_D, (double)k));
 }
@@ -647,7 +891,7 @@ __global__ void k_compose(const T *phi, const double *remove, long long per_angl
 
 // ---------------------------------------------------------------------------
 struct Layout {
-    size_t phi, rel, word, rw, bw, be, fe, flags, status, minkey, nan, steps, remove, total;
+    size_t phi, rel, word, rw, bw, be, fe, flags, status, minkey, nan, steps, remove, elist[2], rlist[2], cnt, total;
 };
 
 int num_rounds(long long P)
@@ -686,6 +930,11 @@ Layout layout_of(const odt_sino_desc &d)
         L.bw = take((size_t)N * 8);
         L.be = take((size_t)N * 4);
         L.fe = take((size_t)A * 4);
+        for (int k = 0; k < 2; ++k) {
+            L.elist[k] = take((size_t)N * 2 * 8);
+            L.rlist[k] = take((size_t)N * 4);
+        }
+        L.cnt = take(4 * 4);
     }
     L.total = o;
     return L;
@@ -771,15 +1020,38 @@ odt_status run(const odt_sino_desc &d, const void *sino, void *out, char *ws, cu
         if (cudaMemsetAsync(flags, 0, (size_t)(rounds + 1) * 4, s) != cudaSuccess)
             return launched("unwrap workspace reset");
         const dim3 pg((unsigned)((d.nx + 31) / 32), (unsigned)((d.ny + 7) / 8), (unsigned)A), pb(32, 8);
+        uint2 *el[2] = {(uint2 *)(ws + L.elist[0]), (uint2 *)(ws + L.elist[1])};
+        uint32_t *rl[2] = {(uint32_t *)(ws + L.rlist[0]), (uint32_t *)(ws + L.rlist[1])};
+        uint32_t *ecnt = (uint32_t *)(ws + L.cnt), *rcnt = ecnt + 2;
+        if (cudaMemsetAsync(ecnt, 0, 16, s) != cudaSuccess)
+            return launched("unwrap workspace reset");
         k_uw_init<T><<<pg, pb, 0, s>>>(phi, F, d.seed, rel, word, bw, be);
-        for (int r = 0; r < rounds; ++r) {
-            k_uw_minw<<<pg, pb, 0, s>>>(F, rel, word, bw, flags, r);
+        // rounds 0 and 1 over the pixel grid; round 1 also lists the edges
+        // that cross components and the roots that stay
+        for (int r = 0; r < std::min(rounds, 2); ++r) {
+            k_uw_minw<<<pg, pb, 0, s>>>(F, rel, word, bw, flags, r, r == 1 ? el[0] : nullptr, ecnt);
             k_uw_mine<<<pg, pb, 0, s>>>(F, rel, word, bw, be, flags, r);
             if (r == 0)
                 k_uw_anchor<<<(unsigned)A, 1024, 0, s>>>(F, bw, be, fe);
-            k_uw_hook<T><<<pg, pb, 0, s>>>(F, phi, word, be, rw, flags, r);
+            k_uw_hook<T><<<pg, pb, 0, s>>>(F, phi, word, be, rw, flags, r, r == 1 ? rl[0] : nullptr, rcnt);
             k_uw_jump<<<pg, pb, 0, s>>>(F, word, rw, flags, r, status);
             k_uw_flatten<<<pg, pb, 0, s>>>(F, word, rw, bw, be, flags, r);
+        }
+        // rounds >= 2 on the lists, in and out alternating (round 2 reads
+        // the lists round 1 wrote into slot 0)
+        for (int r = 2; r < rounds; ++r) {
+            const int in = r & 1 ? 1 : 0, out = in ^ 1;
+            if (cudaMemsetAsync(ecnt + out, 0, 4, s) != cudaSuccess ||
+                cudaMemsetAsync(rcnt + out, 0, 4, s) != cudaSuccess)
+                return launched("unwrap list reset");
+            k_ul_edges_w<<<UL_GRID, UL_BLOCK, 0, s>>>(rel, word, bw, el[in], ecnt + in, el[out], ecnt + out, d.nx,
+                                                      flags, r, status);
+            k_ul_edges_e<<<UL_GRID, UL_BLOCK, 0, s>>>(rel, word, bw, be, el[out], ecnt + out, d.nx, flags, r,
+                                                      status);
+            k_ul_hook<T><<<UL_GRID, UL_BLOCK, 0, s>>>(F, phi, word, be, rw, rl[in], rcnt + in, rl[out], rcnt + out,
+                                                      flags, r, status);
+            k_ul_jump<<<UL_GRID, UL_BLOCK, 0, s>>>(rw, rl[in], rcnt + in, flags, r, status);
+            k_ul_update<<<UL_GRID, UL_BLOCK, 0, s>>>(word, rw, bw, be, rl[in], rcnt + in, flags, r);
         }
         k_uw_finish<T><<<pg, pb, 0, s>>>(F, phi, word, fe, status);
     }
