@@ -190,3 +190,81 @@ def test_plan_create_argument_checks(native_lib):
     st = native_lib.odt_bpp3d_plan_create(ctypes.byref(d), ctypes.byref(h))
     assert st == _native.ODT_ERR_UNSUPPORTED
     assert native_lib.odt_status_string(5) == b"device-side check failed"
+
+
+def _sino_desc(A=3, ny=8, nx=9, dtype=None, kind=None, align=1):
+    d = _native.SinoDesc()
+    d.num_angles, d.ny, d.nx = A, ny, nx
+    d.dtype = _native.ODT_DATA_C64 if dtype is None else dtype
+    d.kind = _native.ODT_SINO_RYTOV if kind is None else kind
+    d.align = align
+    d.seed = 47
+    d.u0_re = 1.0
+    return d
+
+
+def test_sino_descriptor_checks(native_lib):
+    """odt_sino_workspace_size validates the descriptor on the host."""
+    nb = ctypes.c_uint64()
+    ok = native_lib.odt_sino_workspace_size
+    assert ok(ctypes.byref(_sino_desc()), ctypes.byref(nb)) == _native.ODT_OK
+    three_d = nb.value
+    assert ok(ctypes.byref(_sino_desc(ny=0)), ctypes.byref(nb)) == _native.ODT_OK
+    assert 0 < nb.value < three_d  # no spanning-tree buffers for lines
+    for bad in (_sino_desc(A=0), _sino_desc(nx=0), _sino_desc(ny=-1),
+                _sino_desc(dtype=_native.ODT_DATA_F32),
+                _sino_desc(kind=7), _sino_desc(ny=0, nx=2),
+                _sino_desc(kind=_native.ODT_SINO_ALIGN),
+                _sino_desc(kind=_native.ODT_SINO_ALIGN,
+                           dtype=_native.ODT_DATA_F64, align=0),
+                _sino_desc(A=70000, ny=2, nx=2)):
+        assert ok(ctypes.byref(bad), ctypes.byref(nb)) == \
+            _native.ODT_ERR_INVALID_ARGUMENT
+    real = _sino_desc(kind=_native.ODT_SINO_UNWRAP, dtype=_native.ODT_DATA_F64)
+    assert ok(ctypes.byref(real), ctypes.byref(nb)) == _native.ODT_OK
+    n = ctypes.c_int32()
+    assert native_lib.odt_sino_launch_count(
+        ctypes.byref(_sino_desc()), ctypes.byref(n)) == _native.ODT_OK
+    assert n.value > 20
+    assert native_lib.odt_sino_prepare(
+        ctypes.byref(_sino_desc()), None, None, None, 0, None) == \
+        _native.ODT_ERR_INVALID_ARGUMENT
+
+
+def test_apple_descriptor_checks(native_lib):
+    """odt_apple_workspace_size validates the descriptor on the host."""
+    from odtbrain_gb300 import apple
+    nb = ctypes.c_uint64()
+    ws = native_lib.odt_apple_workspace_size
+    d = apple._desc((16, 12, 16), 2.1, 1.333)
+    assert ws(ctypes.byref(d), ctypes.byref(nb)) == _native.ODT_OK
+    with_env = nb.value
+    d = apple._desc((16, 12, 16), 2.1, 1.333, enforce_envelope=0)
+    assert ws(ctypes.byref(d), ctypes.byref(nb)) == _native.ODT_OK
+    assert nb.value < with_env  # no envelope buffers
+    for shape, kw, code in [
+            ((16, 12, 15), {}, _native.ODT_ERR_INVALID_ARGUMENT),
+            ((16, 12, 16), {"enforce_envelope": 1.2},
+             _native.ODT_ERR_INVALID_ARGUMENT),
+            ((16, 12, 16), {"max_iter": -1}, _native.ODT_ERR_INVALID_ARGUMENT),
+            ((1500, 8, 1500), {}, _native.ODT_ERR_UNSUPPORTED)]:
+        d = apple._desc(shape, 2.1, 1.333, **kw)
+        assert ws(ctypes.byref(d), ctypes.byref(nb)) == code, (shape, kw)
+    # another method name: no constraint (the reference's loop then runs
+    # without one)
+    d = apple._desc((16, 12, 16), 2.1, 1.333, method="other")
+    assert d.method == _native.ODT_APPLE_NONE
+    assert ws(ctypes.byref(d), ctypes.byref(nb)) == _native.ODT_OK
+
+
+def test_apple_gauss_weights_match_scipy():
+    """The 1D Gaussian handed to the envelope kernel is scipy's."""
+    import scipy.ndimage as ndi
+    from odtbrain_gb300 import apple
+    for shape in ((10, 10, 10), (64, 40, 64), (256, 256, 256)):
+        w, r = apple._gauss_weights(shape)
+        sigma = max(shape) / 100
+        x = np.zeros(2 * r + 9)
+        x[r + 4] = 1.0
+        ref = ndi.gaussian_filter1d(x, sigma, mode="constant", truncate=4.0)
+        np.testing.assert_array_equal(ref[4:4 + 2 * r + 1], w[::-1])
