@@ -281,7 +281,6 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     const int n = line.size();  // lNx
     const int ls = xslots<false>(n);
     float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
-    float2 *edge = tw + n;  // [LPC][4]
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
     // lines of whole warps sync on named barrier 1 + l
@@ -332,19 +331,27 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
         line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
         float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
         if (pf) {
-            const int e0 = (padxl - 1 + n) % n, e1 = (padxl + 1) % n;
-            const int e2 = (padxl + nx - 2 + n) % n, e3 = (padxl + nx) % n;
-            float2 t;
-            if (held<L>(v, j, e0, t)) edge[l * 4 + 0] = t;
-            if (held<L>(v, j, e1, t)) edge[l * 4 + 1] = t;
-            if (held<L>(v, j, e2, t)) edge[l * 4 + 2] = t;
-            if (held<L>(v, j, e3, t)) edge[l * 4 + 3] = t;
+            // the line's samples at x0-1, x0+1, x1-1, x1+1 (periodic): every
+            // thread writes its values to the exchange buffer the FFT's last
+            // exchange did not use (its reads ended before that exchange's
+            // barrier), then each thread reads the four
+            // (plain positions 0..n-1: within the line's slots for every
+            // line type, and conflict-free for these stride-1 writes)
+            float2 *sc = (flip ? buf1 : buf0) + l * ls;
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int x = j + r * L::TPL;
+                if (x < n)
+                    sc[x] = v[r];
+            }
             if (bar > 0)
                 line_sync(bar, L::TPL);
             else
                 __syncthreads();
-            const float2 d0 = edge[l * 4 + 0] - edge[l * 4 + 1];
-            const float2 d1 = edge[l * 4 + 3] - edge[l * 4 + 2];
+            const int e0 = (padxl - 1 + n) % n, e1 = (padxl + 1) % n;
+            const int e2 = (padxl + nx - 2 + n) % n, e3 = (padxl + nx) % n;
+            const float2 d0 = sc[e0] - sc[e1];
+            const float2 d1 = sc[e3] - sc[e2];
             Acoef = make_float2(P.bx_ca * d0.x + P.bx_cb * d1.x, P.bx_ca * d0.y + P.bx_cb * d1.y);
             Bcoef = make_float2(P.bx_ca * d1.x + P.bx_cb * d0.x, P.bx_ca * d1.y + P.bx_cb * d0.y);
         }
