@@ -336,6 +336,82 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _reference_line(args, metric, unit, value, step_s, workload, sample,
+                    cores):
+    return {
+        "impl": "reference", "metric": metric, "value": value, "unit": unit,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": step_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic", "config": {"workload": workload,
+                                        "sample": sample},
+        "cpu_baseline": {"value": value, "unit": unit, "cores": cores,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}
+
+
+def run_reference_rytov(args):
+    """--impl reference for the sinogram preparation: the oracle port of
+    the reference's sinogram_as_rytov (Kruskal unwrapping per frame, NumPy
+    alignment) on a bounded sample of two frames per step."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    from oracle import unwrap_oracle
+    from sino_gen import ellipsoid_phantom_sinogram
+    w = WORKLOAD
+    ryt, _ = ellipsoid_phantom_sinogram(
+        w["n"], w["A"], seed=w["seed"], count_range=w["count_range"],
+        semi_range=w["semi_range"], res=w["res"], nm=w["nm"])
+    field = np.exp(ryt)
+    times = []
+    k = 2
+    for it in range(args.warmup + args.steps):
+        a0 = (it * k) % (w["A"] - k)
+        t0 = time.perf_counter()
+        unwrap_oracle.sinogram_as_rytov(field[a0:a0 + k], align=True)
+        if it >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    step = statistics.mean(times)
+    samples = k * field[0].size
+    print(json.dumps(_reference_line(
+        args, "sinogram_as_rytov samples/s on 1 GB300 (3D frames, FP32)",
+        "sinogram samples/s", samples / step, step, w["name"],
+        "2 of the 200 frames per step (oracle port of the reference: "
+        "Kruskal unwrapping, NumPy alignment), FP64", 1)), flush=True)
+
+
+def run_reference_apple(args):
+    """--impl reference for the apple-core correction: the oracle port of
+    the reference's apple.correct (NumPy + scipy.fft, single precision like
+    pyFFTW) on a 256^3 volume, two iterations per step (setup and envelope
+    included in the first)."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    from oracle import apple_oracle
+    w = WORKLOAD
+    n = w["n"]
+    g = np.arange(n) - n / 2
+    z, y, x = np.meshgrid(g, g, g, indexing="ij", sparse=True)
+    vol = (np.exp(-(x * x + y * y + z * z) / (0.1 * n * n))
+           + 0.3 * np.exp(-((x - 0.2 * n) ** 2 + y * y + z * z) / 60.0))
+    k = 2
+    times = []
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        apple_oracle.correct(vol, w["res"], w["nm"], max_iter=k,
+                             min_diff=0.0)
+        if it >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    step = statistics.mean(times)
+    print(json.dumps(_reference_line(
+        args, "apple.correct voxel-iterations/s on 1 GB300 (FP32 FFTs)",
+        "voxel-iterations/s", float(n) ** 3 * k / step, step, w["name"],
+        "2 iterations of a %d^3 correction per step (oracle port of the "
+        "reference: NumPy + scipy.fft), setup and envelope included" % n,
+        1)), flush=True)
+
+
 # --------------------------------------------------------------- GPU side
 def run_ours(args):
     import torch
@@ -976,17 +1052,12 @@ def main():
     WORKLOAD_NAME = WORKLOAD["name"]
     if args.config == "apple":
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable":
-                              "the reference's apple.correct needs pyFFTW, "
-                              "which is not installed"}))
+            run_reference_apple(args)
         else:
             run_apple(args)
     elif args.config == "rytov":
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable":
-                              "the reference's 3D sinogram_as_rytov calls "
-                              "skimage.restoration.unwrap_phase; "
-                              "scikit-image is not installed"}))
+            run_reference_rytov(args)
         else:
             run_rytov(args)
     elif args.config in ("c4", "c5"):
