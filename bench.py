@@ -20,7 +20,7 @@ e2e     the same metric through the public API ``backpropagate_3d`` with a
         pinned host sinogram in and a host volume out (H2D + D2H inside)
 roofline  the dominant kernel stage, timed live with CUDA events around
         each of its launches, against MEASURED_PEAKS.json's HBM bandwidth;
-        for the FFT stages (FP32-arithmetic bound, L2-resident data) also
+        for the FFT stages (FP32-issue bound, HBM well below its rate) also
         their FP32 rate against the nominal FP32 peak ("fp32")
 roofline_rotate  the resampling/accumulation stage against HBM
 cpu_baseline  the FP64 oracle port on this host's cores, on a bounded
@@ -517,8 +517,8 @@ def run_ours(args):
                 "traffic": traffic,
                 "algorithmic_bytes_per_launch": per_launch_bytes,
                 "launch_ms": per_launch_s * 1e3}
-    # the FFT stages are FP32-arithmetic bound (their inputs and outputs stay
-    # in L2): their compute roofline, algorithmic flops 5 N log2 N per
+    # the FFT stages are FP32-issue bound (their HBM traffic is the chunk
+    # buffer between them, well below the HBM rate): their compute roofline, algorithmic flops 5 N log2 N per
     # complex N-point transform plus 6 per propagator multiply, against the
     # nominal FP32 rate 152 SMs x 128 lanes x 2 flops at the median SM clock
     # sampled during the timed steps
