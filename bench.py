@@ -100,6 +100,20 @@ WORKLOADS["apple"] = dict(
     name="apple.correct: 256^3 complex64 reconstruction of the headline "
          "sinogram, method nn, enforce_envelope 0.95, max_iter 100, "
          "min_diff 0.01 (single-precision 3D FFTs)")
+# object function -> refractive index of the headline volume size (the
+# reference's odt_to_ri; opt_to_ri timed beside it)
+WORKLOADS["ri"] = dict(
+    n=256, res=3.0, nm=1.333, seed=2024,
+    name="odt_to_ri: 256^3 complex64 object function -> refractive index "
+         "nm*sqrt(f/km^2+1) (principal root, real part made non-negative)")
+# the 2D reconstruction: the central plane of the headline phantom, 400
+# angles over the full circle, 512 detector pixels
+WORKLOADS["bpp2d"] = dict(
+    A=400, n=512, res=3.0, nm=1.333, lD=0.0, seed=2024,
+    count_range=(3, 12), semi_range=(16, 120),
+    name="backpropagate_2d: A=400 x 512 complex64 Rytov sinogram (central "
+         "plane of an ellipsoid phantom) -> 512^2 complex64 image, padding "
+         "to 2048 (2.1x rule, linear ramp to 0), cubic-spline rotation")
 WORKLOAD = WORKLOADS["c2"]
 WORKLOAD_NAME = WORKLOAD["name"]
 CPU_SAMPLE_ANGLES = 4
@@ -1018,6 +1032,261 @@ def run_apple(args):
     print(json.dumps(line), flush=True)
 
 
+def _ri_volume(w):
+    """Object function of a blob phantom, f = km^2 ((n/nm)^2 - 1) with n in
+    [nm, nm + 0.03] and a small absorbing imaginary part (complex128)."""
+    n = w["n"]
+    rng = np.random.default_rng(w["seed"])
+    g = np.arange(n) - n / 2
+    z, y, x = np.meshgrid(g, g, g, indexing="ij", sparse=True)
+    ri = w["nm"] + 0.03 * np.exp(-(x * x + y * y + z * z) / (0.08 * n * n))
+    km = 2 * np.pi * w["nm"] / w["res"]
+    f = km * km * ((ri / w["nm"]) ** 2 - 1)
+    return f + 1j * rng.normal(0, 1e-3 * km * km, f.shape)
+
+
+def run_ri(args):
+    """odt_to_ri on a 256^3 complex64 volume through the C ABI: one step =
+    one conversion of the whole volume (8 B read + 8 B written per voxel,
+    the algorithmic bytes)."""
+    import ctypes
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    from odtbrain_gb300 import build as native_build
+    native_build.build()
+    import odtbrain_gb300 as odt
+    from odtbrain_gb300 import _native
+    w = WORKLOAD
+    f = _ri_volume(w).astype(np.complex64)
+    N = f.size
+    host = torch.from_numpy(f).pin_memory()
+    df = host.to(dev)
+    out = torch.empty_like(df)
+    stream = torch.cuda.current_stream(dev)
+    L = _native.lib()
+
+    def conv(name, dst):
+        _native.check(getattr(L, name)(
+            ctypes.c_void_p(df.data_ptr()), ctypes.c_void_p(dst.data_ptr()),
+            N, _native.ODT_DATA_C64, w["res"], w["nm"],
+            ctypes.c_void_p(stream.cuda_stream)))
+    flush = torch.empty(L2_FLUSH_BYTES, device=dev, dtype=torch.uint8)
+    if args.ncu_case:
+        for _ in range(2):
+            conv("odt_odt_to_ri", out)
+        torch.cuda.synchronize()
+        print("ncu case done")
+        return
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms, step_ms = _timed(lambda: conv("odt_odt_to_ri", out), args.steps,
+                         args.warmup, flush, stream)
+    clk = clocks.stop()
+    opt_ms, _ = _timed(lambda: conv("odt_opt_to_ri", out), args.steps, 1,
+                       flush, stream)
+    conv("odt_odt_to_ri", out)
+    got = out.cpu().numpy()
+    unit = "voxels/s"
+
+    def e2e():
+        odt.odt_to_ri(f, w["res"], w["nm"])
+    e2e_ms, _ = _timed(e2e, max(3, min(args.steps, 5)), 1, flush, stream)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import odt_oracle
+        f64 = f.astype(np.complex128)
+        t0 = time.perf_counter()
+        ref = odt_oracle.odt_to_ri(f64, w["res"], w["nm"])
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": N / cpu_s, "unit": unit, "cores": 1, "kind": "port",
+               "sample": "the whole %d^3 volume (oracle, NumPy FP64)" % w["n"],
+               "max_abs_rel_diff_vs_gpu":
+                   float(np.abs(got - ref).max() / np.abs(ref).max())}
+    algo = 16.0 * N
+    peak, peak_kind = measured_peaks()
+    achieved = algo / (ms / 1e3) / 1e9
+    line = {"metric": "odt_to_ri voxels/s on 1 GB300 (complex64)",
+            "value": N / (ms / 1e3), "unit": unit, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 (complex64)", "data": "synthetic",
+            "config": {"workload": w["name"],
+                       "l2": "256 MiB flush before every timed step"},
+            "roofline": {"bound": "hbm", "kernel": "k_odt_to_ri_complex",
+                         "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": achieved / peak,
+                         "traffic": profile_traffic("odt_to_ri", N),
+                         "algorithmic_bytes_per_launch": algo,
+                         "launch_ms": ms},
+            "opt_to_ri": {"ms": opt_ms,
+                          "GB_per_s": algo / (opt_ms / 1e3) / 1e9},
+            "clocks": clk, "gpu_launches": 1, "step_ms": step_ms,
+            "e2e": {"value": N / (e2e_ms / 1e3), "unit": unit,
+                    "h2d_bytes_per_step": int(f.nbytes),
+                    "d2h_bytes_per_step": int(f.nbytes),
+                    "ms_per_step": e2e_ms},
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
+def _bpp2d_workload(w):
+    from sino_gen import ellipsoid_phantom_sinogram
+    sino, angles = ellipsoid_phantom_sinogram(
+        w["n"], w["A"], seed=w["seed"], count_range=w["count_range"],
+        semi_range=w["semi_range"], res=w["res"], nm=w["nm"], ny=1)
+    return sino[:, 0, :].astype(np.complex64), angles
+
+
+def run_bpp2d(args):
+    """backpropagate_2d: one step = one 512^2 reconstruction from 400
+    angles; the unit counts pixels times angles."""
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    from odtbrain_gb300 import build as native_build
+    native_build.build()
+    import odtbrain_gb300 as odt
+    from odtbrain_gb300._alg2d import Backprop2D
+    w = WORKLOAD
+    sino, angles = _bpp2d_workload(w)
+    A, n = sino.shape
+    U = float(A) * n * n
+    unit = "pixel-angle updates/s"
+    rec = Backprop2D(sino.shape, angles, w["res"], w["nm"], lD=w["lD"],
+                     device=dev)
+    host = torch.from_numpy(sino).pin_memory()
+    ds = host.to(dev)
+    out = torch.empty((n, n), dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES, device=dev, dtype=torch.uint8)
+    if args.ncu_case:
+        for _ in range(2):
+            rec(ds, out=out)
+        torch.cuda.synchronize()
+        print("ncu case done")
+        return
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms, step_ms = _timed(lambda: rec(ds, out=out, check=False), args.steps,
+                         args.warmup, flush, stream)
+    clk = clocks.stop()
+    rec(ds, out=out, check=True)
+    flush.zero_()
+    stages = rec.timed(ds, out=out)
+    stage_summary = {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
+                         "GB_per_s": (v["bytes"] / (v["ms"] / 1e3) / 1e9
+                                      if v["ms"] > 0 else None)}
+                     for k, v in stages.items()}
+    dom = max(stages, key=lambda k: stages[k]["ms"])
+    ds_ = stages[dom]
+    peak, peak_kind = measured_peaks()
+    achieved = ds_["bytes"] / (ds_["ms"] / 1e3) / 1e9
+
+    def e2e():
+        odt.backpropagate_2d(sino, angles, w["res"], w["nm"], lD=w["lD"])
+    e2e_ms, _ = _timed(e2e, max(3, min(args.steps, 5)), 1, flush, stream)
+    cpu = None
+    if not args.no_cpu_baseline:
+        # parity and CPU time on a bounded sample: 8 of the angles as an
+        # 8-angle problem
+        from oracle import odt_oracle
+        k = 8
+        idx = np.arange(0, A, A // k)[:k]
+        sub = sino[idx].astype(np.complex128)
+        t0 = time.perf_counter()
+        ref = odt_oracle.backpropagate_2d(sub, angles[idx], w["res"],
+                                          w["nm"], lD=w["lD"])
+        cpu_s = time.perf_counter() - t0
+        got = Backprop2D(sub.shape, angles[idx], w["res"], w["nm"],
+                         lD=w["lD"], device=dev)(
+                             torch.from_numpy(sub.astype(np.complex64))
+                             .to(dev)).cpu().numpy()
+        cpu = {"value": k * n * n / cpu_s, "unit": unit, "cores": 1,
+               "kind": "port",
+               "sample": "%d of the %d angles as a %d-angle problem "
+                         "(oracle, NumPy/scipy FP64)" % (k, A, k),
+               "rel_l2_vs_gpu": float(np.linalg.norm(got - ref)
+                                      / np.linalg.norm(ref))}
+    line = {"metric": "backpropagate_2d pixel-angle updates/s on 1 GB300 "
+                      "(FP32)",
+            "value": U / (ms / 1e3), "unit": unit, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 (complex64)", "data": "synthetic",
+            "config": {"workload": w["name"], "A": A, "n": n,
+                       "padded_fft": rec.padding_geometry["lN"],
+                       "l2": "256 MiB flush before every timed step"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved,
+                         "peak": peak, "peak_kind": peak_kind,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None,
+                         "algorithmic_bytes_per_launch":
+                             ds_["bytes"] / max(1, ds_["launches"]),
+                         "launch_ms": ds_["ms"] / max(1, ds_["launches"])},
+            "stages": stage_summary,
+            "clocks": clk, "gpu_launches": rec.launches_per_call,
+            "step_ms": step_ms,
+            "e2e": {"value": U / (e2e_ms / 1e3), "unit": unit,
+                    "h2d_bytes_per_step": int(sino.nbytes),
+                    "d2h_bytes_per_step": int(n * n * 8),
+                    "ms_per_step": e2e_ms},
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_ri(args):
+    """--impl reference for odt_to_ri: the oracle port of the reference
+    (NumPy FP64, as the reference computes) on the whole volume per step."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    from oracle import odt_oracle
+    w = WORKLOAD
+    f = _ri_volume(w)
+    times = []
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        odt_oracle.odt_to_ri(f, w["res"], w["nm"])
+        if it >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    step = statistics.mean(times)
+    print(json.dumps(_reference_line(
+        args, "odt_to_ri voxels/s on 1 GB300 (complex64)", "voxels/s",
+        f.size / step, step, w["name"],
+        "the whole %d^3 volume per step (oracle port of the reference, "
+        "NumPy FP64)" % w["n"], 1)), flush=True)
+
+
+def run_reference_bpp2d(args):
+    """--impl reference for backpropagate_2d: the oracle port of the
+    reference (NumPy FFTs + scipy.ndimage.rotate, FP64) on a bounded
+    sample of 4 angles per step."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    from oracle import odt_oracle
+    w = WORKLOAD
+    sino, angles = _bpp2d_workload(w)
+    A, n = sino.shape
+    s = sino.astype(np.complex128)
+    k = 4
+    times = []
+    for it in range(args.warmup + args.steps):
+        a0 = (it * k) % (A - k)
+        t0 = time.perf_counter()
+        odt_oracle.backpropagate_2d(s[a0:a0 + k], angles[a0:a0 + k],
+                                    w["res"], w["nm"], lD=w["lD"])
+        if it >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    step = statistics.mean(times)
+    print(json.dumps(_reference_line(
+        args, "backpropagate_2d pixel-angle updates/s on 1 GB300 (FP32)",
+        "pixel-angle updates/s", k * n * n / step, step, w["name"],
+        "4 of the 400 angles per step as a 4-angle problem (oracle port of "
+        "the reference: NumPy FFTs, scipy.ndimage.rotate), FP64", 1)),
+        flush=True)
+
+
 def run_ncu_case(rotate_case=False):
     """Small case for ncu captures: the workload's plane and volume sizes
     with 8 angles and the save_memory workspace, or (``rotate_case``) 16
@@ -1060,6 +1329,16 @@ def main():
             run_reference_rytov(args)
         else:
             run_rytov(args)
+    elif args.config == "ri":
+        if args.impl == "reference":
+            run_reference_ri(args)
+        else:
+            run_ri(args)
+    elif args.config == "bpp2d":
+        if args.impl == "reference":
+            run_reference_bpp2d(args)
+        else:
+            run_bpp2d(args)
     elif args.config in ("c4", "c5"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":

@@ -125,6 +125,31 @@ class Backprop2D:
             self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
         return out
 
+    @property
+    def launches_per_call(self):
+        return self.plan.launches_per_execute
+
+    def timed(self, sino, out=None):
+        """Run once with a CUDA event pair around every kernel launch;
+        returns per-stage {"ms", "launches", "bytes"}."""
+        torch = _torch()
+        A, ln = self.shape
+        vdtype = torch.float32 if self.onlyreal else torch.complex64
+        if out is None:
+            out = torch.empty((ln, ln), device=self.device, dtype=vdtype)
+        self(sino, out=out, check=False)  # argument checks, warm tables
+        stream = torch.cuda.current_stream(self.device)
+        t = self.plan.execute_timed(
+            ctypes.c_void_p(sino.data_ptr()),
+            ctypes.c_void_p(self.weights.data_ptr()
+                            if self.weights is not None else 0),
+            ctypes.c_void_p(self.geometry.data_ptr()),
+            ctypes.c_void_p(out.data_ptr()),
+            ctypes.c_void_p(self.workspace.data_ptr()),
+            ctypes.c_void_p(stream.cuda_stream))
+        self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
+        return t
+
 
 def backpropagate_2d(uSin, angles, res, nm, lD=0, coords=None,
                      weight_angles=True,

@@ -255,6 +255,32 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
     }
 }
 
+// (b1) for lNy == 1 (the 2D reconstruction: one detector row, so one row
+// per plane): the column transforms are the identity, and a job's row is
+// the row spectrum times the filter table and the exact propagator of its
+// plane.  One thread per (job, kx); zero columns are stored as zeros.
+__global__ void __launch_bounds__(256) k_columns_line(StageParams P, const float2 *rowspec, float2 *T, int q0,
+                                                      int qn)
+{
+    const int lNx = P.lNx, nz = P.nz;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)qn * lNx)
+        return;
+    const int qrel = (int)(i / lNx), kx = (int)(i - (long long)qrel * lNx);
+    const int q = q0 + qrel, a = q / nz, p = q - a * nz;
+    float2 v = make_float2(0.f, 0.f);
+    if (column_active(P, kx)) {
+        v = cmul(rowspec[(size_t)a * lNx + kx], P.tab.G[kx]);
+        if (P.gain)
+            v = cscale(v, P.gain[kx]);
+        if (P.again)
+            v = cmul(v, P.again[(size_t)a * lNx + kx]);
+        const float zp = (float)p - 0.5f * (float)nz + P.zshift;
+        v = cmul(v, expi_phase(P.tab.wsplit[kx], zp));
+    }
+    T[(size_t)qrel * lNx + kx] = v;
+}
+
 // ---------------------------------------------------------------------------
 // (b2) rows: (+ z-boundary rows), backward FFT along x, x-prefilter boundary
 // terms, crop -> slab.
@@ -265,7 +291,8 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
 // the current group is transformed.  When a line is whole warps its FFT
 // exchanges sync only its own warps (named barrier).  The cropped rows of a
 // group are transposed through shared memory and stored as runs of LPC
-// consecutive y per x (rows y >= ny are zero).
+// consecutive y per x (rows y >= ny of a group are zero; groups and CTAs
+// wholly beyond ny are not run).
 template <int LPC>
 constexpr int rows_per_cta()
 {
@@ -286,9 +313,12 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     // lines of whole warps sync on named barrier 1 + l
     const int bar = (L::TPL % 32 == 0 && LPC < 15) ? 1 + l : 0;
     const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl, yp = P.ypitch;
-    const int cpj = yp / RG;  // CTAs per job
+    const int cpj = (ny + RG - 1) / RG;  // CTAs per job (rows y < ny only)
     const int qrel = (int)blockIdx.x / cpj;
     const int ybase = ((int)blockIdx.x - qrel * cpj) * RG;
+    // groups holding at least one row y < ny (the slab rows y >= ny are
+    // never read: the resampling lanes of those y store nothing)
+    const int GV = min(G, (ny - ybase + LPC - 1) / LPC);
     const int qq = q0 + qrel;  // the grid covers exactly qn jobs
     const int a = qq / nz, p = qq - a * nz;
     const bool pf = P.order >= 2;
@@ -310,10 +340,10 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     load_row(ybase + l, v);
     __syncthreads();  // twiddles
 #pragma unroll 1
-    for (int g = 0; g < G; ++g) {
+    for (int g = 0; g < GV; ++g) {
         const int y = ybase + g * LPC + l;
         const bool valid = y < ny;
-        if (g + 1 < G)
+        if (g + 1 < GV)
             load_row(y + LPC, vn);
         if (valid && (zl != 0.f || zh != 0.f)) {
             const float2 *ta = Tab + ((size_t)(a * 2 + 0) * ny + y) * n;
@@ -382,7 +412,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
             const int xx = e / LPC, ll = e - xx * LPC;
             __stcs(dst + (size_t)xx * yp + g * LPC + ll, stage[xx * SP + ll]);
         }
-        if (g + 1 < G) {
+        if (g + 1 < GV) {
             __syncthreads();  // stage reads done before buf0 is reused
 #pragma unroll
             for (int r = 0; r < L::SLOTS; ++r)
@@ -447,7 +477,7 @@ static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 
                                      float2 *slab, int q0, int qn, cudaStream_t s)
 {
     constexpr int LPC = Cfg<L>::LPC;
-    const unsigned grid = (unsigned)((long long)qn * (P.ypitch / rows_per_cta<LPC>()));
+    const unsigned grid = (unsigned)((long long)qn * ((P.ny + rows_per_cta<LPC>() - 1) / rows_per_cta<LPC>()));
     k_rows_inverse<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, Tab, slab, q0, qn);
     return cudaGetLastError();
 }
@@ -519,6 +549,11 @@ cudaError_t launch_rows_forward(const StageParams &P, const void *sino_batch, co
 cudaError_t launch_columns_propagate(const StageParams &P, const float2 *rowspec, float2 *T, int q0, int qn,
                                      cudaStream_t s)
 {
+    if (P.lNy == 1 && P.ny == 1 && P.padyl == 0) {
+        const long long n = (long long)qn * P.lNx;
+        k_columns_line<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, rowspec, T, q0, qn);
+        return cudaGetLastError();
+    }
     return with_line(P.lNy, [&](auto line) { return columns_impl(P, line, rowspec, T, q0, qn, s); });
 }
 

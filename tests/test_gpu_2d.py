@@ -130,3 +130,29 @@ def test_ri_complex_and_single_precision(cuda_ready):
         ref = O.odt_to_ri(np.array([-1e6, 0.5]), 3.0, 1.333)
     got = odt.odt_to_ri(np.array([-1e6, 0.5]), 3.0, 1.333)
     assert np.isnan(got[0]) and np.isclose(got[1], ref[1].real)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 1023, 4097])
+def test_ri_vector_and_tail_paths(cuda_ready, n):
+    """Single-precision conversions take 16-byte accesses on aligned data
+    with a scalar tail, and the scalar kernel on data that is not 16-byte
+    aligned (a tensor view one element in): every path against the
+    oracle."""
+    import torch
+    import odtbrain_gb300 as odt
+    rng = np.random.default_rng(n)
+    base = rng.normal(0, 3, n + 1) + 1j * rng.normal(0, 3, n + 1)
+    for res, nm in ((3.0, 1.333),):
+        for fn in ("odt_to_ri", "opt_to_ri"):
+            for data in (base.astype(np.complex64),
+                         np.abs(base.real).astype(np.float32)):
+                ref = getattr(O, fn)(data[1:].astype(
+                    np.complex128 if data.dtype.kind == "c" else np.float64),
+                    res, nm)
+                scale = np.abs(ref).max()
+                t = torch.tensor(data, device=cuda_ready)
+                for view in (t[1:], t[1:].clone()):
+                    got = getattr(odt, fn)(view, res, nm).cpu().numpy()
+                    assert got.dtype == data.dtype
+                    assert np.abs(got - ref).max() <= 1e-6 * scale, \
+                        (fn, data.dtype, view.data_ptr() % 16)
