@@ -1183,6 +1183,14 @@ def run_bpp2d(args):
     ds_ = stages[dom]
     peak, peak_kind = measured_peaks()
     achieved = ds_["bytes"] / (ds_["ms"] / 1e3) / 1e9
+    # DRAM bytes of the dominant launch from the committed ncu summary,
+    # scaled by its units (planes for the fused row stage, updates for the
+    # resampling)
+    nl = max(1, ds_["launches"])
+    traffic = {"rows_inverse": lambda: profile_traffic("rows_line_2d",
+                                                       A * n / nl),
+               "rotate": lambda: profile_traffic("rotate_plane", U / nl)
+               }.get(dom, lambda: None)()
 
     def e2e():
         odt.backpropagate_2d(sino, angles, w["res"], w["nm"], lD=w["lD"])
@@ -1221,7 +1229,7 @@ def run_bpp2d(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved,
                          "peak": peak, "peak_kind": peak_kind,
                          "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None,
+                         "traffic": traffic,
                          "algorithmic_bytes_per_launch":
                              ds_["bytes"] / max(1, ds_["launches"]),
                          "launch_ms": ds_["ms"] / max(1, ds_["launches"])},

@@ -173,8 +173,6 @@ odt_status validate(const odt_bpp3d_desc *d)
         return fail(ODT_ERR_UNSUPPORTED, "spline orders 4 and 5 are not implemented on the GPU");
     if (!std::isfinite(d->z_shift) || std::fabs(d->z_shift) > 1.0 || 2.0 * d->z_shift != std::rint(2.0 * d->z_shift))
         return fail(ODT_ERR_INVALID_ARGUMENT, "z_shift must be 0, +-0.5 or +-1");
-    if (d->geometry == ODT_GEOM_AFFINE3D && d->intp_order >= 2 && d->ny < 2)
-        return fail(ODT_ERR_UNSUPPORTED, "3D spline prefilter needs ny >= 2");
     if (!odt::line_size_supported(d->pad_nx) || !odt::line_size_supported(d->pad_ny))
         return fail(ODT_ERR_UNSUPPORTED,
                     "FFT length must be a power of two in [64, 4096] or any length <= 1024");
@@ -244,7 +242,9 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     // are per-frequency functions of them)
     const double z_first = 0.0 - 0.5 * nz + d.z_shift, z_last = (double)(nz - 1) - 0.5 * nz + d.z_shift;
     for (int ky = 0; ky < lNy; ++ky) {
-        const double iby = (pf && tilted) ? 1.0 / spline_bhat(order, fftfreq_rad(ky, lNy)) : 1.0;
+        // (scipy leaves an axis of length 1 unfiltered: no y prefilter, and
+        // its boundary coefficients stay zero, for a single detector row)
+        const double iby = (pf && tilted && d.ny >= 2) ? 1.0 / spline_bhat(order, fftfreq_rad(ky, lNy)) : 1.0;
         for (int kx = 0; kx < lNx; ++kx) {
             const size_t k = (size_t)ky * lNx + kx;
             const double ibx = pf ? 1.0 / spline_bhat(order, fftfreq_rad(kx, lNx)) : 1.0;
@@ -560,7 +560,15 @@ odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *
             lt.end(0.0);
         }
         const int total = nb * plan->nz;
-        if (timing) {
+        if (odt::single_row_plan(P)) {
+            // single-row planes: the column stage is the identity and runs
+            // inside the row stage, one launch over the batch's jobs
+            lt.begin(ODT_STAGE_ROWS_INVERSE);
+            e = odt::launch_rows_line(P, rowspec, Tab, slab, 0, total, s);
+            if (e != cudaSuccess)
+                return cuda_fail(e, "rows_line launch");
+            lt.end(nb * spec * 8.0 + (double)total * plane_in * 8.0);
+        } else if (timing) {
             // per-stage timing: the stages one after the other on one stream
             for (int q0 = 0; q0 < total; q0 += plan->jobs) {
                 const int qn = std::min(plan->jobs, total - q0);
@@ -770,7 +778,10 @@ odt_status odt_bpp3d_launch_count(const odt_bpp3d_plan *plan, int64_t *launches)
     for (int b = 0; b < nbatches; ++b) {
         const int nb = std::min(plan->batch, A - b * plan->batch);
         const int64_t total = (int64_t)nb * plan->nz;
-        n += 2 + 2 * ((total + plan->jobs - 1) / plan->jobs);
+        if (odt::single_row_plan(stage_params(plan)))
+            n += 3;  // row spectra, fused column + row stage, resampling
+        else
+            n += 2 + 2 * ((total + plan->jobs - 1) / plan->jobs);
         if (plan->d.intp_order >= 2)
             n += 1;  // z-prefilter boundary columns
         if (plan->d.geometry == ODT_GEOM_Y_AXIS)

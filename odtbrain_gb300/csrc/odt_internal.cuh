@@ -6,13 +6,18 @@
 
 namespace odt {
 
-// Asynchronous 16-byte global -> shared copies (cp.async, L2 only) and their
-// group bookkeeping.
+// Asynchronous global -> shared copies (cp.async: 16 bytes through L2 only,
+// 8 bytes through L1) and their group bookkeeping.
 #ifdef __CUDACC__
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
@@ -67,7 +72,9 @@ struct StageParams {
 };
 
 // y pitch of the slab layout [a][z][x][y]
-inline int yaxis_slab_pitch(int ny) { return (ny + 31) / 32 * 32; }
+// y pitch of the y-axis coefficient slab [a][z][x][y]: a multiple of 32,
+// except for single-row planes (the 2D reconstruction), stored as [a][z][x]
+inline int yaxis_slab_pitch(int ny) { return ny == 1 ? 1 : (ny + 31) / 32 * 32; }
 
 struct RotParams {
     int ny, nx, nz;
@@ -87,6 +94,11 @@ cudaError_t launch_columns_propagate(const StageParams &P, const float2 *rowspec
 // z-prefilter boundary columns of a batch (order >= 2): Tab[a][2][ny][lNx].
 cudaError_t launch_columns_boundary(const StageParams &P, const float2 *rowspec, float2 *Tab, int nb,
                                     cudaStream_t s);
+// Single-row planes (lNy == ny == 1, slab pitch 1): the column and row
+// stages fused in one launch over jobs [q0, q0 + qn), from the row spectra.
+bool single_row_plan(const StageParams &P);
+cudaError_t launch_rows_line(const StageParams &P, const float2 *rowspec, const float2 *Tab, float2 *slab, int q0,
+                             int qn, cudaStream_t s);
 cudaError_t launch_rows_inverse(const StageParams &P, const float2 *T, const float2 *Tab, float2 *slab, int q0,
                                 int qn, cudaStream_t s);
 // Scratch (device bytes) the rotation stage needs for a batch: per-(angle,

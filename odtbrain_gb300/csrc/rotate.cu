@@ -361,15 +361,20 @@ __device__ __forceinline__ TileGeo load_tile(const TileGeo *p)
     return t;
 }
 
-// Parameter record of output (oz, ox) for one angle: word 0 box offset of
-// the first tap (float2 units), word 1 in/out flag, then (wz_i, wz_i) pairs
-// and (wx_k, wx_k) pairs, i, k = 0..ORDER.
+// Taps of output (oz, ox) for one angle: the position (rz, rx) of its first
+// tap in the tile's footprint box and the z and x weights.  False (weights
+// zero) for an output outside the domain, or whose taps leave the box (then
+// recorded in the status word).
 template <int ORDER>
-__device__ __forceinline__ void output_params(const RotParams &R, const TileGeo &cur, const double *g, int oz0,
-                                              int ox0, int oz, int ox, float *rec)
+__device__ __forceinline__ bool output_taps(const RotParams &R, const TileGeo &cur, const double *g, int oz0,
+                                            int ox0, int oz, int ox, int &rz, int &rx, float (&wz)[4],
+                                            float (&wx)[4])
 {
-    int off = 0, ok = 0;
-    float wz[4] = {0.f, 0.f, 0.f, 0.f}, wx[4] = {0.f, 0.f, 0.f, 0.f};
+    bool ok = false;
+    rz = rx = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        wz[k] = wx[k] = 0.f;
     const int nz = R.nz, nx = R.nx;
     if (cur.box_zn > 0 && oz < nz && ox < nx) {
         int Iz, Ix;
@@ -411,15 +416,32 @@ __device__ __forceinline__ void output_params(const RotParams &R, const TileGeo 
                 for (int k = 0; k <= ORDER; ++k)
                     wx[k] = w[k];
             }
-            const int rz = tz0 - cur.box_z0, rx = tx0 - cur.box_x0;
+            rz = tz0 - cur.box_z0;
+            rx = tx0 - cur.box_x0;
             if (rz >= 0 && rz + ORDER < cur.box_zn && rx >= 0 && rx + ORDER < cur.box_xn) {
-                off = (rz * cur.box_xn + rx) * R2_Y;
-                ok = 1;
+                ok = true;
             } else {
                 atomicOr(R.status, DEVCHK_BOX_OVERFLOW);  // tap outside the staged box
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    wz[k] = wx[k] = 0.f;
             }
         }
     }
+    return ok;
+}
+
+// Parameter record of output (oz, ox) for one angle: word 0 box offset of
+// the first tap (float2 units), word 1 in/out flag, then (wz_i, wz_i) pairs
+// and (wx_k, wx_k) pairs, i, k = 0..ORDER.
+template <int ORDER>
+__device__ __forceinline__ void output_params(const RotParams &R, const TileGeo &cur, const double *g, int oz0,
+                                              int ox0, int oz, int ox, float *rec)
+{
+    int rz, rx;
+    float wz[4], wx[4];
+    const int ok = output_taps<ORDER>(R, cur, g, oz0, ox0, oz, ox, rz, rx, wz, wx) ? 1 : 0;
+    const int off = ok ? (rz * cur.box_xn + rx) * R2_Y : 0;
     // 16-byte stores only: header, then the (w, w) pairs two per store
     float w[2 * (ORDER + 1) + 1];
 #pragma unroll
@@ -540,6 +562,122 @@ __global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const f
                 store_sum<ONLYREAL>(R, volume, comp, ((size_t)oz * ny + y) * nx + ox, s[q], cp[q]);
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Single-row path (ny == 1, the 2D reconstruction): the slab is [a][z][x]
+// (pitch 1) and there is no y to spread over lanes, so each of a CTA's 256
+// threads owns one output of a 16 x 16 tile and computes its own taps and
+// weights (output_taps: the decisions of k_rotate_y).  Per angle the tile's
+// footprint (<= 28 x 28 positions, mirrored positions filled from their
+// images) is staged in shared memory with 8-byte cp.async, three buffers
+// deep: the copies of angles a+1 and a+2 are in flight while angle a is
+// interpolated.  The footprint boxes (the last 16 bytes of a tile record)
+// are loaded two angles ahead, the whole records one angle ahead.
+constexpr int RP_BOXE = R2_BOX * R2_BOX;
+constexpr int RP_BUFS = 3;
+
+struct BoxDesc {
+    short z0, x0, zn, xn, interior, real;
+    int pad;
+};
+static_assert(sizeof(BoxDesc) == 16, "BoxDesc is the 16-byte tail of a TileGeo");
+
+__device__ __forceinline__ BoxDesc load_box(const TileGeo *p)
+{
+    const int4 v = reinterpret_cast<const int4 *>(p)[3];
+    return *reinterpret_cast<const BoxDesc *>(&v);
+}
+
+// Issue the footprint copy of one (angle, tile): position (vz, vx) of the
+// box at buf[vz * xn + vx], read from its mirror image.
+__device__ __forceinline__ void stage_plane(const BoxDesc &b, const float2 *aslab, int nz, int nx, float2 *buf)
+{
+    const int xn = b.xn, np = b.zn * xn;
+    for (int p = threadIdx.x; p < np; p += blockDim.x) {
+        const int pz = p / xn, px = p - pz * xn;
+        const int mz = b.real ? b.z0 + pz : mirror_idx(b.z0 + pz, nz);
+        const int mx = b.real ? b.x0 + px : mirror_idx(b.x0 + px, nx);
+        cp_async8(buf + p, aslab + (size_t)mz * nx + mx);
+    }
+}
+
+template <int ORDER, bool ONLYREAL>
+__global__ void __launch_bounds__(R2_T * R2_T) k_rotate_plane(RotParams R, const float2 *__restrict__ slab,
+                                                              const double *__restrict__ geo,
+                                                              const TileGeo *__restrict__ tiles, void *volume,
+                                                              float2 *comp)
+{
+    __shared__ float2 box[RP_BUFS][RP_BOXE];
+    const int tid = threadIdx.x;
+    const int ntx = (R.nx + R2_T - 1) / R2_T, ntz = (R.nz + R2_T - 1) / R2_T;
+    const int tile = blockIdx.y * ntx + blockIdx.x;
+    const int ox0 = blockIdx.x * R2_T, oz0 = blockIdx.y * R2_T;
+    const int ox = ox0 + (tid & (R2_T - 1)), oz = oz0 + tid / R2_T;
+    const int nx = R.nx, nz = R.nz, nb = R.nbatch_angles;
+    const size_t astride = (size_t)nz * nx, rstride = (size_t)ntz * ntx;
+    const TileGeo *trec = tiles + tile;
+    float2 s = make_float2(0.f, 0.f), c = s, part = s;
+    // angles 0 and 1 staged; records: cur = 0, nxt = 1; box d2 = angle 2
+    TileGeo cur = load_tile(trec);
+    TileGeo nxt = cur;
+    BoxDesc d2 = load_box(trec);
+    {
+        const BoxDesc b0 = load_box(trec);
+        if (b0.zn > 0)
+            stage_plane(b0, slab, nz, nx, box[0]);
+        cp_async_commit();
+        if (nb > 1) {
+            nxt = load_tile(trec + rstride);
+            const BoxDesc b1 = load_box(trec + rstride);
+            if (b1.zn > 0)
+                stage_plane(b1, slab + astride, nz, nx, box[1]);
+        }
+        cp_async_commit();
+        if (nb > 2)
+            d2 = load_box(trec + 2 * rstride);
+    }
+    for (int a = 0; a < nb; ++a) {
+        TileGeo nxt2 = nxt;
+        BoxDesc d3 = d2;
+        if (a + 2 < nb) {
+            if (d2.zn > 0)
+                stage_plane(d2, slab + (size_t)(a + 2) * astride, nz, nx, box[(a + 2) % RP_BUFS]);
+            nxt2 = load_tile(trec + (size_t)(a + 2) * rstride);
+            if (a + 3 < nb)
+                d3 = load_box(trec + (size_t)(a + 3) * rstride);
+        }
+        cp_async_commit();
+        int rz, rx;
+        float wz[4], wx[4];
+        const bool ok = output_taps<ORDER>(R, cur, geo + 6 * (size_t)a, oz0, ox0, oz, ox, rz, rx, wz, wx);
+        cp_async_wait<2>();  // angle a's copies (all but the two latest groups)
+        __syncthreads();
+        if (ok) {
+            const int xn = cur.box_xn;
+            const float2 *t = box[a % RP_BUFS] + rz * xn + rx;
+            float2 acc = part;
+#pragma unroll
+            for (int i = 0; i <= ORDER; ++i) {
+                float2 r = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k <= ORDER; ++k)
+                    r = ffma2(make_float2(wx[k], wx[k]), t[i * xn + k], r);
+                acc = ffma2(make_float2(wz[i], wz[i]), r, acc);
+            }
+            part = acc;
+        }
+        if ((a % R2_KAHAN) == R2_KAHAN - 1 || a == nb - 1) {
+            kahan_add(s, c, part);
+            part = make_float2(0.f, 0.f);
+        }
+        __syncthreads();  // box[a % 3] is refilled with angle a + 3 next
+        cur = nxt;
+        nxt = nxt2;
+        d2 = d3;
+    }
+    if (oz < nz && ox < nx)
+        store_sum<ONLYREAL>(R, volume, comp, (size_t)oz * nx + ox, s, c);
 }
 
 // ---------------------------------------------------------------------------
@@ -748,8 +886,13 @@ static cudaError_t rotate_impl(const RotParams &R, int tilted, const float2 *sla
         const int nset = R.nbatch_angles * ntiles;
         TileGeo *tiles = reinterpret_cast<TileGeo *>(scratch);
         k_rotate_y_setup<ORDER><<<(nset + 127) / 128, 128, 0, s>>>(R, geo, tiles);
-        dim3 grid((R.nx + R2_T - 1) / R2_T, (R.nz + R2_T - 1) / R2_T, (R.ny + R2_Y - 1) / R2_Y);
-        k_rotate_y<ORDER, ONLYREAL><<<grid, R2_THREADS, R2_SMEM, s>>>(R, slab, geo, tiles, volume, comp);
+        if (R.ny == 1 && R.ypitch == 1) {
+            dim3 grid((R.nx + R2_T - 1) / R2_T, (R.nz + R2_T - 1) / R2_T);
+            k_rotate_plane<ORDER, ONLYREAL><<<grid, R2_T * R2_T, 0, s>>>(R, slab, geo, tiles, volume, comp);
+        } else {
+            dim3 grid((R.nx + R2_T - 1) / R2_T, (R.nz + R2_T - 1) / R2_T, (R.ny + R2_Y - 1) / R2_Y);
+            k_rotate_y<ORDER, ONLYREAL><<<grid, R2_THREADS, R2_SMEM, s>>>(R, slab, geo, tiles, volume, comp);
+        }
     } else {
         dim3 grid((R.nx + R3_X - 1) / R3_X, (R.ny + R3_Y - 1) / R3_Y, (R.nz + R3_Z - 1) / R3_Z);
         k_rotate_3d<ORDER, ONLYREAL><<<grid, R3_X * 32, 0, s>>>(R, slab, geo, volume, comp);

@@ -255,37 +255,11 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
     }
 }
 
-// (b1) for lNy == 1 (the 2D reconstruction: one detector row, so one row
-// per plane): the column transforms are the identity, and a job's row is
-// the row spectrum times the filter table and the exact propagator of its
-// plane.  One thread per (job, kx); zero columns are stored as zeros.
-__global__ void __launch_bounds__(256) k_columns_line(StageParams P, const float2 *rowspec, float2 *T, int q0,
-                                                      int qn)
-{
-    const int lNx = P.lNx, nz = P.nz;
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long long)qn * lNx)
-        return;
-    const int qrel = (int)(i / lNx), kx = (int)(i - (long long)qrel * lNx);
-    const int q = q0 + qrel, a = q / nz, p = q - a * nz;
-    float2 v = make_float2(0.f, 0.f);
-    if (column_active(P, kx)) {
-        v = cmul(rowspec[(size_t)a * lNx + kx], P.tab.G[kx]);
-        if (P.gain)
-            v = cscale(v, P.gain[kx]);
-        if (P.again)
-            v = cmul(v, P.again[(size_t)a * lNx + kx]);
-        const float zp = (float)p - 0.5f * (float)nz + P.zshift;
-        v = cmul(v, expi_phase(P.tab.wsplit[kx], zp));
-    }
-    T[(size_t)qrel * lNx + kx] = v;
-}
-
 // ---------------------------------------------------------------------------
 // (b2) rows: (+ z-boundary rows), backward FFT along x, x-prefilter boundary
 // terms, crop -> slab.
 // Slab layout [a][z][x][y] (both geometries) with the y pitch P.ypitch (a
-// multiple of 32).  A CTA owns RG consecutive y rows of one plane (job) and
+// multiple of 32, or 1 for single-row planes).  A CTA owns RG consecutive y rows of one plane (job) and
 // transforms them in groups of LPC lines (one line per TPL threads); the T
 // values of the next group are loaded (evict-first) into registers while
 // the current group is transformed.  When a line is whole warps its FFT
@@ -410,7 +384,8 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
         __syncthreads();
         for (int e = threadIdx.x; e < nx * LPC; e += LPC * L::TPL) {
             const int xx = e / LPC, ll = e - xx * LPC;
-            __stcs(dst + (size_t)xx * yp + g * LPC + ll, stage[xx * SP + ll]);
+            if (ybase + g * LPC + ll < ny)  // pitch 1 for single-row planes
+                __stcs(dst + (size_t)xx * yp + g * LPC + ll, stage[xx * SP + ll]);
         }
         if (g + 1 < GV) {
             __syncthreads();  // stage reads done before buf0 is reused
@@ -419,6 +394,166 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
                 v[r] = vn[r];
         }
     }
+}
+
+// (b1+b2) single-row planes (lNy == ny == 1, slab pitch 1: the 2D
+// reconstruction): the column transforms are the identity, so a job's row
+// is the row spectrum times the filter table (and gains) and the propagator
+// of its plane, formed here instead of in a column stage.  A CTA takes RG
+// consecutive jobs as groups of LPC lines (one job per line).  With one
+// line per group the propagator is anchored exactly at the CTA's first job
+// (and wherever the angle changes) and advanced plane by plane with the
+// complex step exp(i w), as in k_columns_propagate; with several lines per
+// group every line is anchored exactly.  Then per line the z-boundary rows
+// of its plane, the backward FFT along x, the x-prefilter boundary terms,
+// and the cropped row stored contiguously at slab[a][p][x].
+template <class L, int LPC>
+__global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
+    k_rows_line(StageParams P, L line, const float2 *rowspec, const float2 *Tab, float2 *slab, int q0, int qn)
+{
+    constexpr int RG = rows_per_cta<LPC>(), G = RG / LPC;
+    extern __shared__ float2 smem[];
+    const int n = line.size();  // lNx
+    const int ls = xslots<false>(n);
+    float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
+    copy_twiddles<L>(tw, P.tab.twx, n);
+    const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
+    const int bar = (L::TPL % 32 == 0 && LPC < 15) ? 1 + l : 0;
+    const int nx = P.nx, nz = P.nz, padxl = P.padxl;
+    const bool pf = P.order >= 2;
+    const int qbase = (int)blockIdx.x * RG;
+    const int GV = min(G, (qn - qbase + LPC - 1) / LPC);  // groups holding a job
+    float2 W[L::SLOTS];  // LPC == 1: the next plane's propagated spectrum
+    int cur_a = -1;
+    __syncthreads();  // twiddles
+#pragma unroll 1
+    for (int g = 0; g < GV; ++g) {
+        const int qrel = qbase + g * LPC + l;
+        const bool valid = qrel < qn;
+        const int q = q0 + (valid ? qrel : 0);
+        const int a = q / nz, p = q - a * nz;
+        float2 v[L::SLOTS];
+        if (LPC == 1 && a == cur_a) {
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int x = j + r * L::TPL;
+                v[r] = W[r];
+                if (column_active(P, x))
+                    W[r] = cmul(W[r], P.tab.step[x]);
+            }
+        } else {
+            const float zp = (float)p - 0.5f * (float)nz + P.zshift;
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int x = j + r * L::TPL;
+                float2 b = make_float2(0.f, 0.f);
+                if (valid && column_active(P, x)) {
+                    b = cmul(rowspec[(size_t)a * n + x], P.tab.G[x]);
+                    if (P.gain)
+                        b = cscale(b, P.gain[x]);
+                    if (P.again)
+                        b = cmul(b, P.again[(size_t)a * n + x]);
+                    b = cmul(b, expi_phase(P.tab.wsplit[x], zp));
+                }
+                v[r] = b;
+                if (LPC == 1)
+                    W[r] = column_active(P, x) ? cmul(b, P.tab.step[x]) : b;
+            }
+            cur_a = a;
+        }
+        if (valid && pf) {
+            const float zl = p < ZPOW_N ? P.tab.zpow[p] : 0.f;
+            const float zh = nz - 1 - p < ZPOW_N ? P.tab.zpow[nz - 1 - p] : 0.f;
+            if (zl != 0.f || zh != 0.f) {
+                const float2 *ta = Tab + (size_t)(a * 2 + 0) * n;
+                const float2 *tb = Tab + (size_t)(a * 2 + 1) * n;
+#pragma unroll
+                for (int r = 0; r < L::SLOTS; ++r) {
+                    const int x = j + r * L::TPL;
+                    if (column_active(P, x)) {
+                        const float2 u = ta[x], w = tb[x];
+                        v[r] = make_float2(fmaf(zh, w.x, fmaf(zl, u.x, v[r].x)),
+                                           fmaf(zh, w.y, fmaf(zl, u.y, v[r].y)));
+                    }
+                }
+            }
+        }
+        int flip = 0;
+        line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
+        float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
+        if (pf) {
+            // the line's samples at x0-1, x0+1, x1-1, x1+1 (periodic), through
+            // the exchange buffer the FFT's last exchange did not use
+            float2 *sc = (flip ? buf1 : buf0) + l * ls;
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int x = j + r * L::TPL;
+                if (x < n)
+                    sc[x] = v[r];
+            }
+            if (bar > 0)
+                line_sync(bar, L::TPL);
+            else
+                __syncthreads();
+            const int e0 = (padxl - 1 + n) % n, e1 = (padxl + 1) % n;
+            const int e2 = (padxl + nx - 2 + n) % n, e3 = (padxl + nx) % n;
+            const float2 d0 = sc[e0] - sc[e1];
+            const float2 d1 = sc[e3] - sc[e2];
+            Acoef = make_float2(P.bx_ca * d0.x + P.bx_cb * d1.x, P.bx_ca * d0.y + P.bx_cb * d1.y);
+            Bcoef = make_float2(P.bx_ca * d1.x + P.bx_cb * d0.x, P.bx_ca * d1.y + P.bx_cb * d0.y);
+        }
+        if (valid) {
+            float2 *dst = slab + ((size_t)a * nz + p) * nx;
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int xx = j + r * L::TPL - padxl;
+                if (xx >= 0 && xx < nx) {
+                    float2 o = v[r];
+                    if (pf) {
+                        if (xx < ZPOW_N) {
+                            const float zz = P.tab.zpow[xx];
+                            o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
+                        }
+                        if (nx - 1 - xx < ZPOW_N) {
+                            const float zz = P.tab.zpow[nx - 1 - xx];
+                            o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
+                        }
+                    }
+                    __stcs(dst + xx, o);
+                }
+            }
+        }
+        // the edge reads of this group end before the next group's FFT
+        // writes the exchange buffers
+        if (g + 1 < GV) {
+            if (bar > 0)
+                line_sync(bar, L::TPL);
+            else
+                __syncthreads();
+        }
+    }
+}
+
+// (b0) z-prefilter boundary columns for single-row planes: the column
+// transforms are the identity, Tab[a][t][kx] = spectrum * G * (alpha, beta).
+__global__ void __launch_bounds__(256) k_columns_boundary_line(StageParams P, const float2 *rowspec, float2 *Tab,
+                                                               int nb)
+{
+    const int lNx = P.lNx;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nb * lNx)
+        return;
+    const int a = (int)(i / lNx), kx = (int)(i - (long long)a * lNx);
+    float2 b = make_float2(0.f, 0.f);
+    if (column_active(P, kx)) {
+        b = cmul(rowspec[(size_t)a * lNx + kx], P.tab.G[kx]);
+        if (P.gain)
+            b = cscale(b, P.gain[kx]);
+        if (P.again)
+            b = cmul(b, P.again[(size_t)a * lNx + kx]);
+    }
+    Tab[(size_t)(a * 2 + 0) * lNx + kx] = cmul(b, P.tab.alpha[kx]);
+    Tab[(size_t)(a * 2 + 1) * lNx + kx] = cmul(b, P.tab.beta[kx]);
 }
 
 // ---------------------------------------------------------------------------
@@ -499,6 +634,10 @@ static cudaError_t set_smem_attrs(int n)
                              (int)smem_rows<L>(n));
     if (e != cudaSuccess)
         return e;
+    e = cudaFuncSetAttribute(k_rows_line<L, Cfg<L>::LPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_rows<L>(n));
+    if (e != cudaSuccess)
+        return e;
     e = cudaFuncSetAttribute(k_columns_boundary<L, Cfg<L>::KX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem_cols<L>(n));
     if (e != cudaSuccess)
@@ -549,17 +688,34 @@ cudaError_t launch_rows_forward(const StageParams &P, const void *sino_batch, co
 cudaError_t launch_columns_propagate(const StageParams &P, const float2 *rowspec, float2 *T, int q0, int qn,
                                      cudaStream_t s)
 {
-    if (P.lNy == 1 && P.ny == 1 && P.padyl == 0) {
-        const long long n = (long long)qn * P.lNx;
-        k_columns_line<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, rowspec, T, q0, qn);
-        return cudaGetLastError();
-    }
     return with_line(P.lNy, [&](auto line) { return columns_impl(P, line, rowspec, T, q0, qn, s); });
+}
+
+bool single_row_plan(const StageParams &P)
+{
+    return P.lNy == 1 && P.ny == 1 && P.padyl == 0 && P.ypitch == 1;
+}
+
+cudaError_t launch_rows_line(const StageParams &P, const float2 *rowspec, const float2 *Tab, float2 *slab, int q0,
+                             int qn, cudaStream_t s)
+{
+    return with_line(P.lNx, [&](auto line) {
+        using L = decltype(line);
+        constexpr int LPC = Cfg<L>::LPC;
+        const unsigned grid = (unsigned)((qn + rows_per_cta<LPC>() - 1) / rows_per_cta<LPC>());
+        k_rows_line<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, rowspec, Tab, slab, q0, qn);
+        return cudaGetLastError();
+    });
 }
 
 cudaError_t launch_columns_boundary(const StageParams &P, const float2 *rowspec, float2 *Tab, int nb,
                                     cudaStream_t s)
 {
+    if (single_row_plan(P)) {
+        const long long n = (long long)nb * P.lNx;
+        k_columns_boundary_line<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, rowspec, Tab, nb);
+        return cudaGetLastError();
+    }
     return with_line(P.lNy, [&](auto line) { return boundary_impl(P, line, rowspec, Tab, nb, s); });
 }
 
