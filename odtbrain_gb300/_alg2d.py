@@ -22,7 +22,8 @@ import numpy as np
 
 from . import _geometry as geom
 from . import _native
-from ._alg3d import _WS_DEFAULT, _device_for, _get_plan, _is_tensor, _torch
+from ._alg3d import (_WS_DEFAULT, _device_for, _get_plan, _get_tables,
+                     _is_tensor, _torch)
 
 
 class Backprop2D:
@@ -56,9 +57,12 @@ class Backprop2D:
                         str(input_dtype).replace("torch.", "")]
         self.input_dtype = (torch.complex64 if in_dtype ==
                             _native.ODT_INPUT_C64 else torch.complex128)
-        weights = (geom.compute_angle_weights_1d(angles) if weight_angles
-                   else None)
-        geometry = geom.rotation_2d_geometry(angles, ln)
+
+        def build_tables():
+            return (geom.compute_angle_weights_1d(angles) if weight_angles
+                    else None, geom.rotation_2d_geometry(angles, ln), None)
+        tkey = (device.index, "2d", angles.dtype.str, angles.shape,
+                angles.tobytes(), ln, bool(weight_angles))
         key = ("2d", device.index, A, ln, g["lN"], g["padl"], pad_mode,
                padval_c, self.onlyreal, in_dtype, float(res), float(nm),
                float(lD))
@@ -87,10 +91,7 @@ class Backprop2D:
 
         with torch.cuda.device(device):
             self.plan = _get_plan(key, build_desc)
-            self.weights = (torch.from_numpy(np.ascontiguousarray(
-                weights, dtype=np.float64)).to(device)
-                if weights is not None else None)
-            self.geometry = torch.from_numpy(geometry).to(device)
+            self.weights, self.geometry, _ = _get_tables(tkey, build_tables)
             self.workspace = torch.empty(max(self.plan.workspace_bytes, 1),
                                          device=device, dtype=torch.uint8)
 

@@ -36,6 +36,12 @@ _PLAN_CACHE = collections.OrderedDict()
 _PLAN_CACHE_SIZE = 8
 _PLAN_LOCK = threading.Lock()
 
+# device copies of the FP64 per-angle tables (weights, geometry): building
+# the rotation geometry of 200 angles takes ~0.75 ms on the host, so repeated
+# calls with the same angles reuse them
+_TABLE_CACHE = collections.OrderedDict()
+_TABLE_CACHE_SIZE = 8
+
 
 def _torch():
     import torch
@@ -87,6 +93,30 @@ def _pad_mode(padding, padval):
             raise ValueError("`padval` must be 'edge' or a number")
         return _native.ODT_PAD_EDGE, 0j
     return _native.ODT_PAD_RAMP, complex(padval)
+
+
+def _get_tables(key, build):
+    """(weights, geometry, taxis) for `key`: `build()` returns the host
+    weights (or None), the geometry and the tilted axis; the device tensors
+    are cached and must not be modified."""
+    with _PLAN_LOCK:
+        hit = _TABLE_CACHE.get(key)
+        if hit is not None:
+            _TABLE_CACHE.move_to_end(key)
+            return hit
+    torch = _torch()
+    device = torch.device("cuda", key[0])
+    weights, geometry, taxis = build()
+    dw = (torch.from_numpy(np.ascontiguousarray(weights, dtype=np.float64))
+          .to(device) if weights is not None else None)
+    dg = torch.from_numpy(np.ascontiguousarray(geometry, dtype=np.float64)) \
+        .to(device)
+    hit = (dw, dg, taxis)
+    with _PLAN_LOCK:
+        _TABLE_CACHE[key] = hit
+        while len(_TABLE_CACHE) > _TABLE_CACHE_SIZE:
+            _TABLE_CACHE.popitem(last=False)
+    return hit
 
 
 def _get_plan(key, build_desc):
@@ -143,18 +173,28 @@ class Backprop3D:
         self.angles = angles
         self._res, self._nm, self._lD = float(res), float(nm), float(lD)
         self._support = None
+        user_weights = weights
         if tilted_axis is None:
             kind = _native.ODT_GEOM_Y_AXIS
-            if weights is None and weight_angles:
-                weights = geom.compute_angle_weights_1d(angles)
-            geometry = geom.rotation_y_geometry(angles, lnx, lnx)
-            taxis = None
+
+            def build_tables():
+                return (geom.compute_angle_weights_1d(angles)
+                        if weight_angles else None,
+                        geom.rotation_y_geometry(angles, lnx, lnx), None)
+            tkey = (device.index, "y", angles.dtype.str, angles.shape,
+                    angles.tobytes(), lnx, bool(weight_angles))
         else:
             kind = _native.ODT_GEOM_AFFINE3D
-            w, geometry, taxis = geom.tilted_geometry(
-                angles, tilted_axis, weight_angles, (lnx, lny, lnx))
-            if weights is None:
-                weights = w
+
+            def build_tables():
+                return geom.tilted_geometry(angles, tilted_axis,
+                                            weight_angles, (lnx, lny, lnx))
+            tkey = (device.index, "tilted", angles.dtype.str, angles.shape,
+                    angles.tobytes(), np.asarray(tilted_axis,
+                                                 dtype=np.float64).tobytes(),
+                    lnx, lny, bool(weight_angles))
+        with torch.cuda.device(device):
+            dweights, dgeometry, taxis = _get_tables(tkey, build_tables)
         in_dtype = {"complex64": _native.ODT_INPUT_C64,
                     "complex128": _native.ODT_INPUT_C128}[str(input_dtype)
                                                          .replace("torch.",
@@ -195,12 +235,11 @@ class Backprop3D:
 
         with torch.cuda.device(self.device):
             self.plan = _get_plan(key, build_desc)
-            self.weights = None
-            if weights is not None:
+            self.weights = dweights
+            if user_weights is not None:
                 self.weights = torch.from_numpy(np.ascontiguousarray(
-                    weights, dtype=np.float64)).to(self.device)
-            self.geometry = torch.from_numpy(np.ascontiguousarray(
-                geometry, dtype=np.float64)).to(self.device)
+                    user_weights, dtype=np.float64)).to(self.device)
+            self.geometry = dgeometry
             self.workspace = torch.empty(max(self.plan.workspace_bytes, 1),
                                          device=self.device,
                                          dtype=torch.uint8)
