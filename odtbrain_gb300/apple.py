@@ -135,11 +135,14 @@ def correct(f, res, nm, method="nn", mask=None, bg_shell_width=None,
     with torch.cuda.device(dev):
         if is_t:
             t = f.to(dev)
-            fr = (t.real if t.is_complex() else t).to(torch.float32)
+        elif np.asarray(f).dtype.kind in "fc":
+            # the array as it is (a plain copy, fast from pinned memory);
+            # the real part is taken on the device
+            t = torch.from_numpy(np.ascontiguousarray(np.asarray(f))).to(dev)
         else:
-            fr = torch.from_numpy(np.ascontiguousarray(
+            t = torch.from_numpy(np.ascontiguousarray(
                 np.real(np.asarray(f)), dtype=np.float32)).to(dev)
-        fr = fr.contiguous()
+        fr = (t.real if t.is_complex() else t).to(torch.float32).contiguous()
         mk = None
         if mask is not None:
             m = mask.to(dev) if _is_tensor(mask) else torch.from_numpy(
