@@ -694,7 +694,10 @@ __global__ void __launch_bounds__(R2_T * R2_T) k_rotate_plane(RotParams R, const
 // neighbouring outputs that share it.  Per angle, the FP32 coordinate
 // splits of the tile origin (three axes) and an "interior" flag (every tap
 // of every output in range: no in/out decisions, no mirroring) are computed
-// once per CTA in FP64 and kept in shared memory for a chunk of angles.
+// once per CTA in FP64 and kept in shared memory for a chunk of angles; the
+// splits are read from there at each use (broadcast loads) rather than held
+// in registers, which keeps the kernel at 64 registers and 4 CTAs per SM:
+// the tap loads are latency bound, and the extra warps hide more of it.
 constexpr int R3_Y = 32, R3_X = 8, R3_Z = 2;
 constexpr int R3_CHUNK = 64;
 constexpr int R3_KAHAN = 8;
@@ -732,7 +735,7 @@ __device__ __forceinline__ float eval_axis3(const AxisCoord3 &a, float d0, float
 }
 
 template <int ORDER, bool ONLYREAL>
-__global__ void __launch_bounds__(256, 3) k_rotate_3d(RotParams R, const float2 *__restrict__ slab,
+__global__ void __launch_bounds__(256, 4) k_rotate_3d(RotParams R, const float2 *__restrict__ slab,
                                                    const double *__restrict__ geo, void *volume, float2 *comp)
 {
     __shared__ AxisCoord3 srec[R3_CHUNK][3];
@@ -777,7 +780,7 @@ __global__ void __launch_bounds__(256, 3) k_rotate_3d(RotParams R, const float2 
         for (int aa = 0; aa < na; ++aa) {
             const int a = a0 + aa;
             const bool interior = sflag[aa][0] && sflag[aa][1] && sflag[aa][2];
-            const AxisCoord3 ax0 = srec[aa][0], ax1 = srec[aa][1], ax2 = srec[aa][2];
+            const AxisCoord3 *axp = srec[aa];
             const float2 *sa = slab + (size_t)a * aslab;
             const double *g = geo + 12 * (size_t)a;
 #pragma unroll
@@ -788,9 +791,9 @@ __global__ void __launch_bounds__(256, 3) k_rotate_3d(RotParams R, const float2 
                 const float d2 = (float)q;
                 int Ib[3];
                 float l[3];
-                l[0] = eval_axis3(ax0, d0, d1, d2, Ib[0]);
-                l[1] = eval_axis3(ax1, d0, d1, d2, Ib[1]);
-                l[2] = eval_axis3(ax2, d0, d1, d2, Ib[2]);
+                l[0] = eval_axis3(axp[0], d0, d1, d2, Ib[0]);
+                l[1] = eval_axis3(axp[1], d0, d1, d2, Ib[1]);
+                l[2] = eval_axis3(axp[2], d0, d1, d2, Ib[2]);
                 const double o2 = (double)z;
                 auto exact = [&](int i) {
                     return __dadd_rn(__dadd_rn(__dadd_rn(__ldg(g + 9 + i), __dmul_rn(__ldg(g + 3 * i), o0)),
