@@ -16,5 +16,6 @@ from ._prepare_sino import sinogram_as_radon, sinogram_as_rytov  # noqa: F401
 from ._translate_ri import odt_to_ri, opt_to_ri  # noqa: F401
 from . import apple  # noqa: F401
 from . import util  # noqa: F401
+from . import warn  # noqa: F401
 
 __version__ = "0.1.0"

@@ -250,6 +250,32 @@ def test_multibatch_kahan(odt, monkeypatch):
     assert_close(one, ref, what="single batch")
 
 
+def test_single_row_multibatch(odt, cuda_ready):
+    """A single-row plan (the fused column + row stage) over several angle
+    batches: the compensation carried across the resampling launches and
+    the per-batch z-boundary rows keep the result unchanged."""
+    import torch
+    from odtbrain_gb300._alg3d import Backprop3D
+    rng = np.random.default_rng(21)
+    A, nx = 40, 64
+    shape = (A, 1, nx)
+    sino = np.exp(1j * rng.normal(0, .4, shape) + rng.normal(0, .05, shape))
+    angles = np.sort(rng.uniform(0, 2 * np.pi, A))
+    ref = O.backpropagate_3d(sino, angles, res=3.0, nm=1.333,
+                             padding=(False, False))
+    d = torch.from_numpy(sino).to(cuda_ready)
+    one = Backprop3D(shape, angles, 3.0, 1.333, padding=(False, False),
+                     input_dtype="complex128", device=cuda_ready)
+    many = Backprop3D(shape, angles, 3.0, 1.333, padding=(False, False),
+                      input_dtype="complex128", device=cuda_ready,
+                      workspace_limit=256 << 10)
+    # five launches per batch: row spectra, boundary columns, fused
+    # column + row stage, geometry setup, resampling
+    assert one.launches_per_call == 5 and many.launches_per_call > 10
+    assert_close(one(d).cpu().numpy(), ref, what="single batch")
+    assert_close(many(d).cpu().numpy(), ref, what="multibatch")
+
+
 def test_torch_tensors_in_and_out(odt):
     import torch
     sino, angles = gauss_sino_3d()

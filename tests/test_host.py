@@ -268,3 +268,20 @@ def test_apple_gauss_weights_match_scipy():
         x[r + 4] = 1.0
         ref = ndi.gaussian_filter1d(x, sigma, mode="constant", truncate=4.0)
         np.testing.assert_array_equal(ref[4:4 + 2 * r + 1], w[::-1])
+
+
+def test_public_names_match_the_reference():
+    """The package exposes the reference's public names
+    (odtbrain/__init__.py:3-15) for the paths it implements; the 2D
+    Fourier-mapping and direct-integration algorithms are not built."""
+    for name in ("backpropagate_2d", "backpropagate_3d",
+                 "backpropagate_3d_tilted", "sinogram_as_radon",
+                 "sinogram_as_rytov", "odt_to_ri", "opt_to_ri", "apple",
+                 "util", "warn", "__version__"):
+        assert hasattr(odt, name), name
+    for name in ("apple_core_3d", "correct", "spillover_region",
+                 "ellipsoid_shell", "count_to_half"):
+        assert callable(getattr(odt.apple, name)), name
+    assert callable(odt.util.compute_angle_weights_1d)
+    assert issubclass(odt.warn.DataUndersampledWarning, UserWarning)
+    assert issubclass(odt.warn.ImplementationAmbiguousWarning, UserWarning)
