@@ -63,6 +63,22 @@ def test_2d_against_oracle_larger(cuda_ready):
         assert _rel(got, ref) < REL, kw
 
 
+@pytest.mark.parametrize("N,A", [(1000, 3), (500, 7), (21, 9)])
+def test_2d_line_lengths(cuda_ready, N, A):
+    """Padded line lengths 4096, 2048 and 64: every thread layout of the
+    fused single-row stage (one 512-thread line per group, one 256-thread
+    line, 32 lines of 8 threads) against the oracle."""
+    import odtbrain_gb300 as odt
+    rng = np.random.default_rng(N)
+    angles = np.sort(rng.uniform(0, 2 * np.pi, A))
+    x = np.linspace(-1, 1, N)
+    sino = (np.exp(-x ** 2 / 0.1)[None, :] * rng.uniform(0.5, 2, (A, 1))
+            + 0.02 * rng.normal(size=(A, N))) * 1j
+    got = odt.backpropagate_2d(sino, angles, 3.0, 1.333)
+    ref = O.backpropagate_2d(sino, angles, 3.0, 1.333)
+    assert _rel(got, ref) < REL
+
+
 def test_2d_torch_and_counters(cuda_ready):
     import torch
     import odtbrain_gb300 as odt
