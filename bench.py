@@ -134,6 +134,8 @@ def parse_args():
     ap.add_argument("--ncu-rotate-case", action="store_true",
                     help="16 angles in one batch (one resampling launch) "
                     "for ncu captures of the resampling kernel")
+    ap.add_argument("--ncu-n", type=int, default=128,
+                    help="volume edge of the apple profiling case")
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: the workload's plane and volume "
                          "size with 8 angles and the save_memory workspace, "
@@ -941,9 +943,10 @@ def run_apple(args):
     from odtbrain_gb300._alg3d import Backprop3D
     w = WORKLOAD
     if args.ncu_case:
-        # profiling case: a 128^3 volume of smooth blobs (no
-        # reconstruction before it), three iterations
-        g = torch.arange(128, device=dev, dtype=torch.float32) - 64.0
+        # profiling case: an n^3 volume of smooth blobs (no reconstruction
+        # before it; n = --ncu-n, 128 by default), three iterations
+        nn = args.ncu_n
+        g = torch.arange(nn, device=dev, dtype=torch.float32) - nn / 2
         z, y, x = torch.meshgrid(g, g, g, indexing="ij")
         vol = (torch.exp(-(x * x + y * y + z * z) / 800.0)
                + 0.3 * torch.exp(-((x - 20) ** 2 + y * y + z * z) / 60.0)
@@ -1022,11 +1025,14 @@ def run_apple(args):
                        "l2": "256 MiB flush before every timed step"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": profile_traffic("apple_iteration",
+                                                    N * iters),
                          "note": "28 B per voxel-iteration (volume read + "
                                  "write, original spectrum and envelope "
-                                 "read); the five FFT passes per iteration "
-                                 "move about 85 B"},
+                                 "read); traffic: DRAM bytes of the "
+                                 "iterations' launches (ncu, 256^3), "
+                                 "71.6 B per voxel-iteration"},
             "clocks": clk, "gpu_launches_per_iteration": 5,
             "step_ms": step_ms,
             "e2e": {"value": N * iters / (e2e_ms / 1e3), "unit": unit,
