@@ -102,14 +102,19 @@ def test_angle_gain_adjoint_matches_dense_autograd(torch_dev, order):
 
 
 @pytest.mark.parametrize("padval", ["edge", 0.7])
-def test_adjoint_dot_product_identity(torch_dev, padval):
+@pytest.mark.parametrize("ny,padding", [(40, (True, True)),
+                                        (1, (True, True)),
+                                        (1, (False, False))])
+def test_adjoint_dot_product_identity(torch_dev, padval, ny, padding):
+    """Also for one detector row: padded (pitch-1 slab, one output per
+    thread in the resampling) and unpadded (the fused single-row stage)."""
     torch, dev = torch_dev
     from odtbrain_gb300._alg3d import Backprop3D
     rng = np.random.default_rng(9)
-    A, ny, nx = 14, 40, 48
+    A, nx = 14, 48
     angles = np.sort(rng.uniform(0, 2 * np.pi, A))
     rec = Backprop3D((A, ny, nx), angles, 2.5, 1.34, lD=1.0, padval=padval,
-                     input_dtype="complex64", device=dev)
+                     padding=padding, input_dtype="complex64", device=dev)
     d = torch.tensor((rng.normal(size=(A, ny, nx)) +
                       1j * rng.normal(size=(A, ny, nx))).astype(np.complex64),
                      device=dev)
