@@ -59,9 +59,9 @@ struct StageParams {
     int kx_zero_lo, kx_zero_hi;  // spectrum columns in [lo, hi) are all zero
                                  // (outside the |k| < km disc)
     float bx_ca, bx_cb;  // x-prefilter boundary solve (n = nx)
-    float by_ca, by_cb;  // y-prefilter boundary solve (n = ny)
-    int ypitch;          // slab [a][z][x][y]: y pitch (ny rounded up to a
-                         // multiple of 32)
+    float by_ca, by_cb;  // y-prefilter boundary solve (n = ny; zero for ny = 1)
+    int ypitch;          // slab [a][z][x][y]: y pitch (yaxis_slab_pitch:
+                         // ny rounded up to a multiple of 32, 1 for ny == 1)
     int col_slots;       // resident CTAs of the column stage on the device
     float zshift;        // plane p sits at z = p - nz/2 + zshift
     FilterTables tab;
