@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_adj_rows(StageParams P, L line
     const int n = line.size();  // lNx
     const int xs = xslots<false>(n);
     float2 *buf0 = smem, *buf1 = smem + LPC * xs, *tw = smem + 2 * LPC * xs;
-    float2 *red = tw + n;  // [LPC][2] boundary sums
+    float2 *red = tw + tw_slots(n);  // [LPC][2] boundary sums
     copy_twiddles<L>(tw, P.tab.twx, n);
     const int l = threadIdx.x / L::TPL, j = threadIdx.x % L::TPL;
     const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl;
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_columns(StageParams P, L li
     const int n = line.size();  // lNy
     const int xs = xslots<true>(n);
     float2 *buf0 = smem, *buf1 = smem + KX * xs, *tw = smem + 2 * KX * xs;
-    float2 *stp = tw + n;  // [n][KX]
+    float2 *stp = tw + tw_slots(n);  // [n][KX]
     copy_twiddles<L>(tw, P.tab.twy, n);
     const int c = threadIdx.x % KX, j = threadIdx.x / KX;
     const int kx = blockIdx.x * KX + c;
@@ -363,12 +363,12 @@ constexpr int kAdjPlanesPerBlock = 16;
 template <class L>
 static size_t smem_adj_rows(int n)
 {
-    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + n + 2 * Cfg<L>::LPC) * sizeof(float2);
+    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + tw_slots(n) + 2 * Cfg<L>::LPC) * sizeof(float2);
 }
 template <class L>
 static size_t smem_adj_cols(int n)
 {
-    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + Cfg<L>::KX * n + n) * sizeof(float2);
+    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + Cfg<L>::KX * n + tw_slots(n)) * sizeof(float2);
 }
 
 template <class L>

@@ -756,12 +756,12 @@ __global__ void k_sh_hist(AP P, int it)
 template <class L>
 size_t smem_x(int n)
 {
-    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + n) * sizeof(float2);
+    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + tw_slots(n)) * sizeof(float2);
 }
 template <class L>
 size_t smem_s(int n)
 {
-    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + n) * sizeof(float2);
+    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + tw_slots(n)) * sizeof(float2);
 }
 
 cudaError_t launch_x(const AP &P, int mode, int it, cudaStream_t s)

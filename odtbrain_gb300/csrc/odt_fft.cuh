@@ -144,6 +144,16 @@ __host__ __device__ constexpr int xslots(int n)
 }
 constexpr int ipow8(int k) { return k == 0 ? 1 : 8 * ipow8(k - 1); }
 
+// Shared-memory twiddle region of a line: the plain table exp(-2 pi i m / N)
+// (N entries), then for power-of-two lines the twiddles of the second
+// radix-8 pass (Ns = 8) stored contiguously per thread class jm: entry
+// jm*7 + r-1 = exp(-2 pi i r jm / 64), the plain table's entry r*jm*N/64.
+// Read from the plain table, the 8 distinct twiddles a warp needs in that
+// pass lie on one or two banks (4- to 8-way conflicts); read from this
+// table they lie on distinct banks.
+constexpr int TW_P1 = 56;
+__host__ __device__ constexpr int tw_slots(int n) { return n + TW_P1; }
+
 // Power-of-two line, 64 <= N <= 4096.
 template <int N_>
 struct Pow2Line {
@@ -170,7 +180,12 @@ struct Pow2Line {
         int Ns = 1;
 #pragma unroll
         for (int pass = 0; pass < P8; ++pass) {
-            if (pass > 0) {
+            if (pass == 1) {
+                const float2 *t1 = tw + N + (j & 7) * 7;
+#pragma unroll
+                for (int r = 1; r < 8; ++r)
+                    v[r] = cmul(v[r], twid<DIR>(t1, r - 1));
+            } else if (pass > 1) {
                 const int jm = j & (Ns - 1);
                 const int stp = jm * (N / (Ns * 8));
 #pragma unroll

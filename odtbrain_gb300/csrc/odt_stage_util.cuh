@@ -73,11 +73,18 @@ __device__ __forceinline__ float2 padded_sample(const StageParams &P, const void
     return ramp(colval(nx - 1), P.padval, padxr - 1 - (xs - nx), padxr);
 }
 
+// The twiddle region (tw_slots(n) entries) from the plain table `src`.
 template <class L>
 __device__ __forceinline__ void copy_twiddles(float2 *dst, const float2 *src, int n)
 {
     for (int i = threadIdx.x; i < n; i += blockDim.x)
         dst[i] = src[i];
+    if (!std::is_same<L, GenericLine>::value) {
+        for (int i = threadIdx.x; i < TW_P1; i += blockDim.x) {
+            const int jm = i / 7, r = i - 7 * jm + 1;
+            dst[n + i] = src[r * jm * (n / 64)];
+        }
+    }
 }
 
 
@@ -125,12 +132,13 @@ struct Cfg<GenericLine> {
 template <class L>
 inline size_t smem_rows(int n)
 {
-    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + n + 4 * Cfg<L>::LPC) * sizeof(float2);
+    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + tw_slots(n) + 4 * Cfg<L>::LPC) * sizeof(float2);
 }
 template <class L>
 inline size_t smem_cols(int n)
 {
-    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + Cfg<L>::KX * n + n + 4 * Cfg<L>::KX) * sizeof(float2);
+    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + Cfg<L>::KX * n + tw_slots(n) + 4 * Cfg<L>::KX) *
+           sizeof(float2);
 }
 
 // Calls fn(line) with the line type for length n.

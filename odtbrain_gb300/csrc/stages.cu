@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(KX * L::TPL) k_columns_boundary(StageParams P,
     extern __shared__ float2 smem[];
     const int n = line.size();
     const int ls = xslots<true>(n);
-    float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls, *edge = tw + n;
+    float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls, *edge = tw + tw_slots(n);
     copy_twiddles<L>(tw, P.tab.twy, n);
     const int c = threadIdx.x % KX, j = threadIdx.x / KX;
     const int kx = blockIdx.x * KX + c;
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
     const int n = line.size();  // lNy
     const int ls = xslots<true>(n);
     float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls;
-    float2 *edge = tw + n;           // [KX][4]
+    float2 *edge = tw + tw_slots(n); // [KX][4]
     float2 *stp = edge + 4 * KX;     // [n][KX] propagator step per element
     copy_twiddles<L>(tw, P.tab.twy, n);
     const int c = threadIdx.x % KX, j = threadIdx.x / KX;
