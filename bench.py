@@ -12,6 +12,17 @@ random-ellipsoid phantom (3-12 ellipsoids, semi-axes 8-60 px, n in
 padfac 1.75 (512x512 padded FFTs), intp_order=2, output 256^3 complex64.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                  [--config NAME]
+
+--config selects another workload (one JSON line each, same keys):
+  c1     the same reconstruction at A=60, 64x64 (the CPU-runnable case)
+  c3     backpropagate_3d_tilted, A=220, 200x200, axis 0.2 rad from y
+  c4     forward + vector-Jacobian product through the autograd wrapper
+  c5     the learned wedge filter against the plain one
+  rytov  sinogram_as_rytov of the headline sinogram's field
+  apple  apple.correct of the headline reconstruction
+  ri     odt_to_ri of a 256^3 volume (opt_to_ri beside it)
+  bpp2d  backpropagate_2d, A=400 x 512
 
 value   device-resident throughput (sinogram already in HBM; the prepared
         plan's kernels timed with CUDA events on their stream, L2 flushed
