@@ -439,6 +439,21 @@ def run_reference_apple(args):
         1)), flush=True)
 
 
+def replica_throughput(units_per_rank, local_ms, world, device=None):
+    """Whole-job throughput of `world` independent replicas, each having
+    processed `units_per_rank` units in `local_ms`: the job takes as long
+    as its slowest rank (max over ranks, one all-reduce), and the units of
+    all ranks count.  Returns (units/s, job ms)."""
+    t = float(local_ms)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        x = torch.tensor([t], dtype=torch.float64, device=device)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        t = float(x.item())
+    return units_per_rank * world / (t / 1e3), t
+
+
 # --------------------------------------------------------------- GPU side
 def run_ours(args):
     import torch
@@ -492,11 +507,7 @@ def run_ours(args):
     clk = clocks.stop()
     rec.check()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    _, total_ms = replica_throughput(U * args.steps, sum(step_ms), world, dev)
     ms_per_step = total_ms / args.steps
     value = U * world / (ms_per_step / 1e3)
 
@@ -594,12 +605,10 @@ def run_ours(args):
         t0 = time.perf_counter()
         out = api(host_np, angles, w["res"], w["nm"], **kw)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_s = statistics.mean(e2e_t)
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": U * world / e2e_s, "unit": UNIT,
+    e2e_value, e2e_ms = replica_throughput(U, statistics.mean(e2e_t) * 1e3,
+                                           world, dev)
+    e2e_s = e2e_ms / 1e3
+    e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": int(host.numel() * host.element_size()),
            "d2h_bytes_per_step": int(out.nbytes),
            "ms_per_step": e2e_s * 1e3}
