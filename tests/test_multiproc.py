@@ -71,3 +71,11 @@ def test_reference_arm_under_torchrun_prints_one_line():
     assert len(lines) == 1, r.stdout
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    for key in ("metric", "unit", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "config"):
+        assert key in d, key
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference")
+    assert cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"],
+                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
