@@ -29,13 +29,21 @@ value   device-resident throughput (sinogram already in HBM; the prepared
         between steps by a 256 MiB write outside the timed events)
 e2e     the same metric through the public API ``backpropagate_3d`` with a
         pinned host sinogram in and a host volume out (H2D + D2H inside)
-roofline  the dominant kernel stage, timed live with CUDA events around
-        each of its launches, against MEASURED_PEAKS.json's HBM bandwidth;
-        for the FFT stages (FP32-issue bound, HBM well below its rate) also
-        their FP32 rate against the nominal FP32 peak ("fp32")
-roofline_rotate  the resampling/accumulation stage against HBM
-cpu_baseline  the FP64 oracle port on this host's cores, on a bounded
-        sample of the same workload (a few angles)
+roofline  stage (b), the propagator + inverse 2D FFT (its two kernels,
+        the largest share of the step), timed live with CUDA events around
+        each launch: algorithmic bytes (spectra read + slabs written) over
+        the two kernels' summed time, against MEASURED_PEAKS.json's HBM
+        bandwidth, and their FP32 rate against the nominal FP32 peak
+roofline_rotate  stage (c), resampling + accumulation, against HBM
+roofline_step  every stage's algorithmic bytes over the whole step
+accuracy  rel-L2 and max error of the timed volume against the FP64 oracle
+        run over the whole workload (all angles)
+cpu_baseline  that FP64 oracle run (the port of the reference's CPU path)
+        on this host's cores
+c3, c4, c5  (default run) the tilted, differentiation and learned-filter
+        configurations measured in the same run after the headline (c3 with
+        its own full-size oracle check, c5 over 200 held-out phantoms);
+        --headline-only skips them
 With --gpus N > 1 (torchrun), every rank runs an independent replica of the
 workload (the path has no exchange step); value sums the ranks' updates
 over the slowest rank's time.
@@ -127,7 +135,6 @@ WORKLOADS["bpp2d"] = dict(
          "to 2048 (2.1x rule, linear ramp to 0), cubic-spline rotation")
 WORKLOAD = WORKLOADS["c2"]
 WORKLOAD_NAME = WORKLOAD["name"]
-CPU_SAMPLE_ANGLES = 4
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -140,6 +147,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true",
                     help="skip the CPU oracle sample (and the rel-L2 check)")
     ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--headline-only", action="store_true",
+                    help="default configuration only: skip the tilted, "
+                    "differentiation and learned-filter sub-results")
     ap.add_argument("--config", choices=sorted(WORKLOADS), default="c2",
                     help="workload (default c2, the headline configuration)")
     ap.add_argument("--ncu-rotate-case", action="store_true",
@@ -154,9 +164,9 @@ def parse_args():
     return ap.parse_args()
 
 
-def make_workload():
+def make_workload(w=None):
     from sino_gen import ellipsoid_phantom_sinogram
-    w = WORKLOAD
+    w = WORKLOAD if w is None else w
     sino, angles = ellipsoid_phantom_sinogram(
         w["n"], w["A"], seed=w["seed"], count_range=w["count_range"],
         semi_range=w["semi_range"], res=w["res"], nm=w["nm"],
@@ -280,34 +290,31 @@ def profile_traffic(stage, units_per_launch):
 
 
 # --------------------------------------------------------------- CPU side
-def cpu_sample(sino, angles, subset):
-    """Time the FP64 oracle on a sub-problem of `subset` angles with all host
-    threads; return (seconds, volume, cores)."""
+def oracle_full(sino, angles, w):
+    """The FP64 oracle over the whole workload (every angle), with all host
+    threads; returns (seconds, volume, cores).  The propagator table of the
+    reference's default path is built inside the timed call, as the
+    reference builds it inside its own."""
     from oracle import odt_oracle
     cores = os.cpu_count() or 1
-    w = WORKLOAD
-    s = sino[subset].astype(np.complex128)
-    a = angles[subset]
-    # one-time setup (the propagator table) outside the timed sample
-    cache = {}
-    odt_oracle.backpropagate_3d(s[:1], a[:1], w["res"], w["nm"],
-                                lD=w["lD"], padfac=w["padfac"],
-                                intp_order=w["intp_order"], nthreads=cores,
-                                fft_workers=cores, angle_subset=[],
-                                weight_angles=False, cache=cache)
+    s = sino.astype(np.complex128)
+    kw = dict(lD=w["lD"], padfac=w["padfac"], intp_order=w["intp_order"],
+              nthreads=cores, fft_workers=cores)
     t0 = time.perf_counter()
     if w["axis"] is None:
-        vol = odt_oracle.backpropagate_3d(s, a, w["res"], w["nm"],
-                                          lD=w["lD"], padfac=w["padfac"],
-                                          intp_order=w["intp_order"],
-                                          nthreads=cores, fft_workers=cores,
-                                          cache=cache)
+        vol = odt_oracle.backpropagate_3d(s, angles, w["res"], w["nm"], **kw)
     else:
         vol = odt_oracle.backpropagate_3d_tilted(
-            s, a, w["res"], w["nm"], lD=w["lD"], tilted_axis=w["axis"],
-            padfac=w["padfac"], intp_order=w["intp_order"], nthreads=cores,
-            fft_workers=cores, cache=cache)
+            s, angles, w["res"], w["nm"], tilted_axis=w["axis"], **kw)
     return time.perf_counter() - t0, vol, cores
+
+
+def rel_errors(got, ref):
+    """rel-L2 and max |error| / max |ref| of a GPU volume against the FP64
+    oracle's."""
+    got = np.asarray(got)
+    return (float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+            float(np.abs(got - ref).max() / np.abs(ref).max()))
 
 
 def run_reference(args):
@@ -467,7 +474,6 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=dev)
     from odtbrain_gb300 import build as native_build
     native_build.build()
-    import odtbrain_gb300 as odt
     from odtbrain_gb300._alg3d import Backprop3D
 
     w = WORKLOAD
@@ -529,57 +535,16 @@ def run_ours(args):
     sm_diff = float((vol_sm - vol).abs().max() / vol.abs().max())
     del rec_sm, vol_sm
 
-    # per-stage live timing (event pair around every launch)
+    # per-stage live timing (event pair around every launch, the stages
+    # serialised on one stream)
     flush.zero_()
     stages = rec.timed(dsino, out=vol)
-    dom = max(stages, key=lambda k: stages[k]["ms"])
-    ds = stages[dom]
-    per_launch_bytes = ds["bytes"] / ds["launches"]
-    per_launch_s = ds["ms"] / ds["launches"] / 1e3
     peak, peak_kind = measured_peaks()
-    achieved = per_launch_bytes / per_launch_s / 1e9
-    # units of the captured launches: planes for the FFT stages, voxel-angle
-    # updates for the resampling
-    nz_ = n
-    units = {"columns_propagate": A * nz_ / max(1, stages["columns_propagate"]["launches"]),
-             "rows_inverse": A * nz_ / max(1, stages["rows_inverse"]["launches"]),
-             "rotate": U / max(1, stages["rotate"]["launches"]),
-             "rows_forward": None}
-    rot_key = "rotate" if w["axis"] is None else "rotate_tilted"
-    traffic = (profile_traffic(rot_key if dom == "rotate" else dom, units[dom])
-               if units.get(dom) else None)
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved,
-                "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
-                if peak_kind == "measured" else "fallback 6.8 TB/s",
-                "traffic": traffic,
-                "algorithmic_bytes_per_launch": per_launch_bytes,
-                "launch_ms": per_launch_s * 1e3}
-    # the FFT stages are FP32-issue bound (their HBM traffic is the chunk
-    # buffer between them, well below the HBM rate): their compute roofline, algorithmic flops 5 N log2 N per
-    # complex N-point transform plus 6 per propagator multiply, against the
-    # nominal FP32 rate 152 SMs x 128 lanes x 2 flops at the median SM clock
-    # sampled during the timed steps
+    peak_source = ("measured (MEASURED_PEAKS.json hbm_gbs)"
+                   if peak_kind == "measured" else "fallback 6.8 TB/s")
     sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    fl = stage_flops(rec, A)
-    fp32 = {k: {"tflops": fl[k] / (stages[k]["ms"] / 1e3) / 1e12,
-                "frac": fl[k] / (stages[k]["ms"] / 1e3) / 1e12 / fp32_peak,
-                "algorithmic_gflop": fl[k] / 1e9}
-            for k in fl if stages.get(k, {}).get("ms")}
-    if dom in fp32:
-        roofline["fp32"] = dict(fp32[dom], peak_tflops=fp32_peak,
-                                peak_source="nominal at %.0f MHz" % sm_mhz)
-    # rotate-accumulate against HBM: slab read + volume traffic
-    rs = stages["rotate"]
-    rot_achieved = rs["bytes"] / (rs["ms"] / 1e3) / 1e9
-    roofline_rotate = {"bound": "hbm", "kernel": "rotate",
-                       "achieved": rot_achieved, "peak": peak, "unit": "GB/s",
-                       "frac": rot_achieved / peak,
-                       "traffic": profile_traffic(rot_key, units["rotate"]),
-                       "algorithmic_bytes_per_launch":
-                           rs["bytes"] / rs["launches"],
-                       "launch_ms": rs["ms"] / rs["launches"]}
+    roofline, roofline_rotate, fp32, whole = stage_rooflines(
+        rec, stages, A, n, w, peak, peak_source, sm_mhz, ms_per_step)
     stage_summary = {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
                          "share": round(v["ms"] / sum(x["ms"] for x in
                                                       stages.values()), 4),
@@ -588,6 +553,159 @@ def run_ours(args):
                      for k, v in stages.items()}
 
     # end to end through the public API, host buffers
+    e2e = public_e2e(w, host, angles, U, args, world, dev, barrier)
+    got_vol = vol.cpu().numpy() if rank == 0 else None
+
+    line = None
+    if rank == 0:
+        extras = {}
+        if not args.headline_only and args.config == "c2":
+            # the other configurations, measured in this run after the
+            # headline's timed region
+            extras["c3"] = measure_recon_config(WORKLOADS["c3"], args, dev,
+                                                flush, stream)
+            extras["c4"] = measure_diff(args, dev)
+            extras["c5"] = measure_learned(args, dev, n_eval=200)
+        cpu = None
+        accuracy = None
+        if not args.no_cpu_baseline:
+            t_cpu, ref, cores = oracle_full(sino, angles, w)
+            cpu = {"value": U / t_cpu, "unit": UNIT, "cores": cores,
+                   "kind": "port",
+                   "sample": "the whole workload (all %d angles, %d x %d^3 "
+                             "updates), FP64 oracle port (scipy.fft + OpenMP "
+                             "C spline resampling), %.1f s"
+                             % (A, A, n, t_cpu)}
+            rel, mx = rel_errors(got_vol, ref)
+            accuracy = {"rel_l2": rel, "max_abs_rel": mx,
+                        "vs": "FP64 oracle, full A=%d (the measured "
+                              "configuration)" % A}
+            del ref
+            if "c3" in extras:
+                c3 = extras["c3"]
+                t3, ref3, _ = oracle_full(c3.pop("_sino"), c3.pop("_angles"),
+                                          WORKLOADS["c3"])
+                rel3, mx3 = rel_errors(c3.pop("_volume"), ref3)
+                c3["accuracy"] = {"rel_l2": rel3, "max_abs_rel": mx3,
+                                  "vs": "FP64 oracle, full A=%d"
+                                  % WORKLOADS["c3"]["A"]}
+                c3["cpu_oracle_s"] = t3
+                del ref3
+        for v in extras.values():
+            for k in [k for k in v if k.startswith("_")]:
+                v.pop(k)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 (complex64)", "data": "synthetic",
+            "config": {"workload": WORKLOAD_NAME, "A": A, "n": n,
+                       "padded_fft": rec.padding_geometry["lNx"], "intp_order": w["intp_order"],
+                       "save_memory": False,
+                       "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "e2e": e2e,
+            "gpu_launches": rec.launches_per_call * args.steps,
+            "roofline": roofline,
+            "roofline_rotate": roofline_rotate,
+            "roofline_step": whole,
+            "fp32_stages": fp32,
+            "stages": stage_summary,
+            "save_memory_ms_per_step": sm_ms,
+            "save_memory_max_rel_diff": sm_diff,
+            "accuracy": accuracy,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "step_ms": [round(x, 3) for x in step_ms],
+        }
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def stage_rooflines(rec, stages, A, n, w, peak, peak_source, sm_mhz,
+                    ms_per_step):
+    """Rooflines from the per-stage CUDA-event times of one serialised
+    execution.
+
+    roofline: stage (b), the propagator + inverse FFT (k_columns_propagate
+      + k_rows_inverse), the largest share of the step.  Algorithmic bytes
+      (per reconstruction): the filtered spectra read, A*lNy*lNx*8, plus the
+      cropped slabs written, A*nz*ny*nx*8; achieved = those bytes over the
+      two kernels' summed time; also their FP32 rate (5 N log2 N flops per
+      transform, 6 per propagator multiply) against the nominal FP32 peak.
+    roofline_rotate: stage (c), slab read + volume traffic over the
+      resampling time.
+    whole: every stage's algorithmic bytes over the pipelined step time."""
+    g = rec.padding_geometry
+    lNy, lNx = g["lNy"], g["lNx"]
+    _A, ny, nx = rec.shape
+    nz = nx
+    U = float(A) * nz * ny * nx
+    col, row = stages["columns_propagate"], stages["rows_inverse"]
+    b_bytes = float(A) * lNy * lNx * 8 + U * 8
+    b_ms = col["ms"] + row["ms"]
+    b_launches = col["launches"] + row["launches"]
+    planes = A * nz
+    tc = profile_traffic("columns_propagate", planes)
+    tr = profile_traffic("rows_inverse", planes)
+    b_traffic = (tc + tr) if tc is not None and tr is not None else None
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fl = stage_flops(rec, A)
+    fp32 = {k: {"tflops": fl[k] / (stages[k]["ms"] / 1e3) / 1e12,
+                "frac": fl[k] / (stages[k]["ms"] / 1e3) / 1e12 / fp32_peak,
+                "algorithmic_gflop": fl[k] / 1e9}
+            for k in fl if stages.get(k, {}).get("ms")}
+    b_flops = sum(fl.values())
+    achieved = b_bytes / (b_ms / 1e3) / 1e9
+    roofline = {
+        "bound": "hbm", "kernel": "stage (b): k_columns_propagate + "
+        "k_rows_inverse (propagator, inverse 2D FFT, crop)",
+        "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_source,
+        "traffic": b_traffic,
+        "traffic_note": "DRAM bytes of both kernels per reconstruction, "
+                        "scaled by planes from one ncu capture each "
+                        "(profiles/dram_traffic.md); includes the chunk "
+                        "buffer between them",
+        "algorithmic_bytes": b_bytes, "ms": b_ms, "launches": b_launches,
+        "fp32": {"tflops": b_flops / (b_ms / 1e3) / 1e12,
+                 "frac": b_flops / (b_ms / 1e3) / 1e12 / fp32_peak,
+                 "algorithmic_gflop": b_flops / 1e9,
+                 "peak_tflops": fp32_peak,
+                 "peak_source": "nominal at %.0f MHz" % sm_mhz}}
+    rs = stages["rotate"]
+    rot_achieved = rs["bytes"] / (rs["ms"] / 1e3) / 1e9
+    rot_key = "rotate" if w["axis"] is None else "rotate_tilted"
+    roofline_rotate = {"bound": "hbm", "kernel": "stage (c): resampling and "
+                       "accumulation", "achieved": rot_achieved,
+                       "peak": peak, "unit": "GB/s",
+                       "frac": rot_achieved / peak,
+                       "peak_source": peak_source,
+                       "traffic": profile_traffic(rot_key, U),
+                       "algorithmic_bytes": rs["bytes"], "ms": rs["ms"],
+                       "launches": rs["launches"],
+                       "algorithmic_bytes_per_launch":
+                           rs["bytes"] / rs["launches"],
+                       "launch_ms": rs["ms"] / rs["launches"]}
+    a_bytes = stages["rows_forward"]["bytes"]
+    step_bytes = a_bytes + b_bytes + rs["bytes"]
+    whole = {"algorithmic_bytes": step_bytes, "ms": ms_per_step,
+             "achieved": step_bytes / (ms_per_step / 1e3) / 1e9,
+             "peak": peak, "unit": "GB/s",
+             "frac": step_bytes / (ms_per_step / 1e3) / 1e9 / peak,
+             "note": "stages (a)+(b)+(c) algorithmic bytes over the "
+                     "pipelined step time"}
+    return roofline, roofline_rotate, fp32, whole
+
+
+def public_e2e(w, host, angles, U, args, world, dev, barrier):
+    """The metric through the public API with host buffers: pinned host
+    sinogram in, NumPy volume out, copies inside the timed region."""
+    import torch
+    import odtbrain_gb300 as odt
     e2e_steps = args.e2e_steps or max(3, min(args.steps, 5))
     kw = dict(lD=w["lD"], padfac=w["padfac"], intp_order=w["intp_order"],
               dtype=np.float32)
@@ -607,65 +725,42 @@ def run_ours(args):
         e2e_t.append(time.perf_counter() - t0)
     e2e_value, e2e_ms = replica_throughput(U, statistics.mean(e2e_t) * 1e3,
                                            world, dev)
-    e2e_s = e2e_ms / 1e3
-    e2e = {"value": e2e_value, "unit": UNIT,
-           "h2d_bytes_per_step": int(host.numel() * host.element_size()),
-           "d2h_bytes_per_step": int(out.nbytes),
-           "ms_per_step": e2e_s * 1e3}
+    return {"value": e2e_value, "unit": UNIT,
+            "h2d_bytes_per_step": int(host.numel() * host.element_size()),
+            "d2h_bytes_per_step": int(out.nbytes),
+            "ms_per_step": e2e_ms}
 
-    line = None
-    if rank == 0:
-        cpu = None
-        accuracy = None
-        if not args.no_cpu_baseline:
-            # not symmetric modulo pi (a symmetric set makes the angle
-            # weights 0/0, in the reference as here)
-            subset = [int(A * f) for f in (0.0, 0.185, 0.455, 0.715)]
-            t_cpu, ref, cores = cpu_sample(sino, angles, subset)
-            cpu = {"value": updates(len(subset), n) / t_cpu, "unit": UNIT,
-                   "cores": cores, "kind": "port",
-                   "sample": "%d of the %d angles as a %d-angle problem "
-                             "(%d x %d^3 updates), FP64 oracle, %.1f s"
-                             % (len(subset), A, len(subset), len(subset), n,
-                                t_cpu)}
-            sub = Backprop3D((len(subset), n, n), angles[subset], w["res"],
-                             w["nm"], lD=w["lD"], tilted_axis=w["axis"],
-                             padfac=w["padfac"],
-                             intp_order=w["intp_order"],
-                             input_dtype="complex64", device=dev)
-            got = sub(dsino[subset].contiguous()).cpu().numpy()
-            rel = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
-            mx = float(np.abs(got - ref).max() / np.abs(ref).max())
-            accuracy = {"rel_l2": rel, "max_abs_rel": mx,
-                        "vs": "FP64 oracle, same %d-angle sub-problem"
-                        % len(subset)}
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT,
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_per_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp32 (complex64)", "data": "synthetic",
-            "config": {"workload": WORKLOAD_NAME, "A": A, "n": n,
-                       "padded_fft": rec.padding_geometry["lNx"], "intp_order": w["intp_order"],
-                       "save_memory": False,
-                       "l2": "flushed between steps (256 MiB write)",
-                       "parallelism": "replicas" if world > 1 else "1 GPU"},
-            "e2e": e2e,
-            "gpu_launches": rec.launches_per_call * args.steps,
-            "roofline": roofline,
-            "roofline_rotate": roofline_rotate,
-            "fp32_stages": fp32,
-            "stages": stage_summary,
-            "save_memory_ms_per_step": sm_ms,
-            "save_memory_max_rel_diff": sm_diff,
-            "accuracy": accuracy,
-            "cpu_baseline": cpu,
-            "clocks": clk,
-            "step_ms": [round(x, 3) for x in step_ms],
-        }
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+
+def measure_recon_config(w, args, dev, flush, stream):
+    """Device-resident and end-to-end timing of another reconstruction
+    workload (one GPU), with its volume kept for the accuracy check."""
+    import torch
+    from odtbrain_gb300._alg3d import Backprop3D
+    sino, angles = make_workload(w)
+    A, n = w["A"], w["n"]
+    U = updates(A, n)
+    host = torch.from_numpy(sino).pin_memory()
+    dsino = host.to(dev)
+    rec = Backprop3D(tuple(sino.shape), angles, w["res"], w["nm"], lD=w["lD"],
+                     tilted_axis=w["axis"], padfac=w["padfac"],
+                     intp_order=w["intp_order"], input_dtype="complex64",
+                     device=dev)
+    vol = torch.empty(rec.volume_shape(), device=dev, dtype=torch.complex64)
+    ms, step_ms = _timed(lambda: rec(dsino, out=vol, check=False),
+                         args.steps, args.warmup, flush, stream)
+    rec.check()
+    flush.zero_()
+    stages = rec.timed(dsino, out=vol)
+    got = vol.cpu().numpy()
+    e2e = public_e2e(w, host, angles, U, args, 1, dev, lambda: None)
+    out = {"workload": w["name"], "ms_per_step": ms, "value": U / (ms / 1e3),
+           "unit": UNIT, "steps": args.steps,
+           "stages_ms": {k: round(v["ms"], 3) for k, v in stages.items()},
+           "e2e": e2e, "gpu_launches_per_step": rec.launches_per_call,
+           "_sino": sino, "_angles": angles, "_volume": got}
+    del rec, vol, dsino
+    torch.cuda.empty_cache()
+    return out
 
 
 def _timed(fn, steps, warmup, flush, stream):
@@ -709,10 +804,25 @@ def run_diff(args):
     dev = torch.device("cuda", 0)
     from odtbrain_gb300 import build as native_build
     native_build.build()
+    if args.ncu_case:
+        measure_diff(args, dev)
+        return
+    r = measure_diff(args, dev)
+    w = WORKLOADS["c4"]
+    U = updates(w["A"], w["n"])
+    ms = r.pop("ms_per_step")
+    line = _base_line(args, w, U / (ms / 1e3), ms, r)
+    print(json.dumps(line), flush=True)
+
+
+def measure_diff(args, dev):
+    """The differentiation workload (A=90, 128^2 -> 128^3): forward + VJP
+    time, forward time and peak device memory; a dict of results."""
+    import torch
     from odtbrain_gb300._alg3d import Backprop3D
     from odtbrain_gb300.autograd import backpropagate_3d_autograd
     from sino_gen import ellipsoid_phantom_sinogram
-    w = WORKLOAD
+    w = WORKLOADS["c4"]
     sino, angles = ellipsoid_phantom_sinogram(
         w["n"], w["A"], seed=w["seed"], count_range=w["count_range"],
         semi_range=w["semi_range"])
@@ -749,7 +859,7 @@ def run_diff(args):
             step()
         torch.cuda.synchronize()
         print("ncu case done")
-        return
+        return None
 
     clocks = ClockSampler(0)
     clocks.start()
@@ -768,7 +878,9 @@ def run_diff(args):
         step(host.to(dev, non_blocking=True))
         out_host.copy_(grads["s"], non_blocking=True)
     e2e_ms, _ = _timed(e2e, max(3, min(args.steps, 5)), 1, flush, stream)
-    line = _base_line(args, w, U / (ms / 1e3), ms, {
+    return {
+        "workload": w["name"], "ms_per_step": ms, "value": U / (ms / 1e3),
+        "unit": UNIT,
         "step": "forward + VJP (sinogram and gain), slabs recomputed",
         "forward_ms": fwd_ms, "backward_ms": ms - fwd_ms,
         "peak_device_mib": (peak - base) / 2**20,
@@ -782,24 +894,36 @@ def run_diff(args):
         "cpu_baseline": None,
         "accuracy": {"checked_by": "tests/test_gpu_adjoint.py: central "
                      "differences h=1e-3 over 64 directions and autograd "
-                     "through the dense FP64 model"}})
-    print(json.dumps(line), flush=True)
+                     "through the dense FP64 model"}}
 
 
 def run_learned(args):
     """Learned wedge filter: GPU time of the learned reconstruction against
-    the plain one, and the error cut of the shipped network on held-out
-    phantoms."""
+    the plain one, and the error cut of the shipped network on the 200
+    held-out phantoms."""
     import torch
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     from odtbrain_gb300 import build as native_build
     native_build.build()
+    r = measure_learned(args, dev, n_eval=200)
+    w = WORKLOADS["c5"]
+    ms = r.pop("ms_per_step")
+    line = _base_line(args, w, r["value"], ms, r)
+    print(json.dumps(line), flush=True)
+
+
+def measure_learned(args, dev, n_eval):
+    """The learned wedge filter (A=40 over 120 deg, 128^2 -> 128^3): GPU
+    time learned vs plain, and mean rel-L2 to the plain dense A=400
+    reconstruction over `n_eval` held-out phantoms (seeds 2,000,000 on,
+    disjoint from training and validation); a dict of results."""
+    import torch
     from odtbrain_gb300._alg3d import Backprop3D
     from odtbrain_gb300.learned import (WEDGE_CONFIG, evaluate,
                                         load_learned_filter, make_pairs,
                                         wedge_angles)
-    w = WORKLOAD
+    w = WORKLOADS["c5"]
     c = dict(WEDGE_CONFIG)
     A, n = c["num_angles"], c["n"]
     U = updates(A, n)
@@ -808,11 +932,19 @@ def run_learned(args):
     rec = Backprop3D((A, n, n), sp, c["res"], c["nm"], device=dev)
     rec_d = Backprop3D((c["dense_angles"], n, n), de, c["res"], c["nm"],
                        device=dev)
-    n_eval = 32
     seeds = 2_000_000 + np.arange(n_eval)  # the held-out seed range
-    sinos, targets = make_pairs(c, seeds, rec, rec_d, sp, de, dev)
+    learned_s, plain_s = [], []
     lf = load_learned_filter(rec)
-    learned, plain = evaluate(lf, sinos, targets)
+    sinos = None
+    for k in range(0, n_eval, 50):  # pairs in batches of 50 phantoms
+        sinos, targets = make_pairs(c, seeds[k:k + 50], rec, rec_d, sp, de,
+                                    dev)
+        l_, p_ = evaluate(lf, sinos, targets)
+        learned_s.append(l_ * len(targets))
+        plain_s.append(p_ * len(targets))
+        del targets
+    learned = float(sum(learned_s) / n_eval)
+    plain = float(sum(plain_s) / n_eval)
     flush = torch.empty(L2_FLUSH_BYTES, device=dev, dtype=torch.uint8)
     stream = torch.cuda.current_stream(dev)
     vol = torch.empty(rec.volume_shape(), dtype=torch.complex64, device=dev)
@@ -840,7 +972,9 @@ def run_learned(args):
         lf(host.to(dev, non_blocking=True), out=vol)
         out_host.copy_(vol, non_blocking=True)
     e2e_ms, _ = _timed(e2e, max(3, min(args.steps, 5)), 1, flush, stream)
-    line = _base_line(args, w, U / (ms_l / 1e3), ms_l, {
+    return {
+        "workload": w["name"], "ms_per_step": ms_l,
+        "value": U / (ms_l / 1e3), "unit": UNIT,
         "step": "learned-gain reconstruction, gains cached per angle set",
         "plain_ms": ms_p, "time_ratio_cached": ms_l / ms_p,
         "learned_with_inference_ms": ms_i,
@@ -853,8 +987,7 @@ def run_learned(args):
                 "h2d_bytes_per_step": int(host.numel() * 8),
                 "d2h_bytes_per_step": int(out_host.numel() * 8),
                 "ms_per_step": e2e_ms},
-        "cpu_baseline": None})
-    print(json.dumps(line), flush=True)
+        "cpu_baseline": None}
 
 
 def run_rytov(args):

@@ -106,7 +106,11 @@ odt_status odt_bpp3d_workspace_size(const odt_bpp3d_plan *plan,
 /* Number of angles the plan processes per pass of the rotation kernel. */
 odt_status odt_bpp3d_angle_batch(const odt_bpp3d_plan *plan, int32_t *batch);
 
-/* Run the backpropagation (the loop of _alg3d_bpp.py:492-549).
+/* Every call that takes a plan must be made with the device the plan was
+ * created on current (cudaSetDevice); otherwise it returns
+ * ODT_ERR_INVALID_ARGUMENT.
+ *
+ * Run the backpropagation (the loop of _alg3d_bpp.py:492-549).
  *   sino      device, (A, ny, nx) complex64 or complex128 (desc.input_dtype)
  *   weights   device, A doubles (angle weights, util.py:4-67) or NULL
  *   geometry  device, A*6 (Y_AXIS) or A*12 (AFFINE3D) doubles
@@ -377,6 +381,22 @@ odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real,
 odt_status odt_bpp3d_read_status(const odt_bpp3d_plan *plan, void *stream);
 
 odt_status odt_bpp3d_plan_destroy(odt_bpp3d_plan *plan);
+
+/* ---- Failure injection (tests of the error paths) -------------------------
+ * Neither call touches a kernel; no counterpart in the reference, whose
+ * error paths are host-side checks only (odtbrain/_alg3d_bpp.py:237-258).
+ *
+ * odt_debug_inject_status: stream-ordered, sets the plan's device status
+ * word to `bits` (0..255, the bits a kernel's own check records), exactly as
+ * a kernel that tripped its check leaves it; the next odt_bpp3d_read_status
+ * on that stream returns ODT_ERR_DEVICE_CHECK and clears it.
+ *
+ * odt_debug_set_table_alloc_limit: process-wide; odt_bpp3d_plan_create
+ * returns ODT_ERR_OUT_OF_MEMORY, without calling cudaMalloc, when the plan's
+ * device tables would exceed `bytes` (0 removes the limit). */
+odt_status odt_debug_inject_status(const odt_bpp3d_plan *plan, int32_t bits,
+                                   void *stream);
+odt_status odt_debug_set_table_alloc_limit(uint64_t bytes);
 
 /* Human-readable text of a status, and detail of the last host-side error
  * of the calling thread. */

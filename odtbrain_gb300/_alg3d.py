@@ -120,6 +120,9 @@ def _get_tables(key, build):
 
 
 def _get_plan(key, build_desc):
+    """The cached native plan for `key` (built by `build_desc` on a miss).
+    Instances with equal keys share one plan, and so its device status
+    word: status reporting is per plan, not per instance."""
     with _PLAN_LOCK:
         plan = _PLAN_CACHE.get(key)
         if plan is not None:
@@ -284,12 +287,14 @@ class Backprop3D:
 
     def __call__(self, sino, out=None, check=True):
         """Reconstruct from a device sinogram; stream-ordered on the current
-        stream.  ``check`` waits for the stream and raises if a kernel
-        recorded a failed internal check."""
-        out, stream, args = self._args(sino, out)
-        self.plan.execute(*args)
-        if check:
-            self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
+        stream of the instance's device.  ``check`` waits for the stream and
+        raises if a kernel recorded a failed internal check."""
+        torch = _torch()
+        with torch.cuda.device(self.device):
+            out, stream, args = self._args(sino, out)
+            self.plan.execute(*args)
+            if check:
+                self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
         return out
 
     def forward_gain(self, sino, gain=None, angle_gain=None, out=None,
@@ -297,15 +302,18 @@ class Backprop3D:
         """Reconstruct with gains multiplying the filter: ``gain`` a real
         (lNy, lNx) float32 map shared by all angles, ``angle_gain`` a
         complex64 (A, lNy, lNx) map per angle (None: no gain)."""
-        out, stream, args = self._args(sino, out)
-        gptr = ctypes.c_void_p(self._check_gain(gain).data_ptr()
-                               if gain is not None else 0)
-        aptr = ctypes.c_void_p(self._check_angle_gain(angle_gain).data_ptr()
-                               if angle_gain is not None else 0)
-        self.plan.execute_gain(args[0], args[1], args[2], gptr, aptr,
-                               args[3], args[4], args[5])
-        if check:
-            self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
+        torch = _torch()
+        with torch.cuda.device(self.device):
+            out, stream, args = self._args(sino, out)
+            gptr = ctypes.c_void_p(self._check_gain(gain).data_ptr()
+                                   if gain is not None else 0)
+            aptr = ctypes.c_void_p(
+                self._check_angle_gain(angle_gain).data_ptr()
+                if angle_gain is not None else 0)
+            self.plan.execute_gain(args[0], args[1], args[2], gptr, aptr,
+                                   args[3], args[4], args[5])
+            if check:
+                self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
         return out
 
     def filter_support(self):
@@ -380,11 +388,12 @@ class Backprop3D:
 
         def ptr(t):
             return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
-        self.plan.adjoint(
-            sptr, ptr(self.weights), ptr(self.geometry), gptr, aptr,
-            ptr(vol_grad), ptr(sgrad), ptr(ggrad), ptr(aggrad), ptr(ws),
-            ctypes.c_void_p(stream.cuda_stream))
-        self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
+        with torch.cuda.device(self.device):
+            self.plan.adjoint(
+                sptr, ptr(self.weights), ptr(self.geometry), gptr, aptr,
+                ptr(vol_grad), ptr(sgrad), ptr(ggrad), ptr(aggrad), ptr(ws),
+                ctypes.c_void_p(stream.cuda_stream))
+            self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
         del ws
         if need_angle_gain:
             return sgrad, ggrad, aggrad
@@ -393,15 +402,23 @@ class Backprop3D:
     def timed(self, sino, out=None):
         """Run once with a CUDA event pair around every kernel launch;
         returns per-stage {"ms", "launches", "bytes"}."""
-        out, stream, args = self._args(sino, out)
-        t = self.plan.execute_timed(*args)
-        self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
+        torch = _torch()
+        with torch.cuda.device(self.device):
+            out, stream, args = self._args(sino, out)
+            t = self.plan.execute_timed(*args)
+            self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
         return t
 
     def check(self):
+        """Wait for the current stream and raise if a kernel of the plan
+        recorded a failed internal check.  The status word belongs to the
+        native plan, which instances of the same shape and parameters share
+        (a per-process cache): a check raised here may come from another
+        such instance's execution, and reading it clears it for all."""
         torch = _torch()
-        stream = torch.cuda.current_stream(self.device)
-        self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
+        with torch.cuda.device(self.device):
+            stream = torch.cuda.current_stream(self.device)
+            self.plan.read_status(ctypes.c_void_p(stream.cuda_stream))
 
 
 def _upload(uSin, device):

@@ -53,6 +53,8 @@ EXPORTED_SYMBOLS = (
     "odt_apple_correct",
     "odt_apple_flags",
     "odt_apple_flags_workspace_size",
+    "odt_debug_inject_status",
+    "odt_debug_set_table_alloc_limit",
     "odt_status_string",
     "odt_last_error",
 )
@@ -198,6 +200,8 @@ def lib():
         L.odt_bpp3d_adjoint.argtypes = [vp] * 12
         L.odt_bpp3d_read_status.argtypes = [vp, vp]
         L.odt_bpp3d_plan_destroy.argtypes = [vp]
+        L.odt_debug_inject_status.argtypes = [vp, ctypes.c_int32, vp]
+        L.odt_debug_set_table_alloc_limit.argtypes = [ctypes.c_uint64]
         for name in ("odt_odt_to_ri", "odt_opt_to_ri"):
             getattr(L, name).argtypes = [vp, vp, ctypes.c_int64,
                                          ctypes.c_int32, ctypes.c_double,
@@ -237,7 +241,9 @@ def lib():
                      "odt_sino_prepare", "odt_sino_launch_count",
                      "odt_sino_read_status", "odt_apple_workspace_size",
                      "odt_apple_correct", "odt_apple_flags",
-                     "odt_apple_flags_workspace_size"):
+                     "odt_apple_flags_workspace_size",
+                     "odt_debug_inject_status",
+                     "odt_debug_set_table_alloc_limit"):
             getattr(L, name).restype = ctypes.c_int
         L.odt_status_string.argtypes = [ctypes.c_int]
         L.odt_status_string.restype = ctypes.c_char_p
@@ -245,6 +251,12 @@ def lib():
         L.odt_last_error.restype = ctypes.c_char_p
         _LIB = L
         return L
+
+
+def set_table_alloc_limit(nbytes):
+    """Test hook: make plan creation fail with MemoryError when its device
+    tables exceed `nbytes` (0 removes the limit)."""
+    check(lib().odt_debug_set_table_alloc_limit(int(nbytes)))
 
 
 def check(status):
@@ -326,6 +338,12 @@ class Plan:
 
     def read_status(self, stream_handle):
         check(lib().odt_bpp3d_read_status(self._h, stream_handle))
+
+    def inject_status(self, bits, stream_handle):
+        """Test hook: set the plan's device status word to `bits`, as a
+        kernel whose own check tripped would (odt_debug_inject_status)."""
+        check(lib().odt_debug_inject_status(self._h, int(bits),
+                                            stream_handle))
 
     def __del__(self):
         h = getattr(self, "_h", None)

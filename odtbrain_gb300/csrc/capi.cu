@@ -39,6 +39,11 @@ odt_status cuda_fail(cudaError_t e, const char *where)
     return fail(ODT_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+// Test hook (odt_debug_set_table_alloc_limit): plan creation refuses table
+// allocations above this many bytes (0: no limit).
+uint64_t g_table_alloc_limit = 0;
+std::mutex g_debug_mutex;
+
 constexpr uint64_t kDefaultWorkspace = 16ull << 30;   // 16 GiB of slabs, chunk buffers etc.
 // column-stage output chunks: two buffers of half this size in total.  Large
 // chunks (1024 planes of a 512-wide spectrum per buffer) mean few launches
@@ -86,6 +91,7 @@ int odt::set_error(int status, const char *msg)
 
 struct odt_bpp3d_plan {
     odt_bpp3d_desc d;
+    int device;      // CUDA device the tables, events and stream belong to
     int nz;
     int batch;       // angles per batch
     int jobs;        // (angle, plane) jobs per column/row launch
@@ -106,6 +112,23 @@ struct odt_bpp3d_plan {
 };
 
 namespace {
+
+// The plan's device must be the current one: its tables, events and second
+// stream belong to that device.
+odt_status check_device(const odt_bpp3d_plan *plan)
+{
+    int dev = -1;
+    const cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    if (dev != plan->device) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "plan was created on CUDA device %d but device %d is current", plan->device,
+                 dev);
+        return fail(ODT_ERR_INVALID_ARGUMENT, buf);
+    }
+    return ODT_OK;
+}
 
 void destroy_sync_objects(odt_bpp3d_plan *p)
 {
@@ -308,7 +331,20 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     const size_t oTy = o; o = align_up(o + (size_t)lNy * 8);
     const size_t oZ = o; o = align_up(o + odt::ZPOW_N * 4);
     const size_t oSt = o; o = align_up(o + 16);
-    cudaError_t e = cudaMalloc(&p->d_tables, o);
+    {
+        std::lock_guard<std::mutex> lock(g_debug_mutex);
+        if (g_table_alloc_limit && o > g_table_alloc_limit) {
+            delete p;
+            return fail(ODT_ERR_OUT_OF_MEMORY, "plan tables exceed the allocation limit set by "
+                                               "odt_debug_set_table_alloc_limit");
+        }
+    }
+    cudaError_t e = cudaGetDevice(&p->device);
+    if (e != cudaSuccess) {
+        delete p;
+        return cuda_fail(e, "cudaGetDevice");
+    }
+    e = cudaMalloc(&p->d_tables, o);
     if (e != cudaSuccess) {
         delete p;
         return e == cudaErrorMemoryAllocation ? fail(ODT_ERR_OUT_OF_MEMORY, "cudaMalloc of plan tables failed")
@@ -520,6 +556,9 @@ odt_status run_plan(const odt_bpp3d_plan *plan, const void *sino, const double *
         return fail(ODT_ERR_INVALID_ARGUMENT, "NULL pointer argument");
     if (((uintptr_t)workspace % kAlign) != 0)
         return fail(ODT_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    const odt_status dst = check_device(plan);
+    if (dst != ODT_OK)
+        return dst;
     const odt_bpp3d_desc &d = plan->d;
     cudaStream_t s = (cudaStream_t)stream;
     StageParams P = stage_params(plan);
@@ -680,6 +719,9 @@ odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const
         return fail(ODT_ERR_INVALID_ARGUMENT, "the gain gradient needs the sinogram");
     if (((uintptr_t)workspace % kAlign) != 0)
         return fail(ODT_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
+    const odt_status dst = check_device(plan);
+    if (dst != ODT_OK)
+        return dst;
     const odt_bpp3d_desc &d = plan->d;
     if (d.geometry != ODT_GEOM_Y_AXIS)
         return fail(ODT_ERR_UNSUPPORTED, "the adjoint is implemented for the y-axis geometry");
@@ -795,6 +837,9 @@ odt_status odt_bpp3d_read_status(const odt_bpp3d_plan *plan, void *stream)
 {
     if (!plan)
         return fail(ODT_ERR_INVALID_ARGUMENT, "NULL plan");
+    const odt_status dst = check_device(plan);
+    if (dst != ODT_OK)
+        return dst;
     int h = 0;
     cudaError_t e = cudaMemcpyAsync(&h, plan->d_status, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
     if (e == cudaSuccess)
@@ -802,11 +847,41 @@ odt_status odt_bpp3d_read_status(const odt_bpp3d_plan *plan, void *stream)
     if (e != cudaSuccess)
         return cuda_fail(e, "status read");
     if (h != 0) {
-        cudaMemsetAsync(plan->d_status, 0, sizeof(int), (cudaStream_t)stream);
+        // cleared synchronously, so a failed clear is reported here and not
+        // by some later call
+        e = cudaMemset(plan->d_status, 0, sizeof(int));
+        if (e != cudaSuccess)
+            return cuda_fail(e, "status clear");
         char buf[96];
         snprintf(buf, sizeof buf, "device check failed (bits 0x%x)", h);
         return fail(ODT_ERR_DEVICE_CHECK, buf);
     }
+    return ODT_OK;
+}
+
+odt_status odt_debug_inject_status(const odt_bpp3d_plan *plan, int32_t bits, void *stream)
+{
+    if (!plan)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "NULL plan");
+    if (bits < 0 || bits > 255)
+        return fail(ODT_ERR_INVALID_ARGUMENT, "status bits must be in 0..255");
+    const odt_status dst = check_device(plan);
+    if (dst != ODT_OK)
+        return dst;
+    // the word's low byte (little-endian), stream-ordered like a kernel's
+    // report; the upper bytes are cleared
+    cudaError_t e = cudaMemsetAsync(plan->d_status, 0, sizeof(int), (cudaStream_t)stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(plan->d_status, bits, 1, (cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "status injection");
+    return ODT_OK;
+}
+
+odt_status odt_debug_set_table_alloc_limit(uint64_t bytes)
+{
+    std::lock_guard<std::mutex> lock(g_debug_mutex);
+    g_table_alloc_limit = bytes;
     return ODT_OK;
 }
 
@@ -869,10 +944,12 @@ extern "C" odt_status odt_bpp3d_execute_noalloc(const odt_bpp3d_plan *plan, cons
                  (unsigned long long)ODT_NOALLOC_SCRATCH_BYTES);
         return fail(ODT_ERR_INVALID_ARGUMENT, buf);
     }
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess)
-        return cuda_fail(e, "cudaGetDevice");
+    // the scratch of the plan's device, which must be current
+    const odt_status dst = check_device(plan);
+    if (dst != ODT_OK)
+        return dst;
+    const int dev = plan->device;
+    cudaError_t e = cudaSuccess;
     if (dev < 0 || dev >= kMaxDevices)
         return fail(ODT_ERR_UNSUPPORTED, "device ordinal beyond the static scratch table");
     void *scratch = nullptr;

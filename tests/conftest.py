@@ -50,3 +50,23 @@ def reference_cases(golden, two_d=False):
             kw["padding"] = tuple(kw["padding"])
         yield n, cases[n + "__sino"], cases[n + "__angles"], kw, \
             cases[n + "__out"]
+
+
+def reference_c1():
+    """The whole 60-angle 64^3 workload and the reference's output for it
+    (tests/golden/reference_c1.npz, written by make_golden.py): returns
+    (sino, angles, kwargs, out) with the input regenerated by the seeded
+    phantom generator and checked against the stored checksum."""
+    from sino_gen import ellipsoid_phantom_sinogram
+    with np.load(os.path.join(GOLDEN, "reference_c1.npz")) as z:
+        args = json.loads(str(z["args"]))
+        kw = json.loads(str(z["kw"]))
+        out = z["out_re"].astype(np.float64) + 1j * z["out_im"]
+        abs_sum = float(z["input_abs_sum"])
+        angles_ref = z["angles"]
+    args["count_range"] = tuple(args["count_range"])
+    args["semi_range"] = tuple(args["semi_range"])
+    sino, angles = ellipsoid_phantom_sinogram(**args)
+    assert abs(np.abs(sino).sum() - abs_sum) <= 1e-12 * abs_sum
+    np.testing.assert_array_equal(angles, angles_ref)
+    return sino, angles, kw, out

@@ -1,10 +1,10 @@
 """Generate the golden fixtures in ``tests/golden/`` from the unmodified
 ODTbrain reference.
 
-Run where the reference source tree is mounted (default /root/reference, or
-$ODT_REFERENCE_ROOT):
+Run where the reference source tree is mounted, naming it in
+$ODT_REFERENCE_ROOT (the directory that contains ``odtbrain/``):
 
-    python tests/golden/make_golden.py
+    ODT_REFERENCE_ROOT=/path/to/ODTbrain python tests/golden/make_golden.py
 
 Writes
   reference_zips.npz   the reference's own golden vectors
@@ -26,9 +26,13 @@ Writes
                        sinogram_as_rytov / sinogram_as_radon
 
   reference_apple.npz  inputs and outputs of the reference's apple.correct
+  reference_c1.npz     the reference's backpropagate_3d of the whole
+                       60-angle, 64x64 -> 64^3 ellipsoid-phantom workload
+                       (FP64 run, stored as float32 real/imaginary parts),
+                       with a checksum of the regenerated input
 
-Parts can be chosen on the command line (backprop, sino, apple); default
-all.
+Parts can be chosen on the command line (backprop, sino, apple, c1);
+default all.
 The input sinogram generator below restates the reference's test helper
 (tests/common_methods.py:63-184) so that the GPU tests can regenerate the
 same inputs without the reference tree.
@@ -63,7 +67,29 @@ def main(parts):
         make_sino(odt)
     if "apple" in parts:
         make_apple(odt)
+    if "c1" in parts:
+        make_c1(odt)
     print("wrote fixtures to", HERE)
+
+
+# The 60-angle 64^3 workload: seeded ellipsoid phantom (1-5 ellipsoids,
+# semi-axes 5-20 px), padfac 1.75 (128^2 FFTs), intp_order 2, complex
+# output, angle weights on.  tests/test_gpu_parity.py regenerates the input
+# with the same call.
+C1_ARGS = dict(n=64, A=60, seed=2023, count_range=(1, 5), semi_range=(5, 20))
+C1_KW = dict(res=3.0, nm=1.333, padfac=1.75, intp_order=2, onlyreal=False)
+
+
+def make_c1(odt):
+    from sino_gen import ellipsoid_phantom_sinogram
+    sino, angles = ellipsoid_phantom_sinogram(**C1_ARGS)
+    out = odt.backpropagate_3d(sino, angles, **C1_KW)
+    np.savez_compressed(
+        os.path.join(HERE, "reference_c1.npz"),
+        out_re=out.real.astype(np.float32),
+        out_im=out.imag.astype(np.float32),
+        input_abs_sum=np.abs(sino).sum(), angles=angles,
+        kw=np.array(json.dumps(C1_KW)), args=np.array(json.dumps(C1_ARGS)))
 
 
 def make_backprop(odt):
@@ -284,4 +310,4 @@ def make_apple(odt):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["backprop", "sino", "apple"])
+    main(sys.argv[1:] or ["backprop", "sino", "apple", "c1"])

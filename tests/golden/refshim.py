@@ -25,7 +25,9 @@ import types
 import numpy as np
 import scipy.fft
 
-REFERENCE_ROOT = os.environ.get("ODT_REFERENCE_ROOT", "/root/reference")
+# Root of the reference source tree (the directory holding ``odtbrain/``),
+# from the environment; load_reference() refuses to guess it.
+REFERENCE_ROOT = os.environ.get("ODT_REFERENCE_ROOT")
 
 
 def _make_pyfftw():
@@ -103,7 +105,13 @@ def _make_skimage():
 
 
 def load_reference():
-    """Return the reference ``odtbrain`` module, imported read-only."""
+    """Return the reference ``odtbrain`` module, imported read-only from
+    $ODT_REFERENCE_ROOT."""
+    if not REFERENCE_ROOT or not os.path.isdir(
+            os.path.join(REFERENCE_ROOT, "odtbrain")):
+        raise RuntimeError(
+            "set ODT_REFERENCE_ROOT to the ODTbrain source tree (the "
+            "directory that contains odtbrain/); got %r" % (REFERENCE_ROOT,))
     sys.dont_write_bytecode = True
     if "odtbrain" in sys.modules and hasattr(sys.modules["odtbrain"],
                                              "backpropagate_3d"):

@@ -11,7 +11,7 @@ import multiprocessing as mp
 import numpy as np
 import pytest
 
-from conftest import reference_cases
+from conftest import reference_c1, reference_cases
 from oracle import odt_oracle as O
 from sino_gen import (cutout, ellipsoid_phantom_sinogram, gauss_sino_3d,
                       gauss_sino_3d_tilted, parameter_sets)
@@ -316,3 +316,91 @@ def test_c3_shape_subset_vs_oracle(odt):
                                       dtype=np.float32, **kw)
     ref = O.backpropagate_3d_tilted(sino, angles, fft_workers=-1, **kw)
     assert_close(got, ref, what="200^3 tilted")
+
+
+def test_full_c1_vs_reference_and_oracle(odt):
+    """The whole 60-angle, 64x64 -> 64^3 workload (ellipsoid phantom,
+    padfac 1.75 -> 128^2 FFTs, order 2, angle weights on, complex output):
+    the GPU result against the unmodified reference's output (fixture) and
+    against the FP64 oracle run here, rel-L2 <= 1e-5 and max <= 1e-5 of
+    the largest magnitude.  The fixture stores float32 parts (rounding
+    ~3e-8), well inside the bound."""
+    sino, angles, kw, ref = reference_c1()
+    got = odt.backpropagate_3d(sino, angles, dtype=np.float64, **kw)
+    assert got.dtype == np.complex128
+    assert_close(got, ref, what="C1 vs reference")
+    kw_o = dict(kw)
+    kw_o.pop("onlyreal")
+    oracle = O.backpropagate_3d(sino, angles, **kw_o)
+    assert_close(got, oracle, what="C1 vs oracle")
+
+
+def test_device_check_status_raises(odt, cuda_ready):
+    """A kernel's own check records bits in the plan's status word; the
+    next status read turns them into ODT_ERR_DEVICE_CHECK and a Python
+    exception, clears the word, and the plan keeps working.  The bits are
+    set by the host (odt_debug_inject_status), so no kernel is made to
+    fail."""
+    import ctypes
+    import torch
+    from odtbrain_gb300 import _native
+    from odtbrain_gb300._alg3d import Backprop3D
+    sino, angles = ellipsoid_phantom_sinogram(32, 12, seed=5,
+                                              count_range=(1, 3),
+                                              semi_range=(3, 8))
+    rec = Backprop3D(sino.shape, angles, 3.0, 1.333,
+                     input_dtype="complex128", device=cuda_ready)
+    d = torch.from_numpy(sino).to(cuda_ready)
+    first = rec(d).cpu().numpy()
+    stream = torch.cuda.current_stream(cuda_ready)
+    handle = ctypes.c_void_p(stream.cuda_stream)
+    rec.plan.inject_status(1, handle)  # DEVCHK_BOX_OVERFLOW
+    with pytest.raises(_native.OdtError, match="bits 0x1") as info:
+        rec.check()
+    assert info.value.status == _native.ODT_ERR_DEVICE_CHECK
+    rec.check()  # cleared by the read
+    # the same bits arriving between a launch and the status read of a call
+    rec.plan.inject_status(2, handle)  # DEVCHK_BAD_CONFIG
+    with pytest.raises(_native.OdtError, match="bits 0x2"):
+        rec(d)
+    again = rec(d).cpu().numpy()
+    np.testing.assert_array_equal(first, again)
+    ref = O.backpropagate_3d(sino, angles, res=3.0, nm=1.333)
+    assert_close(again, ref, what="after a device check")
+
+
+# The full benchmark configurations (their seeded workloads, every angle):
+# the north star states its rel-L2 target for these sizes.
+FULL_CONFIGS = {
+    "c2": dict(n=256, A=200, seed=2024, count_range=(3, 12),
+               semi_range=(8, 60), axis=None),
+    "c3": dict(n=200, A=220, seed=2025, count_range=(3, 12),
+               semi_range=(8, 50),
+               axis=(0.0, float(np.cos(0.2)), float(np.sin(0.2)))),
+}
+
+
+@pytest.mark.parametrize("cfg", ["c2", "c3"])
+def test_full_config_vs_oracle(odt, cfg):
+    """The 200-angle 256^2 -> 256^3 workload (y axis) and the 220-angle
+    200^2 -> 200^3 workload (axis tilted 0.2 rad toward z), complex64 input,
+    angle weights on, padfac 1.75 (512^2 FFTs), order 2: every angle against
+    the FP64 oracle (about a minute of host time each), rel-L2 <= 1e-5 and
+    max <= 1e-5 of the largest magnitude."""
+    c = FULL_CONFIGS[cfg]
+    ax = c["axis"]
+    sino, angles = ellipsoid_phantom_sinogram(
+        c["n"], c["A"], seed=c["seed"], count_range=c["count_range"],
+        semi_range=c["semi_range"], axis=ax or (0, 1, 0))
+    sino = sino.astype(np.complex64)
+    kw = dict(res=3.0, nm=1.333, padfac=1.75, intp_order=2)
+    if ax is None:
+        got = odt.backpropagate_3d(sino, angles, dtype=np.float32, **kw)
+        ref = O.backpropagate_3d(sino.astype(np.complex128), angles,
+                                 fft_workers=-1, **kw)
+    else:
+        got = odt.backpropagate_3d_tilted(sino, angles, dtype=np.float32,
+                                          tilted_axis=ax, **kw)
+        ref = O.backpropagate_3d_tilted(sino.astype(np.complex128), angles,
+                                        tilted_axis=ax, fft_workers=-1, **kw)
+    assert_close(got, ref, what="%s full" % cfg)

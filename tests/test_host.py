@@ -285,3 +285,61 @@ def test_public_names_match_the_reference():
     assert callable(odt.util.compute_angle_weights_1d)
     assert issubclass(odt.warn.DataUndersampledWarning, UserWarning)
     assert issubclass(odt.warn.ImplementationAmbiguousWarning, UserWarning)
+
+
+def _small_desc(d_arrays):
+    d = _native.Bpp3dDesc()
+    d.num_angles, d.ny, d.nx = 4, 16, 16
+    d.pad_ny = d.pad_nx = 64
+    d.pad_y_left = d.pad_x_left = 24
+    d.pad_mode = _native.ODT_PAD_EDGE
+    d.intp_order = 2
+    filt = np.zeros(64 * 64 * 2)
+    ph = np.zeros(64 * 64)
+    d_arrays.extend([filt, ph])
+    d.filter = filt.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.kz_phase = ph.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    return d
+
+
+def test_forced_allocation_failure_raises_memory_error(native_lib):
+    """A plan whose device tables exceed the injected allocation limit is
+    refused with ODT_ERR_OUT_OF_MEMORY before any CUDA call (so this runs on
+    CPU), and the Python binding turns that into MemoryError."""
+    keep = []
+    d = _small_desc(keep)
+    h = ctypes.c_void_p()
+    _native.set_table_alloc_limit(1024)
+    try:
+        st = native_lib.odt_bpp3d_plan_create(ctypes.byref(d), ctypes.byref(h))
+        assert st == _native.ODT_ERR_OUT_OF_MEMORY
+        assert not h.value
+        assert b"allocation limit" in native_lib.odt_last_error()
+        with pytest.raises(MemoryError, match="allocation limit"):
+            _native.Plan(d)
+    finally:
+        _native.set_table_alloc_limit(0)
+    # validation still comes first: a bad descriptor stays a ValueError
+    d.pad_x_left = 60
+    _native.set_table_alloc_limit(1024)
+    try:
+        with pytest.raises(ValueError, match="padding"):
+            _native.Plan(d)
+    finally:
+        _native.set_table_alloc_limit(0)
+
+
+def test_status_codes_map_to_python_exceptions(native_lib):
+    """Each non-OK status becomes the exception the reference's callers
+    expect (ValueError / NotImplementedError / MemoryError) or OdtError."""
+    expect = {_native.ODT_ERR_INVALID_ARGUMENT: ValueError,
+              _native.ODT_ERR_UNSUPPORTED: NotImplementedError,
+              _native.ODT_ERR_OUT_OF_MEMORY: MemoryError,
+              _native.ODT_ERR_CUDA: _native.OdtError,
+              _native.ODT_ERR_DEVICE_CHECK: _native.OdtError}
+    for st, exc in expect.items():
+        with pytest.raises(exc) as info:
+            _native.check(st)
+        if exc is _native.OdtError:
+            assert info.value.status == st
+    _native.check(_native.ODT_OK)

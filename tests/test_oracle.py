@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 import scipy.ndimage as ndi
 
-from conftest import reference_cases
+from conftest import reference_c1, reference_cases
 from oracle import odt_oracle as O
 from sino_gen import cutout, parameter_sets, gauss_sino_3d
 
@@ -165,3 +165,17 @@ def test_dense_model_matches_oracle(order):
     got = model(torch.from_numpy(sino)).numpy()
     ref = O.backpropagate_3d(sino, angles, 3.0, 1.333, intp_order=order)
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_oracle_full_c1_matches_reference():
+    """The whole 60-angle, 64x64 -> 64^3 workload (128^2 FFTs, order 2,
+    weights on) against the unmodified reference's output for it; the
+    fixture holds float32 real/imaginary parts, so the bound is FP32
+    storage rounding."""
+    sino, angles, kw, ref = reference_c1()
+    kw = dict(kw)
+    assert kw.pop("onlyreal") is False
+    got = O.backpropagate_3d(sino, angles, **kw)
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    mx = np.abs(got - ref).max() / np.abs(ref).max()
+    assert rel < 2e-7 and mx < 2e-7, (rel, mx)
