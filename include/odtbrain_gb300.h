@@ -247,6 +247,12 @@ odt_status odt_mlp_gain_forward(const odt_mlp_params *params,
                                 int32_t num_positions, void *gain,
                                 void *stream);
 
+/* Inference runs on the 5th-generation tensor cores (tcgen05.mma with the
+ * accumulators in tensor memory), whose completion waits are bounded; wait
+ * for `stream` and return ODT_ERR_DEVICE_CHECK if such a wait gave up since
+ * the last call (the gains of that call are then invalid). */
+odt_status odt_mlp_read_status(void *stream);
+
 /* Device bytes of the activation store odt_mlp_gain_backward needs for
  * num_positions positions per angle. */
 odt_status odt_mlp_store_size(int32_t num_angles, int32_t num_positions,

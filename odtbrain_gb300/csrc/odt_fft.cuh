@@ -153,6 +153,14 @@ constexpr int ipow8(int k) { return k == 0 ? 1 : 8 * ipow8(k - 1); }
 // table they lie on distinct banks.
 constexpr int TW_P1 = 56;
 __host__ __device__ constexpr int tw_slots(int n) { return n + TW_P1; }
+// Optional third table, for lines whose third radix-8 pass (Ns = 64) reads
+// its twiddles per thread class jm = j mod 64: entry jm*7 + r-1 =
+// exp(-2 pi i r jm / 512), the plain table's entry r*jm*N/512.  Read from
+// it, a warp's twiddles lie on distinct banks at a per-thread base plus a
+// constant offset (from the plain table the even r read with 2- and 4-way
+// conflicts, at addresses computed per r).
+constexpr int TW_P2 = 64 * 7;
+__host__ __device__ constexpr int tw_slots2(int n) { return n + TW_P1 + TW_P2; }
 
 // Power-of-two line, 64 <= N <= 4096.
 template <int N_>
@@ -173,7 +181,8 @@ struct Pow2Line {
     // bar > 0: the line's TPL threads are consecutive warps and sync on
     // named barrier `bar` (only they share the line's buffers); 0: the whole
     // CTA syncs.
-    template <int DIR, bool PAD = false>
+    // TW2: the twiddle region also holds the third table (tw_slots2).
+    template <int DIR, bool PAD = false, bool TW2 = false>
     __device__ __forceinline__ void run(float2 (&v)[8], int j, float2 *line0, float2 *line1, int es,
                                         const float2 *tw, int &flip, int bar = 0) const
     {
@@ -185,6 +194,11 @@ struct Pow2Line {
 #pragma unroll
                 for (int r = 1; r < 8; ++r)
                     v[r] = cmul(v[r], twid<DIR>(t1, r - 1));
+            } else if (pass == 2 && TW2) {
+                const float2 *t2 = tw + N + TW_P1 + (j & 63) * 7;
+#pragma unroll
+                for (int r = 1; r < 8; ++r)
+                    v[r] = cmul(v[r], twid<DIR>(t2, r - 1));
             } else if (pass > 1) {
                 const int jm = j & (Ns - 1);
                 const int stp = jm * (N / (Ns * 8));

@@ -30,7 +30,8 @@ __device__ __forceinline__ void cp_async_wait()
 // Error bits recorded by kernels in the plan's device status word.
 enum : int {
     DEVCHK_BOX_OVERFLOW = 1,   // a rotation footprint did not fit its tile
-    DEVCHK_BAD_CONFIG = 2      // a kernel was launched with an unsupported shape
+    DEVCHK_BAD_CONFIG = 2,     // a kernel was launched with an unsupported shape
+    DEVCHK_COPY_TIMEOUT = 4    // a bulk tensor copy did not complete in time
 };
 
 // Number of boundary-correction terms of the B-spline prefilter that are
@@ -97,6 +98,10 @@ cudaError_t launch_columns_boundary(const StageParams &P, const float2 *rowspec,
 // Single-row planes (lNy == ny == 1, slab pitch 1): the column and row
 // stages fused in one launch over jobs [q0, q0 + qn), from the row spectra.
 bool single_row_plan(const StageParams &P);
+// Square power-of-two padded planes (N >= 256) cropped to their centred
+// half (ny = nx = N/2 from N/4): the column and row stages then run
+// kernels whose crop and edge positions are compile-time constants.
+bool half_crop(const StageParams &P);
 cudaError_t launch_rows_line(const StageParams &P, const float2 *rowspec, const float2 *Tab, float2 *slab, int q0,
                              int qn, cudaStream_t s);
 cudaError_t launch_rows_inverse(const StageParams &P, const float2 *T, const float2 *Tab, float2 *slab, int q0,

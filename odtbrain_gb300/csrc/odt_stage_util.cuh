@@ -88,6 +88,18 @@ __device__ __forceinline__ void copy_twiddles(float2 *dst, const float2 *src, in
 }
 
 
+// copy_twiddles plus the third-pass table (tw_slots2(n) entries; power-of-
+// two lines with a third radix-8 pass, n >= 512).
+template <class L>
+__device__ __forceinline__ void copy_twiddles2(float2 *dst, const float2 *src, int n)
+{
+    copy_twiddles<L>(dst, src, n);
+    for (int i = threadIdx.x; i < TW_P2; i += blockDim.x) {
+        const int jm = i / 7, r = i - 7 * jm + 1;
+        dst[n + TW_P1 + i] = src[r * jm * (n / 512)];
+    }
+}
+
 // Select v[pos / TPL] of the thread holding position `pos` without dynamic
 // register indexing; returns true when this thread holds it.
 template <class L>
@@ -116,12 +128,26 @@ __device__ __forceinline__ bool group_active(const StageParams &P, int kx0)
     return !(kx0 >= P.kx_zero_lo && kx0 + KX <= P.kx_zero_hi);
 }
 
+// Length of a power-of-two line type, 0 for the generic line.
+template <class L>
+constexpr int pow2_len()
+{
+    if constexpr (std::is_same<L, GenericLine>::value)
+        return 0;
+    else
+        return L::N;
+}
+
 // ---------------------------------------------------------------------------
 // Dispatch on the line length.
+// KX columns per column-stage CTA: 512-point columns run 4 per CTA (256
+// threads) so that three CTAs of 85 registers fit an SM; measured on the
+// 256^3 workload, 8 per CTA at 64 registers took 27.1 ms for the column
+// stage against 25.7 ms (and 4 per CTA at 2 CTAs of 128 registers 28.7 ms).
 template <class L>
 struct Cfg {
     static constexpr int LPC = (L::TPL >= 256) ? 1 : 256 / L::TPL;
-    static constexpr int KX = (L::TPL >= 512) ? 1 : ((512 / L::TPL) > 16 ? 16 : 512 / L::TPL);
+    static constexpr int KX = (L::TPL == 64) ? 4 : ((L::TPL >= 512) ? 1 : ((512 / L::TPL) > 16 ? 16 : 512 / L::TPL));
 };
 template <>
 struct Cfg<GenericLine> {
@@ -133,6 +159,21 @@ template <class L>
 inline size_t smem_rows(int n)
 {
     return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + tw_slots(n) + 4 * Cfg<L>::LPC) * sizeof(float2);
+}
+// k_rows_inverse_half: the exchange buffers, the twiddle table and the
+// edge samples.
+template <class L>
+inline size_t smem_rows_half(int n)
+{
+    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + tw_slots(n) + 4 * Cfg<L>::LPC) * sizeof(float2);
+}
+// k_columns_propagate of half-crop plans: smem_cols plus the third-pass
+// twiddle table.
+template <class L>
+inline size_t smem_cols_half(int n)
+{
+    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + Cfg<L>::KX * n + tw_slots2(n) + 4 * Cfg<L>::KX) *
+           sizeof(float2);
 }
 template <class L>
 inline size_t smem_cols(int n)

@@ -31,6 +31,14 @@
 
 namespace odt {
 
+// Column stage of half-crop plans: keep the propagator step exp(i w) of a
+// thread's elements in registers instead of shared memory, and read the
+// third radix-8 pass's twiddles from the per-thread-class table (256^3
+// workload: 25.7 ms without either, 25.7 / 26.0 ms with one of them,
+// 24.1 ms with both).
+constexpr bool kColumnStepRegs = true;
+constexpr bool kColumnTw2 = true;
+
 // ---------------------------------------------------------------------------
 // (a) rows: pad + weight + forward FFT along x.
 // rowspec[a][y][kx], a in the batch, y over the padded height.
@@ -154,6 +162,50 @@ __device__ __forceinline__ void column_inverse_store(const StageParams &P, const
     }
 }
 
+// Half-crop form of column_inverse_store (half_crop plans: ny = N/2 rows
+// starting at N/4 of a power-of-two column of N).  Thread j then holds the
+// cropped rows in slots 2..5, row j + TPL*(r-2), and the four edge samples
+// of the y-prefilter solve at compile-time slots, so the crop needs no
+// predicates and the stores use constant offsets from one row pointer.
+// dst points at row 0 of the job's T block, column kx (row stride N).
+template <class L, int KX, bool TW2>
+__device__ __forceinline__ void column_inverse_store_half(const StageParams &P, const L &line, float2 (&v)[L::SLOTS],
+                                                          int c, int j, float2 *buf0, float2 *buf1,
+                                                          const float2 *tw, float2 *edge, int &flip, float2 *dst)
+{
+    constexpr int N = L::N, TPL = L::TPL, NY = N / 2, PAD = N / 4;
+    line.template run<1, true, TW2>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+    if (P.order >= 2 && P.tilted) {
+        // y-prefilter boundary terms from u at PAD-1, PAD+1, PAD+NY-2, PAD+NY
+        float2 t;
+        if (held<L>(v, j, PAD - 1, t)) edge[c * 4 + 0] = t;
+        if (held<L>(v, j, PAD + 1, t)) edge[c * 4 + 1] = t;
+        if (held<L>(v, j, PAD + NY - 2, t)) edge[c * 4 + 2] = t;
+        if (held<L>(v, j, PAD + NY, t)) edge[c * 4 + 3] = t;
+        __syncthreads();
+        const float2 d0 = edge[c * 4 + 0] - edge[c * 4 + 1];
+        const float2 d1 = edge[c * 4 + 3] - edge[c * 4 + 2];
+        const float2 Ac = make_float2(P.by_ca * d0.x + P.by_cb * d1.x, P.by_ca * d0.y + P.by_cb * d1.y);
+        const float2 Bc = make_float2(P.by_ca * d1.x + P.by_cb * d0.x, P.by_ca * d1.y + P.by_cb * d0.y);
+#pragma unroll
+        for (int r = 2; r <= 5; ++r) {
+            const int yy = j + TPL * (r - 2);
+            if (yy < ZPOW_N) {
+                const float zz = P.tab.zpow[yy];
+                v[r] = make_float2(fmaf(Ac.x, zz, v[r].x), fmaf(Ac.y, zz, v[r].y));
+            }
+            if (NY - 1 - yy < ZPOW_N) {
+                const float zz = P.tab.zpow[NY - 1 - yy];
+                v[r] = make_float2(fmaf(Bc.x, zz, v[r].x), fmaf(Bc.y, zz, v[r].y));
+            }
+        }
+    }
+    float2 *d = dst + (size_t)j * N;
+#pragma unroll
+    for (int r = 2; r <= 5; ++r)
+        d[(r - 2) * TPL * N] = v[r];
+}
+
 // ---------------------------------------------------------------------------
 // (b0) z-prefilter boundary columns, once per angle (order >= 2).  The
 // prefiltered propagator of plane p is E_p + alpha z^p + beta z^(nz-1-p);
@@ -198,25 +250,38 @@ __global__ void __launch_bounds__(KX * L::TPL) k_columns_boundary(StageParams P,
 // propagator (exact anchor, then a complex recurrence whose per-element step
 // lives in shared memory), backward FFT along y, crop.  Output
 // T[q-q0][y][kx], y over the cropped height.
-template <class L, int KX>
-__global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
+template <class L, int KX, bool HALF>
+__global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX * L::TPL <= 512) ? 2 : 1))
     k_columns_propagate(StageParams P, L line, const float2 *rowspec, float2 *T, int q0, int qn, int ppc)
 {
     if (!group_active<KX>(P, blockIdx.x * KX))
         return;  // all-zero columns: the row stage never reads them
+    // half-crop plans: the per-element propagator step lives in registers
+    // and the third radix-8 pass reads per-thread-class twiddles
+    constexpr bool STEP_REGS = HALF && kColumnStepRegs;
+    constexpr bool TW2 = HALF && kColumnTw2 && pow2_len<L>() >= 512;
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNy
     const int ls = xslots<true>(n);
     float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls;
-    float2 *edge = tw + tw_slots(n); // [KX][4]
+    float2 *edge = tw + (TW2 ? tw_slots2(n) : tw_slots(n)); // [KX][4]
     float2 *stp = edge + 4 * KX;     // [n][KX] propagator step per element
-    copy_twiddles<L>(tw, P.tab.twy, n);
+    if constexpr (TW2)
+        copy_twiddles2<L>(tw, P.tab.twy, n);
+    else
+        copy_twiddles<L>(tw, P.tab.twy, n);
     const int c = threadIdx.x % KX, j = threadIdx.x / KX;
     const int kx = blockIdx.x * KX + c;
     const bool colok = kx < P.lNx;
     const int lNx = P.lNx, nz = P.nz, ny = P.ny;
     const int qb = q0 + blockIdx.y * ppc;
     const int qe = min(q0 + qn, qb + ppc);
+    float2 St[L::SLOTS];  // STEP_REGS: exp(i w) of this thread's elements
+    if constexpr (STEP_REGS) {
+#pragma unroll
+        for (int r = 0; r < L::SLOTS; ++r)
+            St[r] = P.tab.step[(size_t)(j + r * L::TPL) * lNx + kx];
+    }
     __syncthreads();
 
     float2 V[L::SLOTS];  // G * exp(i w z_p) for this thread's elements
@@ -237,7 +302,8 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
                 if (colok && ky < n) {
                     const size_t k = (size_t)ky * lNx + kx;
                     V[r] = cmul(V[r], expi_phase(P.tab.wsplit[k], zp));
-                    stp[ky * KX + c] = P.tab.step[k];
+                    if (!STEP_REGS)
+                        stp[ky * KX + c] = P.tab.step[k];
                 }
             }
             cur_a = a;
@@ -247,11 +313,17 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 512) ? 2 : 1)
         for (int r = 0; r < L::SLOTS; ++r) {
             v[r] = V[r];
             const int ky = j + r * L::TPL;
-            if (ky < n)
+            if constexpr (STEP_REGS)
+                V[r] = cmul(V[r], St[r]);
+            else if (HALF || ky < n)  // half-crop plans: a power-of-two line, ky < n
                 V[r] = cmul(V[r], stp[ky * KX + c]);
         }
-        column_inverse_store<L, KX>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
-                                    T + (size_t)(q - q0) * ny * lNx + kx);
+        if constexpr (HALF)
+            column_inverse_store_half<L, KX, TW2>(P, line, v, c, j, buf0, buf1, tw, edge, flip,
+                                                  T + (size_t)(q - q0) * (L::N / 2) * L::N + kx);
+        else
+            column_inverse_store<L, KX>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
+                                        T + (size_t)(q - q0) * ny * lNx + kx);
     }
 }
 
@@ -388,6 +460,126 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
                 __stcs(dst + (size_t)xx * yp + g * LPC + ll, stage[xx * SP + ll]);
         }
         if (g + 1 < GV) {
+            __syncthreads();  // stage reads done before buf0 is reused
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r)
+                v[r] = vn[r];
+        }
+    }
+}
+
+// (b2, half-crop plans) k_rows_inverse for square power-of-two planes
+// whose crop is the centred half (nx = ny = N/2 from N/4; the slab y pitch
+// is then N/2): every position the row needs -- the cropped outputs (slots
+// 2..5 of thread j, x = j + TPL*(r-2)), the x-prefilter edge samples and
+// the rows with boundary terms -- is a compile-time function of the thread
+// and slot, so the row runs without per-element index arithmetic or crop
+// predicates.  The all-zero spectrum columns (outside the |k| < km disc,
+// not written by the column stage) are a per-thread slot mask computed
+// once.  A CTA owns LPC*G consecutive rows of one job, LPC lines at a time.
+template <class L, int LPC, int G>
+__global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
+    k_rows_inverse_half(StageParams P, L line, const float2 *T, const float2 *Tab, float2 *slab, int q0)
+{
+    constexpr int N = L::N, TPL = L::TPL, NX = N / 2, PAD = N / 4, RG = LPC * G, CPJ = NX / RG;
+    static_assert(NX % RG == 0, "rows per CTA must divide the crop");
+    extern __shared__ float2 smem[];
+    constexpr int ls = xslots<false>(N);
+    float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
+    float2 *edge = tw + tw_slots(N);  // [LPC][4]
+    // (the third-pass twiddle table costs more to set up per CTA than its
+    // conflict-free reads save here: +0.7 ms for the 256^3 row stage)
+    copy_twiddles<L>(tw, P.tab.twx, N);
+    const int l = threadIdx.x / TPL, j = threadIdx.x % TPL;
+    const int bar = 1 + l;  // each line is whole warps (TPL >= 32)
+    const int nz = P.nz;
+    const int qrel = (int)blockIdx.x / CPJ;
+    const int ybase = ((int)blockIdx.x - qrel * CPJ) * RG;
+    const int qq = q0 + qrel;
+    const int a = qq / nz, p = qq - a * nz;
+    const bool pf = P.order >= 2;
+    const float zl = (pf && p < ZPOW_N) ? P.tab.zpow[p] : 0.f;
+    const float zh = (pf && nz - 1 - p < ZPOW_N) ? P.tab.zpow[nz - 1 - p] : 0.f;
+    // slots of this thread in the all-zero column band
+    unsigned zmask = 0;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int x = j + r * TPL;
+        if (x >= P.kx_zero_lo && x < P.kx_zero_hi)
+            zmask |= 1u << r;
+    }
+    // x-prefilter boundary weights of this thread's cropped slots: the
+    // A term (z^xx) for xx < ZPOW_N, the B term (z^(NX-1-xx)) near the end
+    float za[4], zb[4];
+#pragma unroll
+    for (int r = 2; r <= 5; ++r) {
+        const int xx = j + TPL * (r - 2);
+        za[r - 2] = (pf && xx < ZPOW_N) ? P.tab.zpow[xx] : 0.f;
+        zb[r - 2] = (pf && NX - 1 - xx < ZPOW_N) ? P.tab.zpow[NX - 1 - xx] : 0.f;
+    }
+    const float2 *Tq = T + (size_t)qrel * NX * N + j;
+    float2 *dst = slab + ((size_t)a * nz + p) * NX * NX + ybase;
+    auto load_row = [&](int y, float2 (&v)[L::SLOTS]) {
+        const float2 *src = Tq + (size_t)y * N;
+#pragma unroll
+        for (int r = 0; r < L::SLOTS; ++r)
+            v[r] = (zmask >> r) & 1u ? make_float2(0.f, 0.f) : __ldcs(src + r * TPL);
+    };
+    float2 v[L::SLOTS], vn[L::SLOTS];
+    load_row(ybase + l, v);
+    __syncthreads();  // twiddles
+#pragma unroll 1
+    for (int g = 0; g < G; ++g) {
+        const int y = ybase + g * LPC + l;
+        if (g + 1 < G)
+            load_row(y + LPC, vn);
+        if (zl != 0.f || zh != 0.f) {
+            const float2 *ta = Tab + ((size_t)(a * 2 + 0) * NX + y) * N + j;
+            const float2 *tb = Tab + ((size_t)(a * 2 + 1) * NX + y) * N + j;
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                if (!((zmask >> r) & 1u)) {
+                    const float2 u = ta[r * TPL], w = tb[r * TPL];
+                    v[r] = make_float2(fmaf(zh, w.x, fmaf(zl, u.x, v[r].x)), fmaf(zh, w.y, fmaf(zl, u.y, v[r].y)));
+                }
+            }
+        }
+        int flip = 0;
+        line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
+        if (pf) {
+            // the samples at PAD-1, PAD+1, PAD+NX-2, PAD+NX: held by one
+            // thread each, at a compile-time slot
+            float2 t;
+            if (held<L>(v, j, PAD - 1, t)) edge[l * 4 + 0] = t;
+            if (held<L>(v, j, PAD + 1, t)) edge[l * 4 + 1] = t;
+            if (held<L>(v, j, PAD + NX - 2, t)) edge[l * 4 + 2] = t;
+            if (held<L>(v, j, PAD + NX, t)) edge[l * 4 + 3] = t;
+            line_sync(bar, TPL);
+            const float2 d0 = edge[l * 4 + 0] - edge[l * 4 + 1];
+            const float2 d1 = edge[l * 4 + 3] - edge[l * 4 + 2];
+            const float2 Ac = make_float2(P.bx_ca * d0.x + P.bx_cb * d1.x, P.bx_ca * d0.y + P.bx_cb * d1.y);
+            const float2 Bc = make_float2(P.bx_ca * d1.x + P.bx_cb * d0.x, P.bx_ca * d1.y + P.bx_cb * d0.y);
+#pragma unroll
+            for (int r = 2; r <= 5; ++r) {
+                v[r] = make_float2(fmaf(Bc.x, zb[r - 2], fmaf(Ac.x, za[r - 2], v[r].x)),
+                                   fmaf(Bc.y, zb[r - 2], fmaf(Ac.y, za[r - 2], v[r].y)));
+            }
+        }
+        // stage[x][l] (pitch LPC+1) in buf0, then runs of LPC y per x
+        __syncthreads();  // every line is done with buf0 (and edge)
+        float2 *stage = buf0;
+        constexpr int SP = LPC + 1;
+#pragma unroll
+        for (int r = 2; r <= 5; ++r)
+            stage[(j + TPL * (r - 2)) * SP + l] = v[r];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < NX / TPL; ++k) {
+            const int e = threadIdx.x + k * LPC * TPL;
+            const int xx = e / LPC, ll = e % LPC;
+            __stcs(dst + (size_t)xx * NX + g * LPC + ll, stage[xx * SP + ll]);
+        }
+        if (g + 1 < G) {
             __syncthreads();  // stage reads done before buf0 is reused
 #pragma unroll
             for (int r = 0; r < L::SLOTS; ++r)
@@ -595,6 +787,23 @@ static cudaError_t boundary_impl(const StageParams &P, L line, const float2 *row
     return cudaGetLastError();
 }
 
+// Lines of a half-crop row kernel: whole warps (the line barriers are
+// per line).
+template <class L>
+constexpr bool half_line()
+{
+    return pow2_len<L>() >= 256;
+}
+// Groups of lines per half-crop row CTA (LPC * G rows): 16 rows, so that
+// the CTA's set-up (twiddle table, boundary weights, zero-column mask) is
+// shared by more lines (256^3 workload: 8 rows 21.7 ms, 16 rows 20.9 ms,
+// 32 rows 21.2 ms for the row stage).
+template <class L>
+constexpr int half_groups()
+{
+    return Cfg<L>::LPC >= 16 ? 1 : 16 / Cfg<L>::LPC;
+}
+
 template <class L>
 static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rowspec, float2 *T, int q0, int qn,
                                 cudaStream_t s)
@@ -602,8 +811,15 @@ static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rows
     constexpr int KX = Cfg<L>::KX;
     const int ppc = planes_per_cta<KX>(P, qn);
     dim3 grid((P.lNx + KX - 1) / KX, (qn + ppc - 1) / ppc);
-    k_columns_propagate<L, KX><<<grid, KX * L::TPL, smem_cols<L>(line.n), s>>>(P, line, rowspec, T, q0, qn,
-                                                                             ppc);
+    if constexpr (half_line<L>()) {
+        if (half_crop(P)) {
+            k_columns_propagate<L, KX, true>
+                <<<grid, KX * L::TPL, smem_cols_half<L>(line.n), s>>>(P, line, rowspec, T, q0, qn, ppc);
+            return cudaGetLastError();
+        }
+    }
+    k_columns_propagate<L, KX, false><<<grid, KX * L::TPL, smem_cols<L>(line.n), s>>>(P, line, rowspec, T, q0, qn,
+                                                                                    ppc);
     return cudaGetLastError();
 }
 
@@ -612,6 +828,15 @@ static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 
                                      float2 *slab, int q0, int qn, cudaStream_t s)
 {
     constexpr int LPC = Cfg<L>::LPC;
+    if constexpr (half_line<L>()) {
+        if (half_crop(P)) {
+            constexpr int G = half_groups<L>();
+            const unsigned grid = (unsigned)((long long)qn * (L::N / 2 / (LPC * G)));
+            k_rows_inverse_half<L, LPC, G><<<grid, LPC * L::TPL, smem_rows_half<L>(line.n), s>>>(P, line, T, Tab,
+                                                                                               slab, q0);
+            return cudaGetLastError();
+        }
+    }
     const unsigned grid = (unsigned)((long long)qn * ((P.ny + rows_per_cta<LPC>() - 1) / rows_per_cta<LPC>()));
     k_rows_inverse<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, Tab, slab, q0, qn);
     return cudaGetLastError();
@@ -642,8 +867,18 @@ static cudaError_t set_smem_attrs(int n)
                              (int)smem_cols<L>(n));
     if (e != cudaSuccess)
         return e;
-    return cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem_cols<L>(n));
+    if constexpr (half_line<L>()) {
+        e = cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols_half<L>(n));
+        if (e != cudaSuccess)
+            return e;
+        e = cudaFuncSetAttribute(k_rows_inverse_half<L, Cfg<L>::LPC, half_groups<L>()>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rows_half<L>(n));
+        if (e != cudaSuccess)
+            return e;
+    }
+    return cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX, false>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols<L>(n));
 }
 
 int columns_slots(const StageParams &P)
@@ -655,7 +890,7 @@ int columns_slots(const StageParams &P)
     const cudaError_t e = with_line(P.lNy, [&](auto line) {
         using L = decltype(line);
         constexpr int KX = Cfg<L>::KX;
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_columns_propagate<L, KX>, KX * L::TPL,
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_columns_propagate<L, KX, false>, KX * L::TPL,
                                                              smem_cols<L>(line.n));
     });
     return e == cudaSuccess ? per * sms : 0;
@@ -689,6 +924,13 @@ cudaError_t launch_columns_propagate(const StageParams &P, const float2 *rowspec
                                      cudaStream_t s)
 {
     return with_line(P.lNy, [&](auto line) { return columns_impl(P, line, rowspec, T, q0, qn, s); });
+}
+
+bool half_crop(const StageParams &P)
+{
+    const int N = P.lNx;
+    return P.lNy == N && N >= 256 && N <= 4096 && (N & (N - 1)) == 0 && 2 * P.ny == N && 2 * P.nx == N &&
+           4 * P.padyl == N && 4 * P.padxl == N && P.nz == P.nx && P.ypitch == P.ny;
 }
 
 bool single_row_plan(const StageParams &P)

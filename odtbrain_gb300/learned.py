@@ -210,6 +210,14 @@ class GainMLP:
             ctypes.c_void_p(stream.cuda_stream)))
         return out
 
+    def check(self):
+        """Wait for the current stream and raise if a tensor-core wait of an
+        inference gave up (odt_mlp_read_status)."""
+        torch = _torch()
+        stream = torch.cuda.current_stream(self.device)
+        _native.check(_native.lib().odt_mlp_read_status(
+            ctypes.c_void_p(stream.cuda_stream)))
+
     def grads(self, feat, gain_grad, positions=None):
         """Gradients of the loss with respect to the FP32 master parameters
         for the loss gradient ``gain_grad`` (complex64 (A, pad_ny, pad_nx),

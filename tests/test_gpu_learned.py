@@ -44,6 +44,7 @@ def test_mlp_forward_matches_oracle(cuda_ready, A, lNy, lNx):
     rng = np.random.default_rng(7)
     af = rng.uniform(-1.5, 1.5, (A, 2)).astype(np.float32)
     g = m.gains(torch.tensor(af, device=dev), lNy, lNx).cpu().numpy()
+    m.check()  # no tensor-core completion wait gave up
     X = M.features(af, lNy, lNx)
     ref, _ = M.forward(st, X, bf16=True)
     exact, _ = M.forward(st, X, bf16=False)
@@ -52,6 +53,26 @@ def test_mlp_forward_matches_oracle(cuda_ready, A, lNy, lNx):
     assert _rel(got - 1, ref - 1) < 1e-3
     # BF16 operands against the exact FP64 network
     assert _rel(got - 1, exact - 1) < 5e-2
+
+
+def test_mlp_forward_many_tiles(cuda_ready):
+    """262,144 points: more 128-point tiles than the persistent grid has
+    warp groups, so every group carries several tiles through the
+    tensor-memory accumulators, twice in a row."""
+    import torch
+    dev = cuda_ready
+    m, st = _random_mlp(torch, dev, seed=5)
+    rng = np.random.default_rng(9)
+    A, lNy, lNx = 4, 256, 256
+    af = rng.uniform(-1.5, 1.5, (A, 2)).astype(np.float32)
+    X = M.features(af, lNy, lNx)
+    ref, _ = M.forward(st, X, bf16=True)
+    for _ in range(2):
+        got = m.gains(torch.tensor(af, device=dev), lNy, lNx).cpu().numpy()
+        m.check()
+        got = got.reshape(-1)
+        assert np.all(np.isfinite(got))
+        assert _rel(got - 1, ref - 1) < 1e-3
 
 
 @pytest.mark.parametrize("A,lNy,lNx", [(3, 32, 32), (2, 17, 30)])
