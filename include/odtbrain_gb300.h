@@ -73,7 +73,8 @@ typedef struct odt_bpp3d_desc {
     int32_t pad_x_left;          /* padxl, _alg3d_bpp.py:302                */
     int32_t pad_mode;            /* enum odt_pad_mode                       */
     double padval_re, padval_im; /* linear-ramp end value                   */
-    int32_t intp_order;          /* spline order 0..3                       */
+    int32_t intp_order;          /* spline order 0..5 (4, 5: nx >= 4, and  */
+                                 /* ny >= 4 or 1 for AFFINE3D)              */
     int32_t geometry;            /* enum odt_geometry                       */
     int32_t onlyreal;            /* output float32 real part only           */
     int32_t input_dtype;         /* enum odt_input_dtype                    */
@@ -138,12 +139,12 @@ odt_status odt_bpp3d_execute_gain(const odt_bpp3d_plan *plan, const void *sino,
                                   const void *angle_gain, void *volume,
                                   void *workspace, void *stream);
 
-/* Bytes of device workspace odt_bpp3d_adjoint needs (y-axis plans). */
+/* Bytes of device workspace odt_bpp3d_adjoint needs. */
 odt_status odt_bpp3d_adjoint_workspace_size(const odt_bpp3d_plan *plan,
                                             uint64_t *bytes);
 
-/* Vector-Jacobian product of odt_bpp3d_execute_gain (y-axis geometry,
- * complex output).  Given the volume cotangent vol_grad (nx, ny, nx)
+/* Vector-Jacobian product of odt_bpp3d_execute_gain (either geometry,
+ * spline orders 0..3, complex output).  Given the volume cotangent vol_grad (nx, ny, nx)
  * complex64, writes (each may be NULL)
  *   sino_grad       (A, ny, nx) complex64 = J_sino^H vol_grad
  *   gain_grad       pad_ny*pad_nx float   = Re(J_gain^H vol_grad)

@@ -1,7 +1,8 @@
 """Differentiable 3D backpropagation.
 
-``backpropagate_3d_autograd`` wraps the GPU reconstruction (y-axis
-geometry, odtbrain/_alg3d_bpp.py:84-555) in a ``torch.autograd.Function``
+``backpropagate_3d_autograd`` wraps the GPU reconstruction (rotation about
+y, odtbrain/_alg3d_bpp.py:84-555, or about a tilted axis,
+odtbrain/_alg3d_bppt.py:374-949) in a ``torch.autograd.Function``
 whose backward pass is the hand-written adjoint of the CUDA pipeline
 (``odt_bpp3d_adjoint``): gradients flow to the complex sinogram and to an
 optional real per-frequency filter gain of the padded spectrum grid
@@ -45,15 +46,18 @@ class _BackpropagateFn(torch.autograd.Function):
 def backpropagate_3d_autograd(sino, angles, res, nm, lD=0, gain=None,
                               weight_angles=True, padding=(True, True),
                               padfac=1.75, padval="edge", intp_order=2,
-                              plan=None):
-    """Differentiable ``backpropagate_3d`` for a complex64 CUDA sinogram
-    tensor (A, Ny, Nx).  ``gain``: optional float32 CUDA tensor of the
-    padded spectrum shape multiplying the filter.  ``plan``: a prepared
+                              plan=None, tilted_axis=None):
+    """Differentiable ``backpropagate_3d`` (or, with ``tilted_axis``,
+    ``backpropagate_3d_tilted``) for a complex64 CUDA sinogram tensor
+    (A, Ny, Nx).  ``gain``: optional float32 CUDA tensor of the padded
+    spectrum shape multiplying the filter.  ``plan``: a prepared
     :class:`Backprop3D` to reuse (built from the arguments otherwise).
-    Returns the complex64 volume (Nx, Ny, Nx), indexed [z, y, x]."""
+    Spline orders 0..3.  Returns the complex64 volume (Nx, Ny, Nx), indexed
+    [z, y, x]."""
     if plan is None:
         plan = Backprop3D(tuple(sino.shape), np.asarray(angles), res, nm,
-                          lD=lD, weight_angles=weight_angles,
+                          lD=lD, tilted_axis=tilted_axis,
+                          weight_angles=weight_angles,
                           padding=padding, padfac=padfac, padval=padval,
                           intp_order=intp_order, input_dtype="complex64",
                           device=sino.device)

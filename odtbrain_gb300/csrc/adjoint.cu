@@ -43,7 +43,13 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_adj_rows(StageParams P, L line
     const int qq = q0 + (int)((valid ? rid : 0) / ny);
     const int y = (int)((valid ? rid : 0) % ny);
     const int a = qq / nz, p = qq % nz;
-    const float2 *src = sgrad + (((size_t)a * ny + y) * nz + p) * nx;
+    // slab gradient of (a, y, p, xx): [a][y][z][x] from the y-axis
+    // resampling transpose, the forward slab layout [a][z][x][ypitch] from
+    // the tilted one
+    const bool tl = P.tilted != 0;
+    const float2 *src = tl ? sgrad + ((size_t)a * nz + p) * nx * P.ypitch + y
+                           : sgrad + (((size_t)a * ny + y) * nz + p) * nx;
+    const size_t xstep = tl ? (size_t)P.ypitch : 1;
     if (threadIdx.x < 2 * LPC)
         red[threadIdx.x] = make_float2(0.f, 0.f);
     __syncthreads();
@@ -56,7 +62,7 @@ __global__ void __launch_bounds__(LPC * L::TPL) k_adj_rows(StageParams P, L line
         const int xx = x - padxl;
         float2 t = make_float2(0.f, 0.f);
         if (valid && x < n && xx >= 0 && xx < nx) {
-            t = src[xx];
+            t = src[xx * xstep];
             if (pf && xx < ZPOW_N) {
                 const float zz = P.tab.zpow[xx];
                 gA.x = fmaf(zz, t.x, gA.x);
@@ -122,11 +128,15 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_columns(StageParams P, L li
     const int xs = xslots<true>(n);
     float2 *buf0 = smem, *buf1 = smem + KX * xs, *tw = smem + 2 * KX * xs;
     float2 *stp = tw + tw_slots(n);  // [n][KX]
+    float2 *red = stp + n * KX;      // [KX][2] y-prefilter boundary sums
     copy_twiddles<L>(tw, P.tab.twy, n);
     const int c = threadIdx.x % KX, j = threadIdx.x / KX;
     const int kx = blockIdx.x * KX + c;
     const bool colok = kx < P.lNx;
     const int lNx = P.lNx, nz = P.nz, ny = P.ny, padyl = P.padyl;
+    // tilted path: the forward's y-prefilter boundary terms (from the four
+    // samples around the crop's ends) are transposed before the FFT
+    const bool yfix = P.order >= 2 && P.tilted;
     const int qb = q0 + blockIdx.y * ppc;
     const int qe = min(q0 + qn, qb + ppc);
     const bool pf = P.order >= 2;
@@ -175,6 +185,55 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_columns(StageParams P, L li
         for (int r = 0; r < L::SLOTS; ++r) {
             const int yy = j + r * L::TPL - padyl;
             v[r] = (colok && yy >= 0 && yy < ny) ? src[(size_t)yy * lNx] : make_float2(0.f, 0.f);
+        }
+        if (yfix) {
+            // out[yy] = u[padyl + yy] + A z^yy + B z^(ny-1-yy), with A, B from
+            // d0 = u[e0] - u[e1], d1 = u[e3] - u[e2]: collect the cotangent's
+            // weighted sums gA, gB over the column, then scatter
+            // (ca gA + cb gB) and (cb gA + ca gB) onto the four samples
+            float2 gA = make_float2(0.f, 0.f), gB = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int yy = j + r * L::TPL - padyl;
+                if (yy >= 0 && yy < ny) {
+                    if (yy < ZPOW_N) {
+                        const float zz = P.tab.zpow[yy];
+                        gA = make_float2(fmaf(zz, v[r].x, gA.x), fmaf(zz, v[r].y, gA.y));
+                    }
+                    if (ny - 1 - yy < ZPOW_N) {
+                        const float zz = P.tab.zpow[ny - 1 - yy];
+                        gB = make_float2(fmaf(zz, v[r].x, gB.x), fmaf(zz, v[r].y, gB.y));
+                    }
+                }
+            }
+            __syncthreads();  // the previous plane's reads of red are done
+            if (j == 0) {
+                red[c * 2] = make_float2(0.f, 0.f);
+                red[c * 2 + 1] = make_float2(0.f, 0.f);
+            }
+            __syncthreads();
+            if (gA.x != 0.f || gA.y != 0.f) {
+                atomicAdd(&red[c * 2].x, gA.x);
+                atomicAdd(&red[c * 2].y, gA.y);
+            }
+            if (gB.x != 0.f || gB.y != 0.f) {
+                atomicAdd(&red[c * 2 + 1].x, gB.x);
+                atomicAdd(&red[c * 2 + 1].y, gB.y);
+            }
+            __syncthreads();
+            const float2 A = red[c * 2], B = red[c * 2 + 1];
+            const float2 d0g = make_float2(P.by_ca * A.x + P.by_cb * B.x, P.by_ca * A.y + P.by_cb * B.y);
+            const float2 d1g = make_float2(P.by_cb * A.x + P.by_ca * B.x, P.by_cb * A.y + P.by_ca * B.y);
+            const int e0 = (padyl - 1 + n) % n, e1 = (padyl + 1) % n;
+            const int e2 = (padyl + ny - 2 + n) % n, e3 = (padyl + ny) % n;
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r) {
+                const int yq = j + r * L::TPL;
+                if (yq == e0) v[r] = v[r] + d0g;
+                if (yq == e1) v[r] = v[r] - d0g;
+                if (yq == e3) v[r] = v[r] + d1g;
+                if (yq == e2) v[r] = v[r] - d1g;
+            }
         }
         line.template run<-1, true>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
         const float zl = (pf && p < ZPOW_N) ? P.tab.zpow[p] : 0.f;
@@ -368,7 +427,8 @@ static size_t smem_adj_rows(int n)
 template <class L>
 static size_t smem_adj_cols(int n)
 {
-    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + Cfg<L>::KX * n + tw_slots(n)) * sizeof(float2);
+    return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + Cfg<L>::KX * n + tw_slots(n) + 2 * Cfg<L>::KX) *
+           sizeof(float2);
 }
 
 template <class L>

@@ -54,17 +54,134 @@ constexpr size_t kAlign = 256;
 
 size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
-// Spline pole and transfer function Bhat(w) of the sampled B-spline
-// (order 2: [1 6 1]/8, order 3: [1 4 1]/6).
-double spline_pole(int order) { return order == 2 ? std::sqrt(8.0) - 3.0 : std::sqrt(3.0) - 2.0; }
-double spline_bhat(int order, double w)
+// The sampled centred B-spline of order 2..5, t[0] + t[1] (z + 1/z) +
+// t[2] (z^2 + 1/z^2): [1 6 1]/8, [1 4 1]/6, [1 76 230 76 1]/384,
+// [1 26 66 26 1]/120 (the kernel scipy.ndimage's prefilter inverts).
+struct SplineTaps {
+    double t[3];
+    int npoles;  // 1 for orders 2, 3; 2 for orders 4, 5
+};
+SplineTaps spline_taps(int order)
 {
-    return order == 2 ? (6.0 + 2.0 * std::cos(w)) / 8.0 : (4.0 + 2.0 * std::cos(w)) / 6.0;
+    switch (order) {
+    case 2: return {{6.0 / 8.0, 1.0 / 8.0, 0.0}, 1};
+    case 3: return {{4.0 / 6.0, 1.0 / 6.0, 0.0}, 1};
+    case 4: return {{230.0 / 384.0, 76.0 / 384.0, 1.0 / 384.0}, 2};
+    default: return {{66.0 / 120.0, 26.0 / 120.0, 1.0 / 120.0}, 2};
+    }
 }
 
-// Coefficients of the boundary solve for a cropped line of length n: with
-// d0 = u[-1] - u[1] and d1 = u[n] - u[n-2], the homogeneous correction
-// A z^k + B z^(n-1-k) has A = ca*d0 + cb*d1 and B = ca*d1 + cb*d0.
+// Transfer function Bhat(w) of the sampled B-spline.
+double spline_bhat(int order, double w)
+{
+    const SplineTaps T = spline_taps(order);
+    return T.t[0] + 2.0 * T.t[1] * std::cos(w) + 2.0 * T.t[2] * std::cos(2.0 * w);
+}
+
+// Poles of the prefilter (the roots of the kernel's polynomial inside the
+// unit circle), largest magnitude first.
+int spline_poles(int order, double *z)
+{
+    const SplineTaps T = spline_taps(order);
+    if (T.npoles == 1) {
+        // t1 z^2 + t0 z + t1 = 0
+        z[0] = (-T.t[0] + std::sqrt(T.t[0] * T.t[0] - 4.0 * T.t[1] * T.t[1])) / (2.0 * T.t[1]);
+        return 1;
+    }
+    // with s = z + 1/z: t2 s^2 + t1 s + (t0 - 2 t2) = 0, then z^2 - s z + 1 = 0;
+    // the root inside the unit circle as 2 / (s - sqrt(s^2 - 4)) (s < -2)
+    const double disc = std::sqrt(T.t[1] * T.t[1] - 4.0 * T.t[2] * (T.t[0] - 2.0 * T.t[2]));
+    const double s1 = (-T.t[1] + disc) / (2.0 * T.t[2]), s2 = (-T.t[1] - disc) / (2.0 * T.t[2]);
+    z[0] = 2.0 / (s1 - std::sqrt(s1 * s1 - 4.0));
+    z[1] = 2.0 / (s2 - std::sqrt(s2 * s2 - 4.0));
+    return 2;
+}
+
+// Boundary solve of the prefilter folded into the transforms.  A line of n
+// samples whose Fourier components were divided by Bhat (the particular
+// solution c_p, known also beyond the line's ends) becomes scipy's
+// mirror-boundary prefiltered line c = c_p + h with
+//   h[k] = sum_i A_i z_i^k + B_i z_i^(n-1-k),
+// where the coefficients follow from the kernel's equations at the first
+// and last npoles samples, written with mirrored neighbours:
+//   (A_1..A_np, B_1..B_np) = K (d_1L..d_npL, d_1R..d_npR),
+//   d_mL = c_p[m] - c_p[-m],   d_mR = c_p[n-1-m] - c_p[n-1+m].
+// K (row-major, 2np x 2np) is returned; false if the system is singular.
+bool boundary_matrix(int order, int n, double *K)
+{
+    const SplineTaps T = spline_taps(order);
+    double z[2];
+    const int np = spline_poles(order, z), n2 = 2 * np;
+    double M[4][4] = {}, R[4][4] = {};
+    auto mirror = [&](int m) {
+        if (n == 1)
+            return 0;
+        const int P = 2 * n - 2;
+        m = std::abs(m) % P;
+        return m < n ? m : P - m;
+    };
+    auto add_h = [&](int eq, double t, int k) {  // t * h[k]
+        for (int i = 0; i < np; ++i) {
+            M[eq][i] += t * std::pow(z[i], k);
+            M[eq][np + i] += t * std::pow(z[i], n - 1 - k);
+        }
+    };
+    int eq = 0;
+    for (int q = 0; q < np; ++q, ++eq) {  // samples q (left) ...
+        for (int k = -np; k <= np; ++k) {
+            const int m = q + k;
+            add_h(eq, T.t[std::abs(k)], mirror(m));
+            if (m < 0)
+                R[eq][-m - 1] -= T.t[std::abs(k)];
+        }
+    }
+    for (int q = 0; q < np; ++q, ++eq) {  // ... and n-1-q (right)
+        for (int k = -np; k <= np; ++k) {
+            const int m = n - 1 - q + k;
+            add_h(eq, T.t[std::abs(k)], mirror(m));
+            if (m > n - 1)
+                R[eq][np + (m - (n - 1)) - 1] -= T.t[std::abs(k)];
+        }
+    }
+    // K = M^-1 R by Gauss-Jordan elimination with partial pivoting
+    for (int c = 0; c < n2; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n2; ++r)
+            if (std::fabs(M[r][c]) > std::fabs(M[piv][c]))
+                piv = r;
+        if (!(std::fabs(M[piv][c]) > 1e-300))
+            return false;
+        for (int j = 0; j < n2; ++j) {
+            std::swap(M[c][j], M[piv][j]);
+            std::swap(R[c][j], R[piv][j]);
+        }
+        const double inv = 1.0 / M[c][c];
+        for (int j = 0; j < n2; ++j) {
+            M[c][j] *= inv;
+            R[c][j] *= inv;
+        }
+        for (int r = 0; r < n2; ++r) {
+            if (r == c)
+                continue;
+            const double f = M[r][c];
+            for (int j = 0; j < n2; ++j) {
+                M[r][j] -= f * M[c][j];
+                R[r][j] -= f * R[c][j];
+            }
+        }
+    }
+    for (int r = 0; r < n2; ++r)
+        for (int j = 0; j < n2; ++j) {
+            K[r * n2 + j] = R[r][j];
+            if (!std::isfinite(R[r][j]))
+                return false;
+        }
+    return true;
+}
+
+// Coefficients of the one-pole boundary solve in the form the adjoint
+// kernels use: with d0 = u[-1] - u[1] and d1 = u[n] - u[n-2], the
+// correction A z^k + B z^(n-1-k) has A = ca*d0 + cb*d1 and B = ca*d1 + cb*d0.
 void boundary_solve(double z, int n, double *ca, double *cb)
 {
     const double a = z - 1.0 / z;
@@ -97,7 +214,9 @@ struct odt_bpp3d_plan {
     int jobs;        // (angle, plane) jobs per column/row launch
     size_t off_rowspec, off_T, off_T2, off_Tab, off_slab, off_comp, off_rot, ws_bytes;
     size_t off_Qg, off_W, off_Pg, adj_ws_bytes;  // adjoint-only regions after ws_bytes
-    double bx_ca, bx_cb, by_ca, by_cb;
+    double bx_ca, bx_cb, by_ca, by_cb;  // one-pole solve in the adjoint's form
+    int npoles;                         // prefilter poles: 0, 1 or 2
+    float kx_solve[16], ky_solve[16];   // boundary_matrix of x and y lines
     int kx_zero_lo, kx_zero_hi;  // all-zero spectrum columns [lo, hi)
     int col_slots;               // resident column-stage CTAs (occupancy x SMs)
     // device tables (one allocation)
@@ -163,6 +282,11 @@ StageParams stage_params(const odt_bpp3d_plan *p)
     P.bx_cb = (float)p->bx_cb;
     P.by_ca = (float)p->by_ca;
     P.by_cb = (float)p->by_cb;
+    P.npoles = p->npoles;
+    for (int i = 0; i < 16; ++i) {
+        P.kxs[i] = p->kx_solve[i];
+        P.kys[i] = p->ky_solve[i];
+    }
     P.ypitch = odt::yaxis_slab_pitch(d.ny);
     P.col_slots = p->col_slots;
     P.zshift = (float)d.z_shift;
@@ -192,8 +316,8 @@ odt_status validate(const odt_bpp3d_desc *d)
         return fail(ODT_ERR_INVALID_ARGUMENT, "unknown input dtype");
     if (d->intp_order < 0 || d->intp_order > 5)
         return fail(ODT_ERR_INVALID_ARGUMENT, "intp_order must be in 0..5");
-    if (d->intp_order > 3)
-        return fail(ODT_ERR_UNSUPPORTED, "spline orders 4 and 5 are not implemented on the GPU");
+    if (d->intp_order >= 4 && (d->nx < 4 || (d->geometry == ODT_GEOM_AFFINE3D && d->ny > 1 && d->ny < 4)))
+        return fail(ODT_ERR_UNSUPPORTED, "spline orders 4 and 5 need lines of at least 4 samples");
     if (!std::isfinite(d->z_shift) || std::fabs(d->z_shift) > 1.0 || 2.0 * d->z_shift != std::rint(2.0 * d->z_shift))
         return fail(ODT_ERR_INVALID_ARGUMENT, "z_shift must be 0, +-0.5 or +-1");
     if (!odt::line_size_supported(d->pad_nx) || !odt::line_size_supported(d->pad_ny))
@@ -246,19 +370,40 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     const size_t K = (size_t)lNy * lNx;
 
     // ---- FP64 host tables -> FP32 device tables
-    std::vector<float2> G(K), W(K), S(K), AL(K), BE(K), twx(lNx), twy(lNy);
-    std::vector<float> zp(odt::ZPOW_N, 0.f);
-    const double z1 = pf ? spline_pole(order) : 0.0;
-    double za_ca = 0, za_cb = 0;
+    // prefilter (order >= 2): npoles poles; per pole the z-boundary tables
+    // alpha_i, beta_i (planes) and the powers z_i^m
+    double zpole[2] = {0.0, 0.0};
+    const int np = pf ? spline_poles(order, zpole) : 0;
+    p->npoles = np;
+    std::vector<float2> G(K), W(K), S(K), AL((size_t)2 * K), BE((size_t)2 * K), twx(lNx), twy(lNy);
+    std::vector<float> zp((size_t)2 * odt::ZPOW_N, 0.f);
+    double Kz[16] = {0}, Kx[16] = {0}, Ky[16] = {0};
+    std::memset(p->kx_solve, 0, sizeof p->kx_solve);
+    std::memset(p->ky_solve, 0, sizeof p->ky_solve);
     if (pf) {
-        boundary_solve(z1, nz, &za_ca, &za_cb);
-        boundary_solve(z1, d.nx, &p->bx_ca, &p->bx_cb);
+        bool ok = boundary_matrix(order, nz, Kz) && boundary_matrix(order, d.nx, Kx);
         if (d.ny >= 2)
-            boundary_solve(z1, d.ny, &p->by_ca, &p->by_cb);
-        double zz = 1.0;
-        for (int m = 0; m < odt::ZPOW_N; ++m) {
-            zp[m] = (float)zz;
-            zz *= z1;
+            ok = ok && boundary_matrix(order, d.ny, Ky);
+        if (!ok) {
+            delete p;
+            return fail(ODT_ERR_UNSUPPORTED, "the spline prefilter's boundary system is singular for these sizes");
+        }
+        for (int i = 0; i < 16; ++i) {
+            p->kx_solve[i] = (float)Kx[i];
+            p->ky_solve[i] = (float)Ky[i];
+        }
+        if (np == 1) {
+            // the adjoint kernels' form of the one-pole solve
+            boundary_solve(zpole[0], d.nx, &p->bx_ca, &p->bx_cb);
+            if (d.ny >= 2)
+                boundary_solve(zpole[0], d.ny, &p->by_ca, &p->by_cb);
+        }
+        for (int i = 0; i < np; ++i) {
+            double zz = 1.0;
+            for (int m = 0; m < odt::ZPOW_N; ++m) {
+                zp[(size_t)i * odt::ZPOW_N + m] = (float)zz;
+                zz *= zpole[i];
+            }
         }
     }
     // positions of the first and last planes (the z-prefilter boundary terms
@@ -278,19 +423,32 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
             const float whi = (float)w;
             W[k] = make_float2(whi, (float)(w - (double)whi));
             S[k] = make_float2((float)std::cos(w), (float)std::sin(w));
+            for (int i = 0; i < 2; ++i) {
+                AL[(size_t)i * K + k] = make_float2(0.f, 0.f);
+                BE[(size_t)i * K + k] = make_float2(0.f, 0.f);
+            }
             if (pf) {
+                // along z the particular solution of plane p is exp(i w z_p):
+                // d_mL = e(z_first) 2i sin(m w), d_mR = -e(z_last) 2i sin(m w)
                 const std::complex<double> I(0.0, 1.0);
                 const std::complex<double> e0 = std::exp(I * (w * z_first));
                 const std::complex<double> en = std::exp(I * (w * z_last));
-                const std::complex<double> d0 = e0 * (-2.0 * std::sin(w)) * I;
-                const std::complex<double> d1 = en * (2.0 * std::sin(w)) * I;
-                const std::complex<double> al = za_ca * d0 + za_cb * d1;
-                const std::complex<double> be = za_ca * d1 + za_cb * d0;
-                AL[k] = make_float2((float)al.real(), (float)al.imag());
-                BE[k] = make_float2((float)be.real(), (float)be.imag());
-            } else {
-                AL[k] = make_float2(0.f, 0.f);
-                BE[k] = make_float2(0.f, 0.f);
+                std::complex<double> dv[4];
+                for (int m = 1; m <= np; ++m) {
+                    dv[m - 1] = e0 * (2.0 * std::sin(m * w)) * I;
+                    dv[np + m - 1] = en * (-2.0 * std::sin(m * w)) * I;
+                }
+                const int n2 = 2 * np;
+                for (int r = 0; r < n2; ++r) {
+                    std::complex<double> c = 0.0;
+                    for (int j = 0; j < n2; ++j)
+                        c += Kz[r * n2 + j] * dv[j];
+                    const float2 cf = make_float2((float)c.real(), (float)c.imag());
+                    if (r < np)
+                        AL[(size_t)r * K + k] = cf;
+                    else
+                        BE[(size_t)(r - np) * K + k] = cf;
+                }
             }
         }
     }
@@ -325,11 +483,11 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     const size_t oG = o; o = align_up(o + K * 8);
     const size_t oW = o; o = align_up(o + K * 8);
     const size_t oS = o; o = align_up(o + K * 8);
-    const size_t oA = o; o = align_up(o + K * 8);
-    const size_t oB = o; o = align_up(o + K * 8);
+    const size_t oA = o; o = align_up(o + 2 * K * 8);
+    const size_t oB = o; o = align_up(o + 2 * K * 8);
     const size_t oTx = o; o = align_up(o + (size_t)lNx * 8);
     const size_t oTy = o; o = align_up(o + (size_t)lNy * 8);
-    const size_t oZ = o; o = align_up(o + odt::ZPOW_N * 4);
+    const size_t oZ = o; o = align_up(o + 2 * odt::ZPOW_N * 4);
     const size_t oSt = o; o = align_up(o + 16);
     {
         std::lock_guard<std::mutex> lock(g_debug_mutex);
@@ -352,9 +510,9 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     }
     char *base = (char *)p->d_tables;
     struct Up { size_t off; const void *src; size_t n; } ups[] = {
-        {oG, G.data(), K * 8}, {oW, W.data(), K * 8}, {oS, S.data(), K * 8}, {oA, AL.data(), K * 8},
-        {oB, BE.data(), K * 8}, {oTx, twx.data(), (size_t)lNx * 8}, {oTy, twy.data(), (size_t)lNy * 8},
-        {oZ, zp.data(), odt::ZPOW_N * 4}};
+        {oG, G.data(), K * 8}, {oW, W.data(), K * 8}, {oS, S.data(), K * 8}, {oA, AL.data(), 2 * K * 8},
+        {oB, BE.data(), 2 * K * 8}, {oTx, twx.data(), (size_t)lNx * 8}, {oTy, twy.data(), (size_t)lNy * 8},
+        {oZ, zp.data(), 2 * odt::ZPOW_N * 4}};
     for (const Up &u : ups) {
         e = cudaMemcpy(base + u.off, u.src, u.n, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) {
@@ -386,7 +544,7 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     // gradients [y][z][x] fit too)
     const size_t slab_bytes = (size_t)nz * odt::yaxis_slab_pitch(d.ny) * d.nx * 8;
     const size_t rowspec_bytes = (size_t)lNy * lNx * 8;              // one angle's row spectra
-    const size_t tab_bytes = pf ? (size_t)2 * d.ny * lNx * 8 : 0;    // one angle's z-boundary rows
+    const size_t tab_bytes = pf ? (size_t)2 * np * d.ny * lNx * 8 : 0;  // one angle's z-boundary rows
     const size_t vol_bytes = (size_t)nz * d.ny * d.nx * 8;           // compensation buffer
     const uint64_t limit = d.workspace_limit ? d.workspace_limit : kDefaultWorkspace;
     // chunk buffers take at most a quarter of the limit, so tight limits
@@ -467,7 +625,7 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
     }
     if (e == cudaSuccess && !tilted)
         e = odt::configure_rotate_kernels();
-    if (e == cudaSuccess && !tilted)
+    if (e == cudaSuccess)
         e = odt::configure_adjoint_kernels(P);
     if (e == cudaSuccess && !tilted)
         e = odt::configure_rotate_adjoint_kernels();
@@ -700,8 +858,8 @@ odt_status odt_bpp3d_adjoint_workspace_size(const odt_bpp3d_plan *plan, uint64_t
 {
     if (!plan || !bytes)
         return fail(ODT_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (plan->d.geometry != ODT_GEOM_Y_AXIS)
-        return fail(ODT_ERR_UNSUPPORTED, "the adjoint is implemented for the y-axis geometry");
+    if (plan->d.intp_order > 3)
+        return fail(ODT_ERR_UNSUPPORTED, "the adjoint is implemented for spline orders 0..3");
     *bytes = plan->adj_ws_bytes;
     return ODT_OK;
 }
@@ -723,10 +881,12 @@ odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const
     if (dst != ODT_OK)
         return dst;
     const odt_bpp3d_desc &d = plan->d;
-    if (d.geometry != ODT_GEOM_Y_AXIS)
-        return fail(ODT_ERR_UNSUPPORTED, "the adjoint is implemented for the y-axis geometry");
+    const bool tilted = d.geometry == ODT_GEOM_AFFINE3D;
+    const int geo_stride = tilted ? 12 : 6;
     if (d.onlyreal)
         return fail(ODT_ERR_UNSUPPORTED, "the adjoint needs a complex (onlyreal=0) plan");
+    if (d.intp_order > 3)
+        return fail(ODT_ERR_UNSUPPORTED, "the adjoint is implemented for spline orders 0..3");
     cudaStream_t s = (cudaStream_t)stream;
     StageParams P = stage_params(plan);
     P.gain = gain;
@@ -760,8 +920,8 @@ odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const
         R.last_pass = 1;
         R.onlyreal = 0;
         R.status = plan->d_status;
-        e = odt::launch_rotate_adjoint(R, d.intp_order, 0, (const float2 *)vol_grad, geometry + (size_t)a0 * 6, slab,
-                                       ws + plan->off_rot, s);
+        e = odt::launch_rotate_adjoint(R, d.intp_order, tilted ? 1 : 0, (const float2 *)vol_grad,
+                                       geometry + (size_t)a0 * geo_stride, slab, ws + plan->off_rot, s);
         if (e != cudaSuccess)
             return cuda_fail(e, "rotate_adjoint launch");
         if (gain_grad || angle_gain_grad) {

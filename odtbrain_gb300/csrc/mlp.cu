@@ -588,6 +588,189 @@ __global__ void __launch_bounds__(32 * BWD_WARPS) k_mlp_backward_data(MlpWeights
 }
 
 // ---------------------------------------------------------------------------
+// Backward, data part, on tcgen05: one warp group (128 threads) per CTA
+// carries a tile of 128 points (thread = point = TMEM lane).  The forward is
+// recomputed with the pre-activations Z1, Z2, Z3 left in TMEM columns
+// [0, 64), [64, 128), [128, 192); the back-propagated products dH3, dH2,
+// dH1 (dZ times the transposed weights) land in columns [192, 256).  Every
+// layer input and pre-activation gradient is stored in BF16 (MlpStore) for
+// the weight-gradient kernels, exactly as k_mlp_backward_data stores them.
+constexpr uint32_t TB_TMEM_COLS = 256;
+
+struct SmemTb {
+    uint8_t a[128 * MLP_H * 2];            // the A operand, 128 x (16 or 64) BF16
+    uint8_t w2[MLP_H * MLP_H * 2], w3[MLP_H * MLP_H * 2];    // [out][in]
+    uint8_t w2t[MLP_H * MLP_H * 2], w3t[MLP_H * MLP_H * 2];  // [in][out]
+    uint8_t w1[MLP_H * MLP_IN * 2];        // 64 x 16
+    uint8_t w4t[MLP_H * MLP_OUTP * 2];     // 64 x 16 (W4 transposed)
+    float b1[MLP_H], b2[MLP_H], b3[MLP_H];
+    uint64_t bar;
+    uint32_t tmem_base;
+    int abort;
+};
+// at least 100 KB of shared memory, so that no more than two CTAs (the
+// 512 TMEM columns of an SM) share an SM: a third would wait in its TMEM
+// allocation
+constexpr size_t TB_SMEM = sizeof(SmemTb) + 1024 > 100 * 1024 ? sizeof(SmemTb) + 1024 : 100 * 1024;
+
+__device__ __forceinline__ float silu_grad_of(float z)
+{
+    const float sg = sigmoid(z);
+    return sg * (1.f + z * (1.f - sg));
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_backward_data_tc(MlpWeights W, MlpGrid Gd, const float2 *dgain,
+                                                                 MlpStore St)
+{
+    extern __shared__ uint8_t tb_smem_raw[];
+    SmemTb &S = *reinterpret_cast<SmemTb *>((reinterpret_cast<uintptr_t>(tb_smem_raw) + 1023) & ~(uintptr_t)1023);
+    const int row = threadIdx.x, warp = row >> 5;
+    tc_copy_kmajor(S.w1, W.w1, MLP_H, MLP_H, MLP_IN);
+    tc_copy_kmajor(S.w2, W.w2, MLP_H, MLP_H, MLP_H);
+    tc_copy_kmajor(S.w3, W.w3, MLP_H, MLP_H, MLP_H);
+    tc_copy_kmajor(S.w2t, W.w2t, MLP_H, MLP_H, MLP_H);
+    tc_copy_kmajor(S.w3t, W.w3t, MLP_H, MLP_H, MLP_H);
+    tc_copy_kmajor(S.w4t, W.w4t, MLP_H, MLP_H, MLP_OUTP);
+    for (int i = row; i < MLP_H; i += blockDim.x) {
+        S.b1[i] = W.b1[i];
+        S.b2[i] = W.b2[i];
+        S.b3[i] = W.b3[i];
+    }
+    if (row == 0) {
+        mbar_init(&S.bar, 1);
+        S.abort = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0)
+        tc::tmem_alloc(&S.tmem_base, TB_TMEM_COLS);
+    fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t lane_base = S.tmem_base + ((uint32_t)(32 * warp) << 16);
+    const uint32_t a_s = smem_u32(S.a);
+    volatile int *abort = &S.abort;
+    uint32_t phase = 0;
+    // D (TMEM column col0) = A * B: K/16 MMAs issued by thread 0, then the
+    // tile waits for them
+    auto mma_into = [&](uint32_t col0, const uint8_t *b, int kchunks, int N) {
+        fence_proxy_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (row == 0) {
+            tc::fence_after_sync();
+            const uint32_t sbo = 128u * kchunks, b_s = smem_u32(b);
+            for (int k = 0; k < kchunks / 2; ++k)
+                tc::mma(S.tmem_base + col0, tc::smem_desc(a_s + 256u * k, 128u, sbo),
+                        tc::smem_desc(b_s + 256u * k, 128u, sbo), tc::idesc_bf16(128, N), k > 0 ? 1u : 0u);
+            tc::commit(&S.bar);
+        }
+        const bool ok = !*abort && mbar_wait(&S.bar, phase, kTcWaitNs);
+        phase ^= 1u;
+        if (!ok)
+            *abort = 1;
+        tc::fence_after_sync();
+    };
+    // 64 columns of this thread's lane from column col0
+    auto ld64 = [&](uint32_t col0, uint32_t (&r)[4][16]) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            tc::tmem_ld16(lane_base + col0 + 16u * c, r[c]);
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            tc::tmem_wait(r[c]);
+    };
+    // 8 BF16 values as one 16-byte chunk of the A operand (K = 64) and of
+    // the store row
+    auto put8 = [&](const float (&v)[8], int c, __nv_bfloat16 *grow) {
+        const uint4 q = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                                   pack_bf16(v[6], v[7]));
+        *reinterpret_cast<uint4 *>(S.a + tc::kmaj(row, c, 8)) = q;
+        if (grow)
+            reinterpret_cast<uint4 *>(grow)[c] = q;
+    };
+    const long long P = Gd.P;
+    const long long ntiles = (P + 127) / 128;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const long long p = t * 128 + row;
+        const bool valid = p < P;
+        float f[4] = {0.f, 0.f, 0.f, 0.f};
+        if (valid)
+            point_features(Gd, p, f);
+        const uint4 h0 = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), 0u, 0u);
+        *reinterpret_cast<uint4 *>(S.a + tc::kmaj(row, 0, 2)) = h0;
+        *reinterpret_cast<uint4 *>(S.a + tc::kmaj(row, 1, 2)) = make_uint4(0u, 0u, 0u, 0u);
+        if (valid) {
+            reinterpret_cast<uint4 *>(St.h0 + p * MLP_IN)[0] = h0;
+            reinterpret_cast<uint4 *>(St.h0 + p * MLP_IN)[1] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        // forward: Z_l in TMEM, H_l = SiLU(Z_l + b_l) stored and fed on
+        const uint8_t *wf[3] = {S.w1, S.w2, S.w3};
+        const float *bf[3] = {S.b1, S.b2, S.b3};
+        __nv_bfloat16 *hs[3] = {St.h1, St.h2, St.h3};
+#pragma unroll 1
+        for (int l = 0; l < 3; ++l) {
+            mma_into(64u * l, wf[l], l == 0 ? MLP_IN / 8 : MLP_H / 8, 64);
+            uint32_t r[4][16];
+            ld64(64u * l, r);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                float v[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    v[i] = silu(__uint_as_float(r[c >> 1][(c & 1) * 8 + i]) + bf[l][8 * c + i]);
+                put8(v, c, valid ? hs[l] + p * MLP_H : nullptr);
+            }
+        }
+        // output gradient (d out_re, d out_im) as A (K = 16)
+        const long long gi = valid ? gain_index(Gd, p) : -1;
+        const float2 d = gi >= 0 ? dgain[gi] : make_float2(0.f, 0.f);
+        const uint4 dz4 = make_uint4(pack_bf16(d.x, d.y), 0u, 0u, 0u);
+        *reinterpret_cast<uint4 *>(S.a + tc::kmaj(row, 0, 2)) = dz4;
+        *reinterpret_cast<uint4 *>(S.a + tc::kmaj(row, 1, 2)) = make_uint4(0u, 0u, 0u, 0u);
+        if (valid) {
+            reinterpret_cast<uint4 *>(St.dz4 + p * MLP_OUTP)[0] = dz4;
+            reinterpret_cast<uint4 *>(St.dz4 + p * MLP_OUTP)[1] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        // backward: dH_l = dZ_{l+1} W_{l+1} (transposed weights as B), then
+        // dZ_l = dH_l * SiLU'(Z_l + b_l)
+        const uint8_t *wt[3] = {S.w4t, S.w3t, S.w2t};
+        __nv_bfloat16 *dzs[3] = {St.dz3, St.dz2, St.dz1};
+#pragma unroll 1
+        for (int k = 0; k < 3; ++k) {
+            const int l = 2 - k;  // the layer whose dZ this step forms
+            mma_into(192u, wt[k], k == 0 ? MLP_OUTP / 8 : MLP_H / 8, 64);
+            uint32_t g[4][16], z[4][16];
+            ld64(192u, g);
+            ld64(64u * l, z);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                float v[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const float zz = __uint_as_float(z[c >> 1][(c & 1) * 8 + i]) + bf[l][8 * c + i];
+                    v[i] = __uint_as_float(g[c >> 1][(c & 1) * 8 + i]) * silu_grad_of(zz);
+                }
+                put8(v, c, valid ? dzs[k] + p * MLP_H : nullptr);
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (*abort) {
+        if (row == 0) {
+            mbar_wait(&S.bar, phase ^ 1u, kTcWaitNs);
+            atomicOr(&g_mlp_status, 1);
+        }
+        __syncthreads();
+    }
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(S.tmem_base, TB_TMEM_COLS);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Weight gradients of an M x N layer (M = 16*MT output rows including the
 // padding, N = 8*NT inputs): dW[m][n] = sum_p DZ[p][m] H[p][n] and
 // db[m] = sum_p DZ[p][m].  A CTA reduces a contiguous chunk of points; warp w
@@ -831,9 +1014,29 @@ odt_status odt_mlp_gain_backward(const odt_mlp_params *params, int32_t num_angle
     const long long groups = (P + 15) / 16;
     const long long want = (groups + BWD_WARPS - 1) / BWD_WARPS;
     const long long cap = 4LL * sms;
-    k_mlp_backward_data<<<(unsigned)(want < cap ? want : cap), 32 * BWD_WARPS, 0, s>>>(
-        W, Gd, (const float2 *)gain_grad, S);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaSuccess;
+    if (kMlpTensorMemory) {
+        static thread_local int configured_device = -1;
+        int dev = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess && configured_device != dev) {
+            e = cudaFuncSetAttribute(k_mlp_backward_data_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)TB_SMEM);
+            if (e == cudaSuccess)
+                configured_device = dev;
+        }
+        if (e != cudaSuccess)
+            return err(ODT_ERR_CUDA, std::string("k_mlp_backward_data_tc configuration: ") + cudaGetErrorString(e));
+        // two CTAs (256 TMEM columns each) per SM
+        const long long tiles = (P + 127) / 128;
+        const long long tcap = 2LL * sms;
+        k_mlp_backward_data_tc<<<(unsigned)(tiles < tcap ? tiles : tcap), 128, TB_SMEM, s>>>(
+            W, Gd, (const float2 *)gain_grad, S);
+    } else {
+        k_mlp_backward_data<<<(unsigned)(want < cap ? want : cap), 32 * BWD_WARPS, 0, s>>>(
+            W, Gd, (const float2 *)gain_grad, S);
+    }
+    e = cudaGetLastError();
     if (e != cudaSuccess)
         return err(ODT_ERR_CUDA, std::string("k_mlp_backward_data: ") + cudaGetErrorString(e));
     // split-K over the points: about two chunks per SM

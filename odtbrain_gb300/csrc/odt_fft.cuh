@@ -258,7 +258,8 @@ struct GenericLine {
     int n;
     __device__ __forceinline__ int size() const { return n; }
 
-    template <int DIR, bool PAD = false>
+    // (TW2 is accepted for a uniform interface; the direct DFT has no passes)
+    template <int DIR, bool PAD = false, bool TW2 = false>
     __device__ __forceinline__ void run(float2 (&v)[16], int j, float2 *line0, float2 *line1, int es,
                                         const float2 *tw, int &flip, int bar = 0) const
     {

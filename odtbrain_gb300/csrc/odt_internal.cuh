@@ -35,18 +35,19 @@ enum : int {
 };
 
 // Number of boundary-correction terms of the B-spline prefilter that are
-// applied; the pole satisfies |z|^24 < 2e-14, below FP32 resolution.
+// applied; every pole (largest: order 5, |z| = 0.431) satisfies |z|^24 <
+// 2e-9, below FP32 resolution of the corrected values.
 constexpr int ZPOW_N = 24;
 
 struct FilterTables {
     const float2 *G;      // [lNy*lNx] filter * prefilter particular factors
     const float2 *wsplit; // [lNy*lNx] propagator phase km*(M-1): (hi, lo)
     const float2 *step;   // [lNy*lNx] exp(i*km*(M-1))
-    const float2 *alpha;  // [lNy*lNx] z-prefilter boundary term at p = 0
-    const float2 *beta;   // [lNy*lNx] z-prefilter boundary term at p = nz-1
+    const float2 *alpha;  // [pole][lNy*lNx] z-prefilter boundary terms from p = 0
+    const float2 *beta;   // [pole][lNy*lNx] z-prefilter boundary terms from p = nz-1
     const float2 *twx;    // [lNx] exp(-2 pi i m / lNx)
     const float2 *twy;    // [lNy] exp(-2 pi i m / lNy)
-    const float *zpow;    // [ZPOW_N] pole^m
+    const float *zpow;    // [pole][ZPOW_N] pole^m
 };
 
 struct StageParams {
@@ -59,8 +60,11 @@ struct StageParams {
     int in_c128;      // input sinogram is complex128
     int kx_zero_lo, kx_zero_hi;  // spectrum columns in [lo, hi) are all zero
                                  // (outside the |k| < km disc)
-    float bx_ca, bx_cb;  // x-prefilter boundary solve (n = nx)
+    float bx_ca, bx_cb;  // x-prefilter boundary solve (n = nx), one pole (adjoint)
     float by_ca, by_cb;  // y-prefilter boundary solve (n = ny; zero for ny = 1)
+    int npoles;          // prefilter poles: 1 (orders 2, 3), 2 (orders 4, 5)
+    float kxs[16];       // boundary solve of x lines: (A_i, B_i) = K d, 2np x 2np
+    float kys[16];       // the same for y lines (tilted path)
     int ypitch;          // slab [a][z][x][y]: y pitch (yaxis_slab_pitch:
                          // ny rounded up to a multiple of 32, 1 for ny == 1)
     int col_slots;       // resident CTAs of the column stage on the device

@@ -1396,11 +1396,153 @@ __global__ void __launch_bounds__(RA_THREADS, 1) k_rotate_y_adjoint(RotParams R,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Transpose of the tilted resampling (k_rotate_3d):
+//   slab_grad[a][Z][X][Y] += sum over outputs o of angle a whose (mirrored)
+//       taps include (Z, X, Y) of w0 w1 w2 * vol_grad[o]
+// in the forward's slab layout [a][z][x][y] (pitch R.ypitch).  The tiles,
+// FP32 coordinates, in/out decisions (FP64 re-evaluation near the domain
+// edge), tap starts and weights are those of k_rotate_3d, so this is the
+// exact transpose of the forward's arithmetic.  Each output pushes its
+// (ORDER+1)^3 taps with global atomic adds; the 32 lanes of a warp are
+// consecutive y, whose taps fall on nearly consecutive slab y, so a warp's
+// adds hit one or two 256-byte runs.  slab_grad must start at zero.
+template <int ORDER>
+__global__ void __launch_bounds__(256, ORDER >= 4 ? 2 : 4) k_rotate_3d_adjoint(RotParams R,
+                                                                            const float2 *__restrict__ vol_grad,
+                                                                            const double *__restrict__ geo,
+                                                                            float2 *slab_grad)
+{
+    __shared__ AxisCoord3 srec[R3_CHUNK][3];
+    __shared__ int sflag[R3_CHUNK][3];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nx = R.nx, ny = R.ny, nz = R.nz, yp = R.ypitch;
+    const int x0 = blockIdx.x * R3_X, y0 = blockIdx.y * R3_Y, z0 = blockIdx.z * R3_Z;
+    const int x = x0 + w, y = y0 + lane;
+    const bool vxy = x < nx && y < ny;
+    const bool full = x0 + R3_X <= nx && y0 + R3_Y <= ny && z0 + R3_Z <= nz;
+    const int n3[3] = {nx, ny, nz};
+    const size_t aslab = (size_t)nz * nx * yp;
+    const float d0 = (float)w, d1 = (float)(-lane);
+    const double o0 = (double)x, o1 = (double)(ny - 1 - y);
+    float2 gv[R3_Z];
+#pragma unroll
+    for (int q = 0; q < R3_Z; ++q) {
+        const int z = z0 + q;
+        gv[q] = (vxy && z < nz) ? __ldg(vol_grad + ((size_t)z * ny + y) * nx + x) : make_float2(0.f, 0.f);
+    }
+    const int nb = R.nbatch_angles;
+    for (int a0 = 0; a0 < nb; a0 += R3_CHUNK) {
+        const int na = min(R3_CHUNK, nb - a0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < na * 3; t += blockDim.x) {
+            const int aa = t / 3, i = t % 3;
+            const double *g = geo + 12 * (size_t)(a0 + aa);
+            const double m0 = g[3 * i], m1 = g[3 * i + 1], m2 = g[3 * i + 2];
+            const double c = ((g[9 + i] + m0 * (double)x0) + m1 * (double)(ny - 1 - y0)) + m2 * (double)z0;
+            srec[aa][i] = make_axis3(c, m0, m1, m2);
+            const double e0 = m0 * (R3_X - 1), e1 = -m1 * (R3_Y - 1), e2 = m2 * (R3_Z - 1);
+            const double lo = c + fmin(e0, 0.0) + fmin(e1, 0.0) + fmin(e2, 0.0);
+            const double hi = c + fmax(e0, 0.0) + fmax(e1, 0.0) + fmax(e2, 0.0);
+            sflag[aa][i] = (full && lo >= R3_LO<ORDER> && hi <= n3[i] - R3_HI<ORDER>) ? 1 : 0;
+        }
+        __syncthreads();
+        for (int aa = 0; aa < na; ++aa) {
+            const int a = a0 + aa;
+            const bool interior = sflag[aa][0] && sflag[aa][1] && sflag[aa][2];
+            const AxisCoord3 *axp = srec[aa];
+            float2 *sg = slab_grad + (size_t)a * aslab;
+            const double *g = geo + 12 * (size_t)a;
+#pragma unroll
+            for (int q = 0; q < R3_Z; ++q) {
+                const int z = z0 + q;
+                if (!vxy || z >= nz)
+                    continue;
+                const float d2 = (float)q;
+                int Ib[3];
+                float l[3];
+                l[0] = eval_axis3(axp[0], d0, d1, d2, Ib[0]);
+                l[1] = eval_axis3(axp[1], d0, d1, d2, Ib[1]);
+                l[2] = eval_axis3(axp[2], d0, d1, d2, Ib[2]);
+                const double o2 = (double)z;
+                auto exact = [&](int i) {
+                    return __dadd_rn(__dadd_rn(__dadd_rn(__ldg(g + 9 + i), __dmul_rn(__ldg(g + 3 * i), o0)),
+                                               __dmul_rn(__ldg(g + 3 * i + 1), o1)),
+                                     __dmul_rn(__ldg(g + 3 * i + 2), o2));
+                };
+                if (!interior) {
+                    bool in = true;
+#pragma unroll
+                    for (int i = 0; i < 3; ++i)
+                        in = in && inside_axis(l[i], Ib[i], n3[i], [&] { return exact(i); });
+                    if (!in)
+                        continue;
+                }
+                int t0[3];
+                float wt[3][ORDER + 1];
+                if (ORDER == 0) {
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        t0[i] = (int)floor(exact(i) + 0.5);
+                        wt[i][0] = 1.f;
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 3; ++i)
+                        t0[i] = Ib[i] + Spline<ORDER>::weights(l[i], wt[i]);
+                }
+                int ix[ORDER + 1], iy[ORDER + 1], iz[ORDER + 1];
+#pragma unroll
+                for (int k = 0; k <= ORDER; ++k) {
+                    ix[k] = interior ? t0[0] + k : mirror_idx(t0[0] + k, nx);
+                    iy[k] = ny - 1 - (interior ? t0[1] + k : mirror_idx(t0[1] + k, ny));
+                    iz[k] = interior ? t0[2] + k : mirror_idx(t0[2] + k, nz);
+                }
+                const float2 gq = gv[q];
+#pragma unroll
+                for (int k2 = 0; k2 <= ORDER; ++k2) {
+#pragma unroll
+                    for (int k0 = 0; k0 <= ORDER; ++k0) {
+                        float2 *col = sg + ((size_t)iz[k2] * nx + ix[k0]) * yp;
+                        const float w02 = wt[2][k2] * wt[0][k0];
+#pragma unroll
+                        for (int k1 = 0; k1 <= ORDER; ++k1) {
+                            const float wv = w02 * wt[1][k1];
+                            atomicAdd(&col[iy[k1]].x, wv * gq.x);
+                            atomicAdd(&col[iy[k1]].y, wv * gq.y);
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
 cudaError_t launch_rotate_adjoint(const RotParams &R, int order, int tilted, const float2 *vol_grad,
                                   const double *geo, float2 *slab_grad, void *scratch, cudaStream_t s)
 {
-    if (tilted)
-        return cudaErrorNotSupported;
+    if (tilted) {
+        // slab_grad accumulates atomically: cleared first (stream-ordered)
+        cudaError_t e =
+            cudaMemsetAsync(slab_grad, 0, (size_t)R.nbatch_angles * R.nz * R.nx * R.ypitch * sizeof(float2), s);
+        if (e != cudaSuccess)
+            return e;
+        dim3 grid((R.nx + R3_X - 1) / R3_X, (R.ny + R3_Y - 1) / R3_Y, (R.nz + R3_Z - 1) / R3_Z);
+        switch (order) {
+#define ODT_ADJ3_CASE(O)                                                              \
+    case O:                                                                           \
+        k_rotate_3d_adjoint<O><<<grid, R3_X * 32, 0, s>>>(R, vol_grad, geo, slab_grad); \
+        break;
+            ODT_ADJ3_CASE(0)
+            ODT_ADJ3_CASE(1)
+            ODT_ADJ3_CASE(2)
+            ODT_ADJ3_CASE(3)
+#undef ODT_ADJ3_CASE
+        default:
+            return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
     const int ntiles = ((R.nx + RA_T - 1) / RA_T) * ((R.nz + RA_T - 1) / RA_T);
     const int nset = R.nbatch_angles * ntiles;
     AdjTileGeo *tiles = reinterpret_cast<AdjTileGeo *>(scratch);

@@ -38,6 +38,11 @@ namespace odt {
 // 24.1 ms with both).
 constexpr bool kColumnStepRegs = true;
 constexpr bool kColumnTw2 = true;
+// Row stage of power-of-two rows (>= 256) with any crop: k_rows_inverse_pow2
+// instead of the general k_rows_inverse.
+constexpr bool kRowsPow2 = true;
+// Half-crop row kernel with 8 lines per CTA (else Cfg's 4).
+constexpr bool kRowsHalfLpc8 = true;
 
 // ---------------------------------------------------------------------------
 // (a) rows: pad + weight + forward FFT along x.
@@ -115,30 +120,26 @@ __device__ __forceinline__ void column_spectrum(const StageParams &P, const L &l
 
 // Backward FFT along y of v, then the y-prefilter boundary terms (tilted
 // path, order >= 2) and the cropped store dst[yy * lNx] for yy < ny.
-template <class L, int KX>
+template <class L, int KX, bool TW2 = false>
 __device__ __forceinline__ void column_inverse_store(const StageParams &P, const L &line, float2 (&v)[L::SLOTS],
                                                      int c, int j, bool colok, float2 *buf0, float2 *buf1,
                                                      const float2 *tw, float2 *edge, int &flip, float2 *dst)
 {
     const int n = line.size();
     const int ny = P.ny, padyl = P.padyl;
-    line.template run<1, true>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
+    line.template run<1, true, TW2>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
     const bool yfix = P.order >= 2 && P.tilted;
-    float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
+    float2 cf[4];
     if (yfix) {
-        // u at y0-1, y0+1, y1-1, y1+1 (periodic over the padded height)
-        const int e0 = (padyl - 1 + n) % n, e1 = (padyl + 1) % n;
-        const int e2 = (padyl + ny - 2 + n) % n, e3 = (padyl + ny) % n;
-        float2 t;
-        if (held<L>(v, j, e0, t)) edge[c * 4 + 0] = t;
-        if (held<L>(v, j, e1, t)) edge[c * 4 + 1] = t;
-        if (held<L>(v, j, e2, t)) edge[c * 4 + 2] = t;
-        if (held<L>(v, j, e3, t)) edge[c * 4 + 3] = t;
+        // u around the crop's ends (periodic over the padded height)
+#pragma unroll
+        for (int e = 0; e < EDGE_SLOTS; ++e) {
+            float2 t;
+            if (edge_used(e, P.npoles) && held<L>(v, j, (padyl + edge_offset(e, ny) + 2 * n) % n, t))
+                edge[c * EDGE_SLOTS + e] = t;
+        }
         __syncthreads();
-        const float2 d0 = edge[c * 4 + 0] - edge[c * 4 + 1];
-        const float2 d1 = edge[c * 4 + 3] - edge[c * 4 + 2];
-        Acoef = make_float2(P.by_ca * d0.x + P.by_cb * d1.x, P.by_ca * d0.y + P.by_cb * d1.y);
-        Bcoef = make_float2(P.by_ca * d1.x + P.by_cb * d0.x, P.by_ca * d1.y + P.by_cb * d0.y);
+        pf_coefs(P.kys, P.npoles, edge + c * EDGE_SLOTS, cf);
     }
     if (!colok)
         return;
@@ -147,16 +148,8 @@ __device__ __forceinline__ void column_inverse_store(const StageParams &P, const
         const int yy = j + r * L::TPL - padyl;
         if (yy >= 0 && yy < ny) {
             float2 o = v[r];
-            if (yfix) {
-                if (yy < ZPOW_N) {
-                    const float zz = P.tab.zpow[yy];
-                    o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
-                }
-                if (ny - 1 - yy < ZPOW_N) {
-                    const float zz = P.tab.zpow[ny - 1 - yy];
-                    o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
-                }
-            }
+            if (yfix)
+                o = pf_apply(P, cf, yy, ny, o);
             dst[(size_t)yy * P.lNx] = o;
         }
     }
@@ -176,29 +169,20 @@ __device__ __forceinline__ void column_inverse_store_half(const StageParams &P, 
     constexpr int N = L::N, TPL = L::TPL, NY = N / 2, PAD = N / 4;
     line.template run<1, true, TW2>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
     if (P.order >= 2 && P.tilted) {
-        // y-prefilter boundary terms from u at PAD-1, PAD+1, PAD+NY-2, PAD+NY
-        float2 t;
-        if (held<L>(v, j, PAD - 1, t)) edge[c * 4 + 0] = t;
-        if (held<L>(v, j, PAD + 1, t)) edge[c * 4 + 1] = t;
-        if (held<L>(v, j, PAD + NY - 2, t)) edge[c * 4 + 2] = t;
-        if (held<L>(v, j, PAD + NY, t)) edge[c * 4 + 3] = t;
-        __syncthreads();
-        const float2 d0 = edge[c * 4 + 0] - edge[c * 4 + 1];
-        const float2 d1 = edge[c * 4 + 3] - edge[c * 4 + 2];
-        const float2 Ac = make_float2(P.by_ca * d0.x + P.by_cb * d1.x, P.by_ca * d0.y + P.by_cb * d1.y);
-        const float2 Bc = make_float2(P.by_ca * d1.x + P.by_cb * d0.x, P.by_ca * d1.y + P.by_cb * d0.y);
+        // y-prefilter boundary terms from u around the crop's ends
+        // (compile-time positions)
 #pragma unroll
-        for (int r = 2; r <= 5; ++r) {
-            const int yy = j + TPL * (r - 2);
-            if (yy < ZPOW_N) {
-                const float zz = P.tab.zpow[yy];
-                v[r] = make_float2(fmaf(Ac.x, zz, v[r].x), fmaf(Ac.y, zz, v[r].y));
-            }
-            if (NY - 1 - yy < ZPOW_N) {
-                const float zz = P.tab.zpow[NY - 1 - yy];
-                v[r] = make_float2(fmaf(Bc.x, zz, v[r].x), fmaf(Bc.y, zz, v[r].y));
-            }
+        for (int e = 0; e < EDGE_SLOTS; ++e) {
+            float2 t;
+            if (edge_used(e, P.npoles) && held<L>(v, j, PAD + edge_offset(e, NY), t))
+                edge[c * EDGE_SLOTS + e] = t;
         }
+        __syncthreads();
+        float2 cf[4];
+        pf_coefs(P.kys, P.npoles, edge + c * EDGE_SLOTS, cf);
+#pragma unroll
+        for (int r = 2; r <= 5; ++r)
+            v[r] = pf_apply(P, cf, j + TPL * (r - 2), NY, v[r]);
     }
     float2 *d = dst + (size_t)j * N;
 #pragma unroll
@@ -232,9 +216,11 @@ __global__ void __launch_bounds__(KX * L::TPL) k_columns_boundary(StageParams P,
     int flip = 0;
     float2 g[L::SLOTS];
     column_spectrum<L, KX>(P, line, rowspec, a, kx, colok, c, j, buf0, buf1, tw, flip, g);
+    const int np = P.npoles;
+    const size_t K = (size_t)P.lNy * P.lNx;
 #pragma unroll 1
-    for (int t = 0; t < 2; ++t) {
-        const float2 *tab = t == 0 ? P.tab.alpha : P.tab.beta;
+    for (int t = 0; t < 2 * np; ++t) {
+        const float2 *tab = t < np ? P.tab.alpha + t * K : P.tab.beta + (t - np) * K;
         float2 v[L::SLOTS];
 #pragma unroll
         for (int r = 0; r < L::SLOTS; ++r) {
@@ -242,7 +228,7 @@ __global__ void __launch_bounds__(KX * L::TPL) k_columns_boundary(StageParams P,
             v[r] = (colok && ky < n) ? cmul(g[r], tab[(size_t)ky * P.lNx + kx]) : make_float2(0.f, 0.f);
         }
         column_inverse_store<L, KX>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
-                                    Tab + ((size_t)(a * 2 + t) * P.ny) * P.lNx + kx);
+                                    Tab + ((size_t)(a * 2 * np + t) * P.ny) * P.lNx + kx);
     }
 }
 
@@ -256,16 +242,17 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
 {
     if (!group_active<KX>(P, blockIdx.x * KX))
         return;  // all-zero columns: the row stage never reads them
-    // half-crop plans: the per-element propagator step lives in registers
-    // and the third radix-8 pass reads per-thread-class twiddles
-    constexpr bool STEP_REGS = HALF && kColumnStepRegs;
-    constexpr bool TW2 = HALF && kColumnTw2 && pow2_len<L>() >= 512;
+    // power-of-two columns: the per-element propagator step lives in
+    // registers and (N >= 512) the third radix-8 pass reads
+    // per-thread-class twiddles
+    constexpr bool STEP_REGS = kColumnStepRegs && pow2_len<L>() > 0;
+    constexpr bool TW2 = kColumnTw2 && col_tw2<L>();
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNy
     const int ls = xslots<true>(n);
     float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls;
-    float2 *edge = tw + (TW2 ? tw_slots2(n) : tw_slots(n)); // [KX][4]
-    float2 *stp = edge + 4 * KX;     // [n][KX] propagator step per element
+    float2 *edge = tw + (TW2 ? tw_slots2(n) : tw_slots(n)); // [KX][EDGE_SLOTS]
+    float2 *stp = edge + EDGE_SLOTS * KX;  // [n][KX] propagator step per element
     if constexpr (TW2)
         copy_twiddles2<L>(tw, P.tab.twy, n);
     else
@@ -314,7 +301,7 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
             v[r] = V[r];
             const int ky = j + r * L::TPL;
             if constexpr (STEP_REGS)
-                V[r] = cmul(V[r], St[r]);
+                V[r] = cmul(V[r], St[r]);  // (ky < n: a power-of-two line)
             else if (HALF || ky < n)  // half-crop plans: a power-of-two line, ky < n
                 V[r] = cmul(V[r], stp[ky * KX + c]);
         }
@@ -322,8 +309,8 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
             column_inverse_store_half<L, KX, TW2>(P, line, v, c, j, buf0, buf1, tw, edge, flip,
                                                   T + (size_t)(q - q0) * (L::N / 2) * L::N + kx);
         else
-            column_inverse_store<L, KX>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
-                                        T + (size_t)(q - q0) * ny * lNx + kx);
+            column_inverse_store<L, KX, TW2>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
+                                             T + (size_t)(q - q0) * ny * lNx + kx);
     }
 }
 
@@ -368,8 +355,17 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     const int qq = q0 + qrel;  // the grid covers exactly qn jobs
     const int a = qq / nz, p = qq - a * nz;
     const bool pf = P.order >= 2;
-    const float zl = (pf && p < ZPOW_N) ? P.tab.zpow[p] : 0.f;
-    const float zh = (pf && nz - 1 - p < ZPOW_N) ? P.tab.zpow[nz - 1 - p] : 0.f;
+    const int np = P.npoles;
+    // z-boundary weights of this plane: z_i^p (alpha rows), z_i^(nz-1-p)
+    // (beta rows), per pole
+    float zl[2], zh[2];
+    bool zb_any = false;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        zl[i] = (pf && i < np && p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + p] : 0.f;
+        zh[i] = (pf && i < np && nz - 1 - p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + nz - 1 - p] : 0.f;
+        zb_any = zb_any || zl[i] != 0.f || zh[i] != 0.f;
+    }
     const float2 *Tq = T + (size_t)qrel * ny * n;
     float2 *dst = slab + ((size_t)a * nz + p) * nx * yp + ybase;
     // this thread's T values of row y (zeros for y >= ny or zero columns)
@@ -391,26 +387,32 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
         const bool valid = y < ny;
         if (g + 1 < GV)
             load_row(y + LPC, vn);
-        if (valid && (zl != 0.f || zh != 0.f)) {
-            const float2 *ta = Tab + ((size_t)(a * 2 + 0) * ny + y) * n;
-            const float2 *tb = Tab + ((size_t)(a * 2 + 1) * ny + y) * n;
+        if (valid && zb_any) {
 #pragma unroll
-            for (int r = 0; r < L::SLOTS; ++r) {
-                const int x = j + r * L::TPL;
-                if (column_active(P, x)) {
-                    const float2 u = ta[x], w = tb[x];
-                    v[r] = make_float2(fmaf(zh, w.x, fmaf(zl, u.x, v[r].x)), fmaf(zh, w.y, fmaf(zl, u.y, v[r].y)));
+            for (int i = 0; i < 2; ++i) {
+                if (i < np) {
+                    const float2 *ta = Tab + ((size_t)(a * 2 * np + i) * ny + y) * n;
+                    const float2 *tb = Tab + ((size_t)(a * 2 * np + np + i) * ny + y) * n;
+#pragma unroll
+                    for (int r = 0; r < L::SLOTS; ++r) {
+                        const int x = j + r * L::TPL;
+                        if (column_active(P, x)) {
+                            const float2 u = ta[x], w = tb[x];
+                            v[r] = make_float2(fmaf(zh[i], w.x, fmaf(zl[i], u.x, v[r].x)),
+                                               fmaf(zh[i], w.y, fmaf(zl[i], u.y, v[r].y)));
+                        }
+                    }
                 }
             }
         }
         int flip = 0;
         line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
-        float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
+        float2 cf[4];
         if (pf) {
-            // the line's samples at x0-1, x0+1, x1-1, x1+1 (periodic): every
+            // the line's samples around the crop's ends (periodic): every
             // thread writes its values to the exchange buffer the FFT's last
             // exchange did not use (its reads ended before that exchange's
-            // barrier), then each thread reads the four
+            // barrier), then each thread reads the edge samples
             // (plain positions 0..n-1: within the line's slots for every
             // line type, and conflict-free for these stride-1 writes)
             float2 *sc = (flip ? buf1 : buf0) + l * ls;
@@ -424,12 +426,11 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
                 line_sync(bar, L::TPL);
             else
                 __syncthreads();
-            const int e0 = (padxl - 1 + n) % n, e1 = (padxl + 1) % n;
-            const int e2 = (padxl + nx - 2 + n) % n, e3 = (padxl + nx) % n;
-            const float2 d0 = sc[e0] - sc[e1];
-            const float2 d1 = sc[e3] - sc[e2];
-            Acoef = make_float2(P.bx_ca * d0.x + P.bx_cb * d1.x, P.bx_ca * d0.y + P.bx_cb * d1.y);
-            Bcoef = make_float2(P.bx_ca * d1.x + P.bx_cb * d0.x, P.bx_ca * d1.y + P.bx_cb * d0.y);
+            float2 ed[EDGE_SLOTS];
+#pragma unroll
+            for (int e = 0; e < EDGE_SLOTS; ++e)
+                ed[e] = edge_used(e, np) ? sc[(padxl + edge_offset(e, nx) + 2 * n) % n] : make_float2(0.f, 0.f);
+            pf_coefs(P.kxs, np, ed, cf);
         }
         // stage[x][l] (pitch LPC+1) in buf0, then runs of LPC y per x
         __syncthreads();  // every line is done with buf0
@@ -440,16 +441,8 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
             const int xx = j + r * L::TPL - padxl;
             if (xx >= 0 && xx < nx) {
                 float2 o = v[r];
-                if (pf) {
-                    if (xx < ZPOW_N) {
-                        const float zz = P.tab.zpow[xx];
-                        o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
-                    }
-                    if (nx - 1 - xx < ZPOW_N) {
-                        const float zz = P.tab.zpow[nx - 1 - xx];
-                        o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
-                    }
-                }
+                if (pf)
+                    o = pf_apply(P, cf, xx, nx, o);
                 stage[xx * SP + l] = valid ? o : make_float2(0.f, 0.f);
             }
         }
@@ -478,7 +471,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
 // not written by the column stage) are a per-thread slot mask computed
 // once.  A CTA owns LPC*G consecutive rows of one job, LPC lines at a time.
 template <class L, int LPC, int G>
-__global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
+__global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : ((LPC * L::TPL <= 512) ? 2 : 1))
     k_rows_inverse_half(StageParams P, L line, const float2 *T, const float2 *Tab, float2 *slab, int q0)
 {
     constexpr int N = L::N, TPL = L::TPL, NX = N / 2, PAD = N / 4, RG = LPC * G, CPJ = NX / RG;
@@ -486,7 +479,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     extern __shared__ float2 smem[];
     constexpr int ls = xslots<false>(N);
     float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
-    float2 *edge = tw + tw_slots(N);  // [LPC][4]
+    float2 *edge = tw + tw_slots(N);  // [LPC][EDGE_SLOTS]
     // (the third-pass twiddle table costs more to set up per CTA than its
     // conflict-free reads save here: +0.7 ms for the 256^3 row stage)
     copy_twiddles<L>(tw, P.tab.twx, N);
@@ -498,8 +491,15 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     const int qq = q0 + qrel;
     const int a = qq / nz, p = qq - a * nz;
     const bool pf = P.order >= 2;
-    const float zl = (pf && p < ZPOW_N) ? P.tab.zpow[p] : 0.f;
-    const float zh = (pf && nz - 1 - p < ZPOW_N) ? P.tab.zpow[nz - 1 - p] : 0.f;
+    const int np = P.npoles;
+    float zl[2], zh[2];  // z-boundary weights of this plane, per pole
+    bool zb_any = false;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        zl[i] = (pf && i < np && p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + p] : 0.f;
+        zh[i] = (pf && i < np && nz - 1 - p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + nz - 1 - p] : 0.f;
+        zb_any = zb_any || zl[i] != 0.f || zh[i] != 0.f;
+    }
     // slots of this thread in the all-zero column band
     unsigned zmask = 0;
 #pragma unroll
@@ -508,8 +508,9 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
         if (x >= P.kx_zero_lo && x < P.kx_zero_hi)
             zmask |= 1u << r;
     }
-    // x-prefilter boundary weights of this thread's cropped slots: the
-    // A term (z^xx) for xx < ZPOW_N, the B term (z^(NX-1-xx)) near the end
+    // x-prefilter boundary weights of this thread's cropped slots for the
+    // first pole: the A term (z^xx) for xx < ZPOW_N, the B term
+    // (z^(NX-1-xx)) near the end
     float za[4], zb[4];
 #pragma unroll
     for (int r = 2; r <= 5; ++r) {
@@ -533,36 +534,57 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
         const int y = ybase + g * LPC + l;
         if (g + 1 < G)
             load_row(y + LPC, vn);
-        if (zl != 0.f || zh != 0.f) {
-            const float2 *ta = Tab + ((size_t)(a * 2 + 0) * NX + y) * N + j;
-            const float2 *tb = Tab + ((size_t)(a * 2 + 1) * NX + y) * N + j;
+        if (zb_any) {
 #pragma unroll
-            for (int r = 0; r < L::SLOTS; ++r) {
-                if (!((zmask >> r) & 1u)) {
-                    const float2 u = ta[r * TPL], w = tb[r * TPL];
-                    v[r] = make_float2(fmaf(zh, w.x, fmaf(zl, u.x, v[r].x)), fmaf(zh, w.y, fmaf(zl, u.y, v[r].y)));
+            for (int i = 0; i < 2; ++i) {
+                if (i < np) {
+                    const float2 *ta = Tab + ((size_t)(a * 2 * np + i) * NX + y) * N + j;
+                    const float2 *tb = Tab + ((size_t)(a * 2 * np + np + i) * NX + y) * N + j;
+#pragma unroll
+                    for (int r = 0; r < L::SLOTS; ++r) {
+                        if (!((zmask >> r) & 1u)) {
+                            const float2 u = ta[r * TPL], w = tb[r * TPL];
+                            v[r] = make_float2(fmaf(zh[i], w.x, fmaf(zl[i], u.x, v[r].x)),
+                                               fmaf(zh[i], w.y, fmaf(zl[i], u.y, v[r].y)));
+                        }
+                    }
                 }
             }
         }
         int flip = 0;
         line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
         if (pf) {
-            // the samples at PAD-1, PAD+1, PAD+NX-2, PAD+NX: held by one
-            // thread each, at a compile-time slot
-            float2 t;
-            if (held<L>(v, j, PAD - 1, t)) edge[l * 4 + 0] = t;
-            if (held<L>(v, j, PAD + 1, t)) edge[l * 4 + 1] = t;
-            if (held<L>(v, j, PAD + NX - 2, t)) edge[l * 4 + 2] = t;
-            if (held<L>(v, j, PAD + NX, t)) edge[l * 4 + 3] = t;
+            // the samples around the crop's ends: each held by one thread,
+            // at a compile-time slot
+#pragma unroll
+            for (int e = 0; e < EDGE_SLOTS; ++e) {
+                float2 t;
+                if (edge_used(e, np) && held<L>(v, j, PAD + edge_offset(e, NX), t))
+                    edge[l * EDGE_SLOTS + e] = t;
+            }
             line_sync(bar, TPL);
-            const float2 d0 = edge[l * 4 + 0] - edge[l * 4 + 1];
-            const float2 d1 = edge[l * 4 + 3] - edge[l * 4 + 2];
-            const float2 Ac = make_float2(P.bx_ca * d0.x + P.bx_cb * d1.x, P.bx_ca * d0.y + P.bx_cb * d1.y);
-            const float2 Bc = make_float2(P.bx_ca * d1.x + P.bx_cb * d0.x, P.bx_ca * d1.y + P.bx_cb * d0.y);
+            float2 cf[4];
+            pf_coefs(P.kxs, np, edge + l * EDGE_SLOTS, cf);
+            const float2 Ac = cf[0], Bc = cf[np];  // first pole
 #pragma unroll
             for (int r = 2; r <= 5; ++r) {
                 v[r] = make_float2(fmaf(Bc.x, zb[r - 2], fmaf(Ac.x, za[r - 2], v[r].x)),
                                    fmaf(Bc.y, zb[r - 2], fmaf(Ac.y, za[r - 2], v[r].y)));
+            }
+            if (np == 2) {  // second pole (orders 4, 5)
+                const float2 A2 = cf[1], B2 = cf[3];
+#pragma unroll
+                for (int r = 2; r <= 5; ++r) {
+                    const int xx = j + TPL * (r - 2);
+                    if (xx < ZPOW_N) {
+                        const float z = P.tab.zpow[ZPOW_N + xx];
+                        v[r] = make_float2(fmaf(A2.x, z, v[r].x), fmaf(A2.y, z, v[r].y));
+                    }
+                    if (NX - 1 - xx < ZPOW_N) {
+                        const float z = P.tab.zpow[ZPOW_N + NX - 1 - xx];
+                        v[r] = make_float2(fmaf(B2.x, z, v[r].x), fmaf(B2.y, z, v[r].y));
+                    }
+                }
             }
         }
         // stage[x][l] (pitch LPC+1) in buf0, then runs of LPC y per x
@@ -580,6 +602,148 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
             __stcs(dst + (size_t)xx * NX + g * LPC + ll, stage[xx * SP + ll]);
         }
         if (g + 1 < G) {
+            __syncthreads();  // stage reads done before buf0 is reused
+#pragma unroll
+            for (int r = 0; r < L::SLOTS; ++r)
+                v[r] = vn[r];
+        }
+    }
+}
+
+// (b2, power-of-two rows of 256 or more, any crop) k_rows_inverse with the
+// per-element work of the half-crop kernel moved out of the row loop: the
+// crop slots, the all-zero column slots and the first pole's x-boundary
+// weights are per-thread masks and registers computed once; edge samples go
+// through the shared buffer at positions computed once per CTA.  A CTA owns
+// LPC*G consecutive rows of one job (rows y >= ny are not run).
+template <class L, int LPC, int G>
+__global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
+    k_rows_inverse_pow2(StageParams P, L line, const float2 *T, const float2 *Tab, float2 *slab, int q0)
+{
+    constexpr int N = L::N, TPL = L::TPL, RG = LPC * G;
+    extern __shared__ float2 smem[];
+    constexpr int ls = xslots<false>(N);
+    float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
+    float2 *edge = tw + tw_slots(N);  // [LPC][EDGE_SLOTS]
+    copy_twiddles<L>(tw, P.tab.twx, N);
+    const int l = threadIdx.x / TPL, j = threadIdx.x % TPL;
+    const int bar = 1 + l;  // each line is whole warps (TPL >= 32)
+    const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl, yp = P.ypitch;
+    const int cpj = (ny + RG - 1) / RG;
+    const int qrel = (int)blockIdx.x / cpj;
+    const int ybase = ((int)blockIdx.x - qrel * cpj) * RG;
+    const int GV = min(G, (ny - ybase + LPC - 1) / LPC);
+    const int qq = q0 + qrel;
+    const int a = qq / nz, p = qq - a * nz;
+    const bool pf = P.order >= 2;
+    const int np = P.npoles;
+    float zl[2], zh[2];
+    bool zb_any = false;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        zl[i] = (pf && i < np && p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + p] : 0.f;
+        zh[i] = (pf && i < np && nz - 1 - p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + nz - 1 - p] : 0.f;
+        zb_any = zb_any || zl[i] != 0.f || zh[i] != 0.f;
+    }
+    unsigned zmask = 0, cmask = 0;
+    float za[8], zb[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int x = j + r * TPL, xx = x - padxl;
+        if (x >= P.kx_zero_lo && x < P.kx_zero_hi)
+            zmask |= 1u << r;
+        if (xx >= 0 && xx < nx)
+            cmask |= 1u << r;
+        za[r] = (pf && xx >= 0 && xx < ZPOW_N) ? P.tab.zpow[xx] : 0.f;
+        zb[r] = (pf && xx < nx && nx - 1 - xx < ZPOW_N) ? P.tab.zpow[nx - 1 - xx] : 0.f;
+    }
+    int epos[EDGE_SLOTS];  // line positions of the edge samples
+#pragma unroll
+    for (int e = 0; e < EDGE_SLOTS; ++e)
+        epos[e] = (padxl + edge_offset(e, nx) + 2 * N) % N;
+    const float2 *Tq = T + (size_t)qrel * ny * N + j;
+    float2 *dst = slab + ((size_t)a * nz + p) * nx * yp + ybase;
+    auto load_row = [&](int y, float2 (&v)[L::SLOTS]) {
+        const bool valid = y < ny;
+        const float2 *src = Tq + (size_t)(valid ? y : 0) * N;
+#pragma unroll
+        for (int r = 0; r < L::SLOTS; ++r)
+            v[r] = (!valid || ((zmask >> r) & 1u)) ? make_float2(0.f, 0.f) : __ldcs(src + r * TPL);
+    };
+    float2 v[L::SLOTS], vn[L::SLOTS];
+    load_row(ybase + l, v);
+    __syncthreads();  // twiddles
+#pragma unroll 1
+    for (int g = 0; g < GV; ++g) {
+        const int y = ybase + g * LPC + l;
+        const bool valid = y < ny;
+        if (g + 1 < GV)
+            load_row(y + LPC, vn);
+        if (valid && zb_any) {
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                if (i < np) {
+                    const float2 *ta = Tab + ((size_t)(a * 2 * np + i) * ny + y) * N + j;
+                    const float2 *tb = Tab + ((size_t)(a * 2 * np + np + i) * ny + y) * N + j;
+#pragma unroll
+                    for (int r = 0; r < L::SLOTS; ++r) {
+                        if (!((zmask >> r) & 1u)) {
+                            const float2 u = ta[r * TPL], w = tb[r * TPL];
+                            v[r] = make_float2(fmaf(zh[i], w.x, fmaf(zl[i], u.x, v[r].x)),
+                                               fmaf(zh[i], w.y, fmaf(zl[i], u.y, v[r].y)));
+                        }
+                    }
+                }
+            }
+        }
+        int flip = 0;
+        line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
+        if (pf) {
+#pragma unroll
+            for (int e = 0; e < EDGE_SLOTS; ++e) {
+                float2 t;
+                if (edge_used(e, np) && held<L>(v, j, epos[e], t))
+                    edge[l * EDGE_SLOTS + e] = t;
+            }
+            line_sync(bar, TPL);
+            float2 cf[4];
+            pf_coefs(P.kxs, np, edge + l * EDGE_SLOTS, cf);
+            const float2 Ac = cf[0], Bc = cf[np];
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                v[r] = make_float2(fmaf(Bc.x, zb[r], fmaf(Ac.x, za[r], v[r].x)),
+                                   fmaf(Bc.y, zb[r], fmaf(Ac.y, za[r], v[r].y)));
+            if (np == 2) {  // second pole (orders 4, 5)
+                const float2 A2 = cf[1], B2 = cf[3];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const int xx = j + TPL * r - padxl;
+                    if (xx >= 0 && xx < ZPOW_N) {
+                        const float z = P.tab.zpow[ZPOW_N + xx];
+                        v[r] = make_float2(fmaf(A2.x, z, v[r].x), fmaf(A2.y, z, v[r].y));
+                    }
+                    if (xx < nx && nx - 1 - xx < ZPOW_N) {
+                        const float z = P.tab.zpow[ZPOW_N + nx - 1 - xx];
+                        v[r] = make_float2(fmaf(B2.x, z, v[r].x), fmaf(B2.y, z, v[r].y));
+                    }
+                }
+            }
+        }
+        // stage[x][l] (pitch LPC+1) in buf0, then runs of LPC y per x
+        __syncthreads();  // every line is done with buf0 (and edge)
+        float2 *stage = buf0;
+        constexpr int SP = LPC + 1;
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+            if ((cmask >> r) & 1u)
+                stage[(j + TPL * r - padxl) * SP + l] = valid ? v[r] : make_float2(0.f, 0.f);
+        __syncthreads();
+        for (int e = threadIdx.x; e < nx * LPC; e += LPC * TPL) {
+            const int xx = e / LPC, ll = e - (e / LPC) * LPC;
+            if (ybase + g * LPC + ll < ny)
+                __stcs(dst + (size_t)xx * yp + g * LPC + ll, stage[xx * SP + ll]);
+        }
+        if (g + 1 < GV) {
             __syncthreads();  // stage reads done before buf0 is reused
 #pragma unroll
             for (int r = 0; r < L::SLOTS; ++r)
@@ -654,25 +818,29 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
             cur_a = a;
         }
         if (valid && pf) {
-            const float zl = p < ZPOW_N ? P.tab.zpow[p] : 0.f;
-            const float zh = nz - 1 - p < ZPOW_N ? P.tab.zpow[nz - 1 - p] : 0.f;
-            if (zl != 0.f || zh != 0.f) {
-                const float2 *ta = Tab + (size_t)(a * 2 + 0) * n;
-                const float2 *tb = Tab + (size_t)(a * 2 + 1) * n;
+            const int np = P.npoles;
 #pragma unroll
-                for (int r = 0; r < L::SLOTS; ++r) {
-                    const int x = j + r * L::TPL;
-                    if (column_active(P, x)) {
-                        const float2 u = ta[x], w = tb[x];
-                        v[r] = make_float2(fmaf(zh, w.x, fmaf(zl, u.x, v[r].x)),
-                                           fmaf(zh, w.y, fmaf(zl, u.y, v[r].y)));
+            for (int i = 0; i < 2; ++i) {
+                const float zl = (i < np && p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + p] : 0.f;
+                const float zh = (i < np && nz - 1 - p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + nz - 1 - p] : 0.f;
+                if (zl != 0.f || zh != 0.f) {
+                    const float2 *ta = Tab + (size_t)(a * 2 * np + i) * n;
+                    const float2 *tb = Tab + (size_t)(a * 2 * np + np + i) * n;
+#pragma unroll
+                    for (int r = 0; r < L::SLOTS; ++r) {
+                        const int x = j + r * L::TPL;
+                        if (column_active(P, x)) {
+                            const float2 u = ta[x], w = tb[x];
+                            v[r] = make_float2(fmaf(zh, w.x, fmaf(zl, u.x, v[r].x)),
+                                               fmaf(zh, w.y, fmaf(zl, u.y, v[r].y)));
+                        }
                     }
                 }
             }
         }
         int flip = 0;
         line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
-        float2 Acoef = make_float2(0.f, 0.f), Bcoef = make_float2(0.f, 0.f);
+        float2 cf[4];
         if (pf) {
             // the line's samples at x0-1, x0+1, x1-1, x1+1 (periodic), through
             // the exchange buffer the FFT's last exchange did not use
@@ -687,12 +855,11 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
                 line_sync(bar, L::TPL);
             else
                 __syncthreads();
-            const int e0 = (padxl - 1 + n) % n, e1 = (padxl + 1) % n;
-            const int e2 = (padxl + nx - 2 + n) % n, e3 = (padxl + nx) % n;
-            const float2 d0 = sc[e0] - sc[e1];
-            const float2 d1 = sc[e3] - sc[e2];
-            Acoef = make_float2(P.bx_ca * d0.x + P.bx_cb * d1.x, P.bx_ca * d0.y + P.bx_cb * d1.y);
-            Bcoef = make_float2(P.bx_ca * d1.x + P.bx_cb * d0.x, P.bx_ca * d1.y + P.bx_cb * d0.y);
+            float2 ed[EDGE_SLOTS];
+#pragma unroll
+            for (int e = 0; e < EDGE_SLOTS; ++e)
+                ed[e] = edge_used(e, P.npoles) ? sc[(padxl + edge_offset(e, nx) + 2 * n) % n] : make_float2(0.f, 0.f);
+            pf_coefs(P.kxs, P.npoles, ed, cf);
         }
         if (valid) {
             float2 *dst = slab + ((size_t)a * nz + p) * nx;
@@ -701,16 +868,8 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
                 const int xx = j + r * L::TPL - padxl;
                 if (xx >= 0 && xx < nx) {
                     float2 o = v[r];
-                    if (pf) {
-                        if (xx < ZPOW_N) {
-                            const float zz = P.tab.zpow[xx];
-                            o = make_float2(fmaf(Acoef.x, zz, o.x), fmaf(Acoef.y, zz, o.y));
-                        }
-                        if (nx - 1 - xx < ZPOW_N) {
-                            const float zz = P.tab.zpow[nx - 1 - xx];
-                            o = make_float2(fmaf(Bcoef.x, zz, o.x), fmaf(Bcoef.y, zz, o.y));
-                        }
-                    }
+                    if (pf)
+                        o = pf_apply(P, cf, xx, nx, o);
                     __stcs(dst + xx, o);
                 }
             }
@@ -744,8 +903,12 @@ __global__ void __launch_bounds__(256) k_columns_boundary_line(StageParams P, co
         if (P.again)
             b = cmul(b, P.again[(size_t)a * lNx + kx]);
     }
-    Tab[(size_t)(a * 2 + 0) * lNx + kx] = cmul(b, P.tab.alpha[kx]);
-    Tab[(size_t)(a * 2 + 1) * lNx + kx] = cmul(b, P.tab.beta[kx]);
+    const int np = P.npoles;
+    const size_t K = (size_t)P.lNy * lNx;
+    for (int i = 0; i < np; ++i) {
+        Tab[(size_t)(a * 2 * np + i) * lNx + kx] = cmul(b, P.tab.alpha[i * K + kx]);
+        Tab[(size_t)(a * 2 * np + np + i) * lNx + kx] = cmul(b, P.tab.beta[i * K + kx]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -803,6 +966,14 @@ constexpr int half_groups()
 {
     return Cfg<L>::LPC >= 16 ? 1 : 16 / Cfg<L>::LPC;
 }
+// Lines per CTA of the half-crop row kernel: with 64-thread lines, 8 lines
+// (512 threads, 2 CTAs per SM), so that the transposed store writes runs of
+// 8 y (64 bytes) per x instead of 4.
+template <class L>
+constexpr int half_rows_lpc()
+{
+    return (kRowsHalfLpc8 && L::TPL == 64) ? 8 : Cfg<L>::LPC;
+}
 
 template <class L>
 static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rowspec, float2 *T, int q0, int qn,
@@ -818,8 +989,8 @@ static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rows
             return cudaGetLastError();
         }
     }
-    k_columns_propagate<L, KX, false><<<grid, KX * L::TPL, smem_cols<L>(line.n), s>>>(P, line, rowspec, T, q0, qn,
-                                                                                    ppc);
+    k_columns_propagate<L, KX, false><<<grid, KX * L::TPL, smem_cols_prop<L>(line.n), s>>>(P, line, rowspec, T, q0,
+                                                                                         qn, ppc);
     return cudaGetLastError();
 }
 
@@ -830,9 +1001,18 @@ static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 
     constexpr int LPC = Cfg<L>::LPC;
     if constexpr (half_line<L>()) {
         if (half_crop(P)) {
+            constexpr int LH = half_rows_lpc<L>(), G = 16 / LH;
+            const unsigned grid = (unsigned)((long long)qn * (L::N / 2 / (LH * G)));
+            k_rows_inverse_half<L, LH, G><<<grid, LH * L::TPL, smem_rows_half<L, LH>(line.n), s>>>(P, line, T, Tab,
+                                                                                                 slab, q0);
+            return cudaGetLastError();
+        }
+    }
+    if constexpr (half_line<L>()) {
+        if (kRowsPow2 && !single_row_plan(P) && P.ny > 1) {
             constexpr int G = half_groups<L>();
-            const unsigned grid = (unsigned)((long long)qn * (L::N / 2 / (LPC * G)));
-            k_rows_inverse_half<L, LPC, G><<<grid, LPC * L::TPL, smem_rows_half<L>(line.n), s>>>(P, line, T, Tab,
+            const unsigned grid = (unsigned)((long long)qn * ((P.ny + LPC * G - 1) / (LPC * G)));
+            k_rows_inverse_pow2<L, LPC, G><<<grid, LPC * L::TPL, smem_rows_half<L>(line.n), s>>>(P, line, T, Tab,
                                                                                                slab, q0);
             return cudaGetLastError();
         }
@@ -872,13 +1052,18 @@ static cudaError_t set_smem_attrs(int n)
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols_half<L>(n));
         if (e != cudaSuccess)
             return e;
-        e = cudaFuncSetAttribute(k_rows_inverse_half<L, Cfg<L>::LPC, half_groups<L>()>,
+        e = cudaFuncSetAttribute(k_rows_inverse_half<L, half_rows_lpc<L>(), 16 / half_rows_lpc<L>()>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem_rows_half<L, half_rows_lpc<L>()>(n));
+        if (e != cudaSuccess)
+            return e;
+        e = cudaFuncSetAttribute(k_rows_inverse_pow2<L, Cfg<L>::LPC, half_groups<L>()>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rows_half<L>(n));
         if (e != cudaSuccess)
             return e;
     }
     return cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX, false>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols<L>(n));
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols_prop<L>(n));
 }
 
 int columns_slots(const StageParams &P)
@@ -891,7 +1076,7 @@ int columns_slots(const StageParams &P)
         using L = decltype(line);
         constexpr int KX = Cfg<L>::KX;
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_columns_propagate<L, KX, false>, KX * L::TPL,
-                                                             smem_cols<L>(line.n));
+                                                             smem_cols_prop<L>(line.n));
     });
     return e == cudaSuccess ? per * sms : 0;
 }

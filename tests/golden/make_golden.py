@@ -139,6 +139,11 @@ def make_backprop(odt):
         intp_order=3, dtype=float, **p1)
     add("bpp_rect_nopad", odt.backpropagate_3d, s2, a2,
         padding=(False, False), dtype=float, **p2)
+    # quartic and quintic splines (two prefilter poles)
+    add("bpp_order4", odt.backpropagate_3d, sino, angles, padval="edge",
+        intp_order=4, dtype=float, **p1)
+    add("bpp_rect_order5", odt.backpropagate_3d, s2, a2, padval=0,
+        intp_order=5, dtype=float, **p2)
     add("bppt_default_p2", odt.backpropagate_3d_tilted, sino, angles,
         padval=0, dtype=float, **p2)
     st, at = gauss_sino_3d_tilted(A=11, tilt_plane=0.3)
@@ -147,6 +152,11 @@ def make_backprop(odt):
         tilted_axis=ax, padval="edge", dtype=float, **p1)
     add("bppt_axis_order1", odt.backpropagate_3d_tilted, st, at,
         tilted_axis=ax, intp_order=1, padval=0, dtype=float, **p1)
+    add("bppt_axis_order5", odt.backpropagate_3d_tilted, st, at,
+        tilted_axis=ax, intp_order=5, padval="edge", dtype=float, **p1)
+    add("bppt_rect_order4", odt.backpropagate_3d_tilted, s2, a2,
+        tilted_axis=[0, np.cos(0.2), np.sin(0.2)], intp_order=4,
+        dtype=float, **p2)
     add("bppt_yz_onlyreal", odt.backpropagate_3d_tilted, s2, a2,
         tilted_axis=[0, np.cos(0.2), np.sin(0.2)], onlyreal=True,
         dtype=float, **p2)

@@ -76,7 +76,7 @@ def test_reference_cases(odt, golden):
         assert_close(got, out, what=name)
 
 
-@pytest.mark.parametrize("order", [0, 1, 2, 3])
+@pytest.mark.parametrize("order", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("kind", ["y", "tilted"])
 def test_orders_vs_oracle(odt, order, kind):
     rng = np.random.default_rng(order * 7 + (kind == "y"))
@@ -404,3 +404,48 @@ def test_full_config_vs_oracle(odt, cfg):
         ref = O.backpropagate_3d_tilted(sino.astype(np.complex128), angles,
                                         tilted_axis=ax, fft_workers=-1, **kw)
     assert_close(got, ref, what="%s full" % cfg)
+
+
+@pytest.mark.parametrize("order", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("kind", ["y", "tilted"])
+def test_pow2_rows_any_crop(odt, order, kind):
+    """Rectangular 60x100 planes padded to 128x256: the power-of-two row
+    stage with a crop that is not the centred half (pad 78 of 256), every
+    spline order, both geometries, against the FP64 oracle."""
+    rng = np.random.default_rng(100 + order + 10 * (kind == "y"))
+    A, ny, nx = 4, 60, 100
+    sino = (1 + rng.normal(0, .05, (A, ny, nx))
+            + 1j * rng.normal(0, .3, (A, ny, nx)))
+    angles = np.sort(rng.uniform(0, 2 * np.pi, A))
+    kw = dict(res=3.0, nm=1.333, intp_order=order, padval="edge",
+              weight_angles=False)
+    if kind == "y":
+        ref = O.backpropagate_3d(sino, angles, fft_workers=-1, **kw)
+        got = odt.backpropagate_3d(sino, angles, **kw)
+    else:
+        ax = (0.1, np.cos(0.3), np.sin(0.3))
+        ref = O.backpropagate_3d_tilted(sino, angles, tilted_axis=ax,
+                                        fft_workers=-1, **kw)
+        got = odt.backpropagate_3d_tilted(sino, angles, tilted_axis=ax, **kw)
+    assert_close(got, ref, what="order %d %s 60x100" % (order, kind))
+
+
+@pytest.mark.parametrize("order", [4, 5])
+def test_high_orders_full_planes(odt, order):
+    """Quartic and quintic splines (two prefilter poles) on 256^2 -> 512^2
+    planes, the centred-half crop of the benchmark's shapes, 3 angles, both
+    geometries, against the FP64 oracle."""
+    sino, angles = ellipsoid_phantom_sinogram(
+        256, 3, seed=13 + order, count_range=(3, 8), semi_range=(8, 60),
+        angles=np.array([0.4, 2.1, 4.0]))
+    kw = dict(res=3.0, nm=1.333, intp_order=order, weight_angles=False)
+    got = odt.backpropagate_3d(sino.astype(np.complex64), angles,
+                               dtype=np.float32, **kw)
+    ref = O.backpropagate_3d(sino, angles, fft_workers=-1, **kw)
+    assert_close(got, ref, what="order %d, 256^3" % order)
+    ax = (0, np.cos(0.2), np.sin(0.2))
+    got = odt.backpropagate_3d_tilted(sino.astype(np.complex64), angles,
+                                      dtype=np.float32, tilted_axis=ax, **kw)
+    ref = O.backpropagate_3d_tilted(sino, angles, tilted_axis=ax,
+                                    fft_workers=-1, **kw)
+    assert_close(got, ref, what="order %d, tilted 256^3" % order)

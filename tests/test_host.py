@@ -170,16 +170,25 @@ def test_plan_create_argument_checks(native_lib):
     d.pad_ny = d.pad_nx = 64
     d.pad_y_left = d.pad_x_left = 24
     d.pad_mode = _native.ODT_PAD_EDGE
-    d.intp_order = 4
+    d.intp_order = 6
     filt = np.zeros(64 * 64 * 2)
     ph = np.zeros(64 * 64)
     d.filter = filt.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     d.kz_phase = ph.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     h = ctypes.c_void_p()
     st = native_lib.odt_bpp3d_plan_create(ctypes.byref(d), ctypes.byref(h))
+    assert st == _native.ODT_ERR_INVALID_ARGUMENT
+    assert b"0..5" in native_lib.odt_last_error()
+    # orders 4 and 5 (two prefilter poles) need lines of >= 4 samples
+    d.intp_order = 5
+    d.nx = 3
+    d.pad_nx = 3
+    d.pad_x_left = 0
+    st = native_lib.odt_bpp3d_plan_create(ctypes.byref(d), ctypes.byref(h))
     assert st == _native.ODT_ERR_UNSUPPORTED
     with pytest.raises(NotImplementedError):
         _native.check(st)
+    d.nx, d.pad_nx, d.pad_x_left = 16, 64, 24
     d.intp_order = 2
     d.pad_x_left = 60
     st = native_lib.odt_bpp3d_plan_create(ctypes.byref(d), ctypes.byref(h))
