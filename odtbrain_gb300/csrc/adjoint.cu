@@ -133,6 +133,10 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_columns(StageParams P, L li
     const int c = threadIdx.x % KX, j = threadIdx.x / KX;
     const int kx = blockIdx.x * KX + c;
     const bool colok = kx < P.lNx;
+    // k_adj_rows writes the cotangent rows Tg only in the active columns;
+    // a zero-band column of an active group is read as zero, never from
+    // the unwritten workspace
+    const bool colact = colok && column_active(P, kx);
     const int lNx = P.lNx, nz = P.nz, ny = P.ny, padyl = P.padyl;
     // tilted path: the forward's y-prefilter boundary terms (from the four
     // samples around the crop's ends) are transposed before the FFT
@@ -184,7 +188,7 @@ __global__ void __launch_bounds__(KX * L::TPL) k_adj_columns(StageParams P, L li
 #pragma unroll
         for (int r = 0; r < L::SLOTS; ++r) {
             const int yy = j + r * L::TPL - padyl;
-            v[r] = (colok && yy >= 0 && yy < ny) ? src[(size_t)yy * lNx] : make_float2(0.f, 0.f);
+            v[r] = (colact && yy >= 0 && yy < ny) ? src[(size_t)yy * lNx] : make_float2(0.f, 0.f);
         }
         if (yfix) {
             // out[yy] = u[padyl + yy] + A z^yy + B z^(ny-1-yy), with A, B from

@@ -93,46 +93,43 @@ __host__ __device__ constexpr bool edge_used(int slot, int np)
     return ((slot & 3) >> 1) < np;
 }
 
-// Coefficients (A_1, A_2, B_1, B_2) (c[np + i] = B_i) from the 8 edge slots.
-__device__ __forceinline__ void pf_coefs(const float *K, int np, const float2 *ed, float2 (&c)[4])
+// Coefficients of an NP-pole prefilter (NP = 1: orders 2, 3; NP = 2:
+// orders 4, 5) from the edge slots: c[i] = A_(i+1), c[NP + i] = B_(i+1).
+// K is the 2NP x 2NP boundary solve, row-major.  NP is a compile-time
+// constant so that c stays in registers.
+template <int NP>
+__device__ __forceinline__ void pf_coefs(const float *K, const float2 *ed, float2 (&c)[2 * NP])
 {
-    float2 d[4];
+    float2 d[2 * NP];
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        if (q < np) {
-            d[q] = ed[2 * q + 1] - ed[2 * q];               // u[q+1] - u[-(q+1)]
-            d[np + q] = ed[4 + 2 * q] - ed[4 + 2 * q + 1];  // u[n-2-q] - u[n+q]
-        }
+    for (int q = 0; q < NP; ++q) {
+        d[q] = ed[2 * q + 1] - ed[2 * q];               // u[q+1] - u[-(q+1)]
+        d[NP + q] = ed[4 + 2 * q] - ed[4 + 2 * q + 1];  // u[n-2-q] - u[n+q]
     }
-    const int n2 = 2 * np;
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+    for (int r = 0; r < 2 * NP; ++r) {
         c[r] = make_float2(0.f, 0.f);
-        if (r < n2) {
 #pragma unroll
-            for (int jj = 0; jj < 4; ++jj)
-                if (jj < n2) {
-                    const float k = K[r * n2 + jj];
-                    c[r] = make_float2(fmaf(k, d[jj].x, c[r].x), fmaf(k, d[jj].y, c[r].y));
-                }
+        for (int jj = 0; jj < 2 * NP; ++jj) {
+            const float k = K[r * 2 * NP + jj];
+            c[r] = make_float2(fmaf(k, d[jj].x, c[r].x), fmaf(k, d[jj].y, c[r].y));
         }
     }
 }
 
 // Output k of the n-sample line with its boundary terms added.
-__device__ __forceinline__ float2 pf_apply(const StageParams &P, const float2 (&c)[4], int k, int n, float2 o)
+template <int NP>
+__device__ __forceinline__ float2 pf_apply(const StageParams &P, const float2 (&c)[2 * NP], int k, int n, float2 o)
 {
 #pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        if (i < P.npoles) {
-            if (k < ZPOW_N) {
-                const float z = P.tab.zpow[i * ZPOW_N + k];
-                o = make_float2(fmaf(c[i].x, z, o.x), fmaf(c[i].y, z, o.y));
-            }
-            if (n - 1 - k < ZPOW_N) {
-                const float z = P.tab.zpow[i * ZPOW_N + n - 1 - k];
-                o = make_float2(fmaf(c[P.npoles + i].x, z, o.x), fmaf(c[P.npoles + i].y, z, o.y));
-            }
+    for (int i = 0; i < NP; ++i) {
+        if (k < ZPOW_N) {
+            const float z = P.tab.zpow[i * ZPOW_N + k];
+            o = make_float2(fmaf(c[i].x, z, o.x), fmaf(c[i].y, z, o.y));
+        }
+        if (n - 1 - k < ZPOW_N) {
+            const float z = P.tab.zpow[i * ZPOW_N + n - 1 - k];
+            o = make_float2(fmaf(c[NP + i].x, z, o.x), fmaf(c[NP + i].y, z, o.y));
         }
     }
     return o;
@@ -227,10 +224,10 @@ inline size_t smem_rows(int n)
 }
 // k_rows_inverse_half: the exchange buffers, the twiddle table and the
 // edge samples.
-template <class L, int LPC = Cfg<L>::LPC>
+template <class L>
 inline size_t smem_rows_half(int n)
 {
-    return (size_t)(2 * LPC * xslots<false>(n) + tw_slots(n) + EDGE_SLOTS * LPC) * sizeof(float2);
+    return (size_t)(2 * Cfg<L>::LPC * xslots<false>(n) + tw_slots(n) + EDGE_SLOTS * Cfg<L>::LPC) * sizeof(float2);
 }
 // k_columns_propagate of half-crop plans: smem_cols plus the third-pass
 // twiddle table.
@@ -239,21 +236,6 @@ inline size_t smem_cols_half(int n)
 {
     return (size_t)(2 * Cfg<L>::KX * xslots<true>(n) + Cfg<L>::KX * n + tw_slots2(n) + EDGE_SLOTS * Cfg<L>::KX) *
            sizeof(float2);
-}
-// The column-propagate kernel reads the third-pass twiddle table for
-// power-of-two columns of 512 or more.
-template <class L>
-constexpr bool col_tw2()
-{
-    return pow2_len<L>() >= 512;
-}
-template <class L>
-inline size_t smem_cols(int n);
-// Shared memory of k_columns_propagate (generic crop).
-template <class L>
-inline size_t smem_cols_prop(int n)
-{
-    return col_tw2<L>() ? smem_cols_half<L>(n) : smem_cols<L>(n);
 }
 template <class L>
 inline size_t smem_cols(int n)

@@ -38,11 +38,6 @@ namespace odt {
 // 24.1 ms with both).
 constexpr bool kColumnStepRegs = true;
 constexpr bool kColumnTw2 = true;
-// Row stage of power-of-two rows (>= 256) with any crop: k_rows_inverse_pow2
-// instead of the general k_rows_inverse.
-constexpr bool kRowsPow2 = true;
-// Half-crop row kernel with 8 lines per CTA (else Cfg's 4).
-constexpr bool kRowsHalfLpc8 = true;
 
 // ---------------------------------------------------------------------------
 // (a) rows: pad + weight + forward FFT along x.
@@ -118,9 +113,10 @@ __device__ __forceinline__ void column_spectrum(const StageParams &P, const L &l
     }
 }
 
-// Backward FFT along y of v, then the y-prefilter boundary terms (tilted
-// path, order >= 2) and the cropped store dst[yy * lNx] for yy < ny.
-template <class L, int KX, bool TW2 = false>
+// Backward FFT along y of v, then the y-prefilter boundary terms (YF > 0:
+// tilted path, order >= 2, YF poles) and the cropped store dst[yy * lNx]
+// for yy < ny.
+template <class L, int KX, int YF, bool TW2 = false>
 __device__ __forceinline__ void column_inverse_store(const StageParams &P, const L &line, float2 (&v)[L::SLOTS],
                                                      int c, int j, bool colok, float2 *buf0, float2 *buf1,
                                                      const float2 *tw, float2 *edge, int &flip, float2 *dst)
@@ -128,18 +124,19 @@ __device__ __forceinline__ void column_inverse_store(const StageParams &P, const
     const int n = line.size();
     const int ny = P.ny, padyl = P.padyl;
     line.template run<1, true, TW2>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
-    const bool yfix = P.order >= 2 && P.tilted;
-    float2 cf[4];
-    if (yfix) {
+    constexpr bool yfix = YF > 0;
+    constexpr int NPY = YF > 0 ? YF : 1;
+    float2 cf[2 * NPY];
+    if constexpr (yfix) {
         // u around the crop's ends (periodic over the padded height)
 #pragma unroll
         for (int e = 0; e < EDGE_SLOTS; ++e) {
             float2 t;
-            if (edge_used(e, P.npoles) && held<L>(v, j, (padyl + edge_offset(e, ny) + 2 * n) % n, t))
+            if (edge_used(e, NPY) && held<L>(v, j, (padyl + edge_offset(e, ny) + 2 * n) % n, t))
                 edge[c * EDGE_SLOTS + e] = t;
         }
         __syncthreads();
-        pf_coefs(P.kys, P.npoles, edge + c * EDGE_SLOTS, cf);
+        pf_coefs<NPY>(P.kys, edge + c * EDGE_SLOTS, cf);
     }
     if (!colok)
         return;
@@ -148,8 +145,8 @@ __device__ __forceinline__ void column_inverse_store(const StageParams &P, const
         const int yy = j + r * L::TPL - padyl;
         if (yy >= 0 && yy < ny) {
             float2 o = v[r];
-            if (yfix)
-                o = pf_apply(P, cf, yy, ny, o);
+            if constexpr (yfix)
+                o = pf_apply<NPY>(P, cf, yy, ny, o);
             dst[(size_t)yy * P.lNx] = o;
         }
     }
@@ -161,28 +158,28 @@ __device__ __forceinline__ void column_inverse_store(const StageParams &P, const
 // of the y-prefilter solve at compile-time slots, so the crop needs no
 // predicates and the stores use constant offsets from one row pointer.
 // dst points at row 0 of the job's T block, column kx (row stride N).
-template <class L, int KX, bool TW2>
+template <class L, int KX, int YF, bool TW2>
 __device__ __forceinline__ void column_inverse_store_half(const StageParams &P, const L &line, float2 (&v)[L::SLOTS],
                                                           int c, int j, float2 *buf0, float2 *buf1,
                                                           const float2 *tw, float2 *edge, int &flip, float2 *dst)
 {
     constexpr int N = L::N, TPL = L::TPL, NY = N / 2, PAD = N / 4;
     line.template run<1, true, TW2>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
-    if (P.order >= 2 && P.tilted) {
+    if constexpr (YF > 0) {
         // y-prefilter boundary terms from u around the crop's ends
         // (compile-time positions)
 #pragma unroll
         for (int e = 0; e < EDGE_SLOTS; ++e) {
             float2 t;
-            if (edge_used(e, P.npoles) && held<L>(v, j, PAD + edge_offset(e, NY), t))
+            if (edge_used(e, YF) && held<L>(v, j, PAD + edge_offset(e, NY), t))
                 edge[c * EDGE_SLOTS + e] = t;
         }
         __syncthreads();
-        float2 cf[4];
-        pf_coefs(P.kys, P.npoles, edge + c * EDGE_SLOTS, cf);
+        float2 cf[2 * YF];
+        pf_coefs<YF>(P.kys, edge + c * EDGE_SLOTS, cf);
 #pragma unroll
         for (int r = 2; r <= 5; ++r)
-            v[r] = pf_apply(P, cf, j + TPL * (r - 2), NY, v[r]);
+            v[r] = pf_apply<YF>(P, cf, j + TPL * (r - 2), NY, v[r]);
     }
     float2 *d = dst + (size_t)j * N;
 #pragma unroll
@@ -197,7 +194,7 @@ __device__ __forceinline__ void column_inverse_store_half(const StageParams &P, 
 // (Tab[a][0] = column transform of G*alpha, Tab[a][1] of G*beta) and the row
 // stage adds z^p Tab[a][0] + z^(nz-1-p) Tab[a][1] to the first and last
 // planes' rows.
-template <class L, int KX>
+template <class L, int KX, int YF>
 __global__ void __launch_bounds__(KX * L::TPL) k_columns_boundary(StageParams P, L line, const float2 *rowspec,
                                                                   float2 *Tab)
 {
@@ -227,8 +224,8 @@ __global__ void __launch_bounds__(KX * L::TPL) k_columns_boundary(StageParams P,
             const int ky = j + r * L::TPL;
             v[r] = (colok && ky < n) ? cmul(g[r], tab[(size_t)ky * P.lNx + kx]) : make_float2(0.f, 0.f);
         }
-        column_inverse_store<L, KX>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
-                                    Tab + ((size_t)(a * 2 * np + t) * P.ny) * P.lNx + kx);
+        column_inverse_store<L, KX, YF>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
+                                        Tab + ((size_t)(a * 2 * np + t) * P.ny) * P.lNx + kx);
     }
 }
 
@@ -236,17 +233,17 @@ __global__ void __launch_bounds__(KX * L::TPL) k_columns_boundary(StageParams P,
 // propagator (exact anchor, then a complex recurrence whose per-element step
 // lives in shared memory), backward FFT along y, crop.  Output
 // T[q-q0][y][kx], y over the cropped height.
-template <class L, int KX, bool HALF>
+template <class L, int KX, bool HALF, int YF>
 __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX * L::TPL <= 512) ? 2 : 1))
     k_columns_propagate(StageParams P, L line, const float2 *rowspec, float2 *T, int q0, int qn, int ppc)
 {
     if (!group_active<KX>(P, blockIdx.x * KX))
         return;  // all-zero columns: the row stage never reads them
-    // power-of-two columns: the per-element propagator step lives in
-    // registers and (N >= 512) the third radix-8 pass reads
-    // per-thread-class twiddles
-    constexpr bool STEP_REGS = kColumnStepRegs && pow2_len<L>() > 0;
-    constexpr bool TW2 = kColumnTw2 && col_tw2<L>();
+    // half-crop plans: the per-element propagator step lives in registers
+    // and (N >= 512) the third radix-8 pass reads per-thread-class twiddles
+    // (for other crops both measured slower: tilted 200^3, 37.5 -> 38.1 ms)
+    constexpr bool STEP_REGS = HALF && kColumnStepRegs;
+    constexpr bool TW2 = HALF && kColumnTw2 && pow2_len<L>() >= 512;
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNy
     const int ls = xslots<true>(n);
@@ -306,10 +303,10 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
                 V[r] = cmul(V[r], stp[ky * KX + c]);
         }
         if constexpr (HALF)
-            column_inverse_store_half<L, KX, TW2>(P, line, v, c, j, buf0, buf1, tw, edge, flip,
+            column_inverse_store_half<L, KX, YF, TW2>(P, line, v, c, j, buf0, buf1, tw, edge, flip,
                                                   T + (size_t)(q - q0) * (L::N / 2) * L::N + kx);
         else
-            column_inverse_store<L, KX, TW2>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
+            column_inverse_store<L, KX, YF, TW2>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
                                              T + (size_t)(q - q0) * ny * lNx + kx);
     }
 }
@@ -332,7 +329,7 @@ constexpr int rows_per_cta()
     return LPC >= 8 ? LPC : 8;
 }
 
-template <class L, int LPC>
+template <class L, int LPC, int NP>
 __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     k_rows_inverse(StageParams P, L line, const float2 *T, const float2 *Tab, float2 *slab, int q0, int qn)
 {
@@ -355,7 +352,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     const int qq = q0 + qrel;  // the grid covers exactly qn jobs
     const int a = qq / nz, p = qq - a * nz;
     const bool pf = P.order >= 2;
-    const int np = P.npoles;
+    constexpr int np = NP;
     // z-boundary weights of this plane: z_i^p (alpha rows), z_i^(nz-1-p)
     // (beta rows), per pole
     float zl[2], zh[2];
@@ -407,7 +404,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
         }
         int flip = 0;
         line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
-        float2 cf[4];
+        float2 cf[2 * NP];
         if (pf) {
             // the line's samples around the crop's ends (periodic): every
             // thread writes its values to the exchange buffer the FFT's last
@@ -430,7 +427,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
 #pragma unroll
             for (int e = 0; e < EDGE_SLOTS; ++e)
                 ed[e] = edge_used(e, np) ? sc[(padxl + edge_offset(e, nx) + 2 * n) % n] : make_float2(0.f, 0.f);
-            pf_coefs(P.kxs, np, ed, cf);
+            pf_coefs<NP>(P.kxs, ed, cf);
         }
         // stage[x][l] (pitch LPC+1) in buf0, then runs of LPC y per x
         __syncthreads();  // every line is done with buf0
@@ -442,7 +439,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
             if (xx >= 0 && xx < nx) {
                 float2 o = v[r];
                 if (pf)
-                    o = pf_apply(P, cf, xx, nx, o);
+                    o = pf_apply<NP>(P, cf, xx, nx, o);
                 stage[xx * SP + l] = valid ? o : make_float2(0.f, 0.f);
             }
         }
@@ -470,8 +467,8 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
 // predicates.  The all-zero spectrum columns (outside the |k| < km disc,
 // not written by the column stage) are a per-thread slot mask computed
 // once.  A CTA owns LPC*G consecutive rows of one job, LPC lines at a time.
-template <class L, int LPC, int G>
-__global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : ((LPC * L::TPL <= 512) ? 2 : 1))
+template <class L, int LPC, int G, int NP>
+__global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     k_rows_inverse_half(StageParams P, L line, const float2 *T, const float2 *Tab, float2 *slab, int q0)
 {
     constexpr int N = L::N, TPL = L::TPL, NX = N / 2, PAD = N / 4, RG = LPC * G, CPJ = NX / RG;
@@ -491,7 +488,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : ((LP
     const int qq = q0 + qrel;
     const int a = qq / nz, p = qq - a * nz;
     const bool pf = P.order >= 2;
-    const int np = P.npoles;
+    constexpr int np = NP;
     float zl[2], zh[2];  // z-boundary weights of this plane, per pole
     bool zb_any = false;
 #pragma unroll
@@ -563,15 +560,15 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : ((LP
                     edge[l * EDGE_SLOTS + e] = t;
             }
             line_sync(bar, TPL);
-            float2 cf[4];
-            pf_coefs(P.kxs, np, edge + l * EDGE_SLOTS, cf);
+            float2 cf[2 * NP];
+            pf_coefs<NP>(P.kxs, edge + l * EDGE_SLOTS, cf);
             const float2 Ac = cf[0], Bc = cf[np];  // first pole
 #pragma unroll
             for (int r = 2; r <= 5; ++r) {
                 v[r] = make_float2(fmaf(Bc.x, zb[r - 2], fmaf(Ac.x, za[r - 2], v[r].x)),
                                    fmaf(Bc.y, zb[r - 2], fmaf(Ac.y, za[r - 2], v[r].y)));
             }
-            if (np == 2) {  // second pole (orders 4, 5)
+            if constexpr (NP == 2) {  // second pole (orders 4, 5)
                 const float2 A2 = cf[1], B2 = cf[3];
 #pragma unroll
                 for (int r = 2; r <= 5; ++r) {
@@ -610,148 +607,6 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : ((LP
     }
 }
 
-// (b2, power-of-two rows of 256 or more, any crop) k_rows_inverse with the
-// per-element work of the half-crop kernel moved out of the row loop: the
-// crop slots, the all-zero column slots and the first pole's x-boundary
-// weights are per-thread masks and registers computed once; edge samples go
-// through the shared buffer at positions computed once per CTA.  A CTA owns
-// LPC*G consecutive rows of one job (rows y >= ny are not run).
-template <class L, int LPC, int G>
-__global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
-    k_rows_inverse_pow2(StageParams P, L line, const float2 *T, const float2 *Tab, float2 *slab, int q0)
-{
-    constexpr int N = L::N, TPL = L::TPL, RG = LPC * G;
-    extern __shared__ float2 smem[];
-    constexpr int ls = xslots<false>(N);
-    float2 *buf0 = smem, *buf1 = smem + LPC * ls, *tw = smem + 2 * LPC * ls;
-    float2 *edge = tw + tw_slots(N);  // [LPC][EDGE_SLOTS]
-    copy_twiddles<L>(tw, P.tab.twx, N);
-    const int l = threadIdx.x / TPL, j = threadIdx.x % TPL;
-    const int bar = 1 + l;  // each line is whole warps (TPL >= 32)
-    const int ny = P.ny, nx = P.nx, nz = P.nz, padxl = P.padxl, yp = P.ypitch;
-    const int cpj = (ny + RG - 1) / RG;
-    const int qrel = (int)blockIdx.x / cpj;
-    const int ybase = ((int)blockIdx.x - qrel * cpj) * RG;
-    const int GV = min(G, (ny - ybase + LPC - 1) / LPC);
-    const int qq = q0 + qrel;
-    const int a = qq / nz, p = qq - a * nz;
-    const bool pf = P.order >= 2;
-    const int np = P.npoles;
-    float zl[2], zh[2];
-    bool zb_any = false;
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        zl[i] = (pf && i < np && p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + p] : 0.f;
-        zh[i] = (pf && i < np && nz - 1 - p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + nz - 1 - p] : 0.f;
-        zb_any = zb_any || zl[i] != 0.f || zh[i] != 0.f;
-    }
-    unsigned zmask = 0, cmask = 0;
-    float za[8], zb[8];
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-        const int x = j + r * TPL, xx = x - padxl;
-        if (x >= P.kx_zero_lo && x < P.kx_zero_hi)
-            zmask |= 1u << r;
-        if (xx >= 0 && xx < nx)
-            cmask |= 1u << r;
-        za[r] = (pf && xx >= 0 && xx < ZPOW_N) ? P.tab.zpow[xx] : 0.f;
-        zb[r] = (pf && xx < nx && nx - 1 - xx < ZPOW_N) ? P.tab.zpow[nx - 1 - xx] : 0.f;
-    }
-    int epos[EDGE_SLOTS];  // line positions of the edge samples
-#pragma unroll
-    for (int e = 0; e < EDGE_SLOTS; ++e)
-        epos[e] = (padxl + edge_offset(e, nx) + 2 * N) % N;
-    const float2 *Tq = T + (size_t)qrel * ny * N + j;
-    float2 *dst = slab + ((size_t)a * nz + p) * nx * yp + ybase;
-    auto load_row = [&](int y, float2 (&v)[L::SLOTS]) {
-        const bool valid = y < ny;
-        const float2 *src = Tq + (size_t)(valid ? y : 0) * N;
-#pragma unroll
-        for (int r = 0; r < L::SLOTS; ++r)
-            v[r] = (!valid || ((zmask >> r) & 1u)) ? make_float2(0.f, 0.f) : __ldcs(src + r * TPL);
-    };
-    float2 v[L::SLOTS], vn[L::SLOTS];
-    load_row(ybase + l, v);
-    __syncthreads();  // twiddles
-#pragma unroll 1
-    for (int g = 0; g < GV; ++g) {
-        const int y = ybase + g * LPC + l;
-        const bool valid = y < ny;
-        if (g + 1 < GV)
-            load_row(y + LPC, vn);
-        if (valid && zb_any) {
-#pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                if (i < np) {
-                    const float2 *ta = Tab + ((size_t)(a * 2 * np + i) * ny + y) * N + j;
-                    const float2 *tb = Tab + ((size_t)(a * 2 * np + np + i) * ny + y) * N + j;
-#pragma unroll
-                    for (int r = 0; r < L::SLOTS; ++r) {
-                        if (!((zmask >> r) & 1u)) {
-                            const float2 u = ta[r * TPL], w = tb[r * TPL];
-                            v[r] = make_float2(fmaf(zh[i], w.x, fmaf(zl[i], u.x, v[r].x)),
-                                               fmaf(zh[i], w.y, fmaf(zl[i], u.y, v[r].y)));
-                        }
-                    }
-                }
-            }
-        }
-        int flip = 0;
-        line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
-        if (pf) {
-#pragma unroll
-            for (int e = 0; e < EDGE_SLOTS; ++e) {
-                float2 t;
-                if (edge_used(e, np) && held<L>(v, j, epos[e], t))
-                    edge[l * EDGE_SLOTS + e] = t;
-            }
-            line_sync(bar, TPL);
-            float2 cf[4];
-            pf_coefs(P.kxs, np, edge + l * EDGE_SLOTS, cf);
-            const float2 Ac = cf[0], Bc = cf[np];
-#pragma unroll
-            for (int r = 0; r < 8; ++r)
-                v[r] = make_float2(fmaf(Bc.x, zb[r], fmaf(Ac.x, za[r], v[r].x)),
-                                   fmaf(Bc.y, zb[r], fmaf(Ac.y, za[r], v[r].y)));
-            if (np == 2) {  // second pole (orders 4, 5)
-                const float2 A2 = cf[1], B2 = cf[3];
-#pragma unroll
-                for (int r = 0; r < 8; ++r) {
-                    const int xx = j + TPL * r - padxl;
-                    if (xx >= 0 && xx < ZPOW_N) {
-                        const float z = P.tab.zpow[ZPOW_N + xx];
-                        v[r] = make_float2(fmaf(A2.x, z, v[r].x), fmaf(A2.y, z, v[r].y));
-                    }
-                    if (xx < nx && nx - 1 - xx < ZPOW_N) {
-                        const float z = P.tab.zpow[ZPOW_N + nx - 1 - xx];
-                        v[r] = make_float2(fmaf(B2.x, z, v[r].x), fmaf(B2.y, z, v[r].y));
-                    }
-                }
-            }
-        }
-        // stage[x][l] (pitch LPC+1) in buf0, then runs of LPC y per x
-        __syncthreads();  // every line is done with buf0 (and edge)
-        float2 *stage = buf0;
-        constexpr int SP = LPC + 1;
-#pragma unroll
-        for (int r = 0; r < 8; ++r)
-            if ((cmask >> r) & 1u)
-                stage[(j + TPL * r - padxl) * SP + l] = valid ? v[r] : make_float2(0.f, 0.f);
-        __syncthreads();
-        for (int e = threadIdx.x; e < nx * LPC; e += LPC * TPL) {
-            const int xx = e / LPC, ll = e - (e / LPC) * LPC;
-            if (ybase + g * LPC + ll < ny)
-                __stcs(dst + (size_t)xx * yp + g * LPC + ll, stage[xx * SP + ll]);
-        }
-        if (g + 1 < GV) {
-            __syncthreads();  // stage reads done before buf0 is reused
-#pragma unroll
-            for (int r = 0; r < L::SLOTS; ++r)
-                v[r] = vn[r];
-        }
-    }
-}
-
 // (b1+b2) single-row planes (lNy == ny == 1, slab pitch 1: the 2D
 // reconstruction): the column transforms are the identity, so a job's row
 // is the row spectrum times the filter table (and gains) and the propagator
@@ -763,7 +618,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
 // group every line is anchored exactly.  Then per line the z-boundary rows
 // of its plane, the backward FFT along x, the x-prefilter boundary terms,
 // and the cropped row stored contiguously at slab[a][p][x].
-template <class L, int LPC>
+template <class L, int LPC, int NP>
 __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
     k_rows_line(StageParams P, L line, const float2 *rowspec, const float2 *Tab, float2 *slab, int q0, int qn)
 {
@@ -818,7 +673,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
             cur_a = a;
         }
         if (valid && pf) {
-            const int np = P.npoles;
+            constexpr int np = NP;
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
                 const float zl = (i < np && p < ZPOW_N) ? P.tab.zpow[i * ZPOW_N + p] : 0.f;
@@ -840,7 +695,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
         }
         int flip = 0;
         line.template run<1>(v, j, buf0 + l * ls, buf1 + l * ls, 1, tw, flip, bar);
-        float2 cf[4];
+        float2 cf[2 * NP];
         if (pf) {
             // the line's samples at x0-1, x0+1, x1-1, x1+1 (periodic), through
             // the exchange buffer the FFT's last exchange did not use
@@ -858,8 +713,8 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
             float2 ed[EDGE_SLOTS];
 #pragma unroll
             for (int e = 0; e < EDGE_SLOTS; ++e)
-                ed[e] = edge_used(e, P.npoles) ? sc[(padxl + edge_offset(e, nx) + 2 * n) % n] : make_float2(0.f, 0.f);
-            pf_coefs(P.kxs, P.npoles, ed, cf);
+                ed[e] = edge_used(e, NP) ? sc[(padxl + edge_offset(e, nx) + 2 * n) % n] : make_float2(0.f, 0.f);
+            pf_coefs<NP>(P.kxs, ed, cf);
         }
         if (valid) {
             float2 *dst = slab + ((size_t)a * nz + p) * nx;
@@ -869,7 +724,7 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 3 : 1)
                 if (xx >= 0 && xx < nx) {
                     float2 o = v[r];
                     if (pf)
-                        o = pf_apply(P, cf, xx, nx, o);
+                        o = pf_apply<NP>(P, cf, xx, nx, o);
                     __stcs(dst + xx, o);
                 }
             }
@@ -929,6 +784,30 @@ static int planes_per_cta(const StageParams &P, int qn)
     return std::min(32, std::max(4, ppc));
 }
 
+// Calls fn(std::integral_constant<int, V>) for V = v (one of 0, 1, 2), so a
+// pole count chosen at run time selects a compile-time instantiation.
+template <class F>
+static cudaError_t with_poles(int v, F &&fn)
+{
+    switch (v) {
+    case 0: return fn(std::integral_constant<int, 0>{});
+    case 1: return fn(std::integral_constant<int, 1>{});
+    case 2: return fn(std::integral_constant<int, 2>{});
+    default: return cudaErrorInvalidValue;
+    }
+}
+// Poles of the y-prefilter the column stage applies (tilted path, order
+// >= 2), 0 for none; poles of the x- and z-prefilters of the row stages
+// (1 also for orders 0 and 1, where the row stages skip the prefilter).
+static int column_poles(const StageParams &P)
+{
+    return (P.tilted && P.order >= 2) ? P.npoles : 0;
+}
+static int row_poles(const StageParams &P)
+{
+    return P.order >= 4 ? 2 : 1;
+}
+
 template <class L>
 static cudaError_t rows_forward_impl(const StageParams &P, L line, const void *sino, const double *w, int nb,
                                      float2 *out, cudaStream_t s)
@@ -946,8 +825,11 @@ static cudaError_t boundary_impl(const StageParams &P, L line, const float2 *row
 {
     constexpr int KX = Cfg<L>::KX;
     dim3 grid((P.lNx + KX - 1) / KX, nb);
-    k_columns_boundary<L, KX><<<grid, KX * L::TPL, smem_cols<L>(line.n), s>>>(P, line, rowspec, Tab);
-    return cudaGetLastError();
+    return with_poles(column_poles(P), [&](auto yf) {
+        k_columns_boundary<L, KX, decltype(yf)::value>
+            <<<grid, KX * L::TPL, smem_cols<L>(line.n), s>>>(P, line, rowspec, Tab);
+        return cudaGetLastError();
+    });
 }
 
 // Lines of a half-crop row kernel: whole warps (the line barriers are
@@ -966,15 +848,6 @@ constexpr int half_groups()
 {
     return Cfg<L>::LPC >= 16 ? 1 : 16 / Cfg<L>::LPC;
 }
-// Lines per CTA of the half-crop row kernel: with 64-thread lines, 8 lines
-// (512 threads, 2 CTAs per SM), so that the transposed store writes runs of
-// 8 y (64 bytes) per x instead of 4.
-template <class L>
-constexpr int half_rows_lpc()
-{
-    return (kRowsHalfLpc8 && L::TPL == 64) ? 8 : Cfg<L>::LPC;
-}
-
 template <class L>
 static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rowspec, float2 *T, int q0, int qn,
                                 cudaStream_t s)
@@ -982,16 +855,19 @@ static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rows
     constexpr int KX = Cfg<L>::KX;
     const int ppc = planes_per_cta<KX>(P, qn);
     dim3 grid((P.lNx + KX - 1) / KX, (qn + ppc - 1) / ppc);
-    if constexpr (half_line<L>()) {
-        if (half_crop(P)) {
-            k_columns_propagate<L, KX, true>
-                <<<grid, KX * L::TPL, smem_cols_half<L>(line.n), s>>>(P, line, rowspec, T, q0, qn, ppc);
-            return cudaGetLastError();
+    return with_poles(column_poles(P), [&](auto yf) {
+        constexpr int YF = decltype(yf)::value;
+        if constexpr (half_line<L>()) {
+            if (half_crop(P)) {
+                k_columns_propagate<L, KX, true, YF>
+                    <<<grid, KX * L::TPL, smem_cols_half<L>(line.n), s>>>(P, line, rowspec, T, q0, qn, ppc);
+                return cudaGetLastError();
+            }
         }
-    }
-    k_columns_propagate<L, KX, false><<<grid, KX * L::TPL, smem_cols_prop<L>(line.n), s>>>(P, line, rowspec, T, q0,
-                                                                                         qn, ppc);
-    return cudaGetLastError();
+        k_columns_propagate<L, KX, false, YF>
+            <<<grid, KX * L::TPL, smem_cols<L>(line.n), s>>>(P, line, rowspec, T, q0, qn, ppc);
+        return cudaGetLastError();
+    });
 }
 
 template <class L>
@@ -999,32 +875,66 @@ static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 
                                      float2 *slab, int q0, int qn, cudaStream_t s)
 {
     constexpr int LPC = Cfg<L>::LPC;
-    if constexpr (half_line<L>()) {
-        if (half_crop(P)) {
-            constexpr int LH = half_rows_lpc<L>(), G = 16 / LH;
-            const unsigned grid = (unsigned)((long long)qn * (L::N / 2 / (LH * G)));
-            k_rows_inverse_half<L, LH, G><<<grid, LH * L::TPL, smem_rows_half<L, LH>(line.n), s>>>(P, line, T, Tab,
-                                                                                                 slab, q0);
+    return with_poles(row_poles(P), [&](auto np) {
+        constexpr int NP = decltype(np)::value;
+        if constexpr (NP >= 1) {
+            if constexpr (half_line<L>()) {
+                if (half_crop(P)) {
+                    constexpr int G = half_groups<L>();
+                    const unsigned grid = (unsigned)((long long)qn * (L::N / 2 / (LPC * G)));
+                    k_rows_inverse_half<L, LPC, G, NP>
+                        <<<grid, LPC * L::TPL, smem_rows_half<L>(line.n), s>>>(P, line, T, Tab, slab, q0);
+                    return cudaGetLastError();
+                }
+            }
+            const unsigned grid =
+                (unsigned)((long long)qn * ((P.ny + rows_per_cta<LPC>() - 1) / rows_per_cta<LPC>()));
+            k_rows_inverse<L, LPC, NP>
+                <<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, Tab, slab, q0, qn);
             return cudaGetLastError();
+        } else {
+            return cudaErrorInvalidValue;
         }
-    }
-    if constexpr (half_line<L>()) {
-        if (kRowsPow2 && !single_row_plan(P) && P.ny > 1) {
-            constexpr int G = half_groups<L>();
-            const unsigned grid = (unsigned)((long long)qn * ((P.ny + LPC * G - 1) / (LPC * G)));
-            k_rows_inverse_pow2<L, LPC, G><<<grid, LPC * L::TPL, smem_rows_half<L>(line.n), s>>>(P, line, T, Tab,
-                                                                                               slab, q0);
-            return cudaGetLastError();
-        }
-    }
-    const unsigned grid = (unsigned)((long long)qn * ((P.ny + rows_per_cta<LPC>() - 1) / rows_per_cta<LPC>()));
-    k_rows_inverse<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, Tab, slab, q0, qn);
-    return cudaGetLastError();
+    });
 }
 
 // The attribute is per kernel and process-wide, so it is always set to the
 // largest size the instantiation can need (the generic line serves every
 // length up to its maximum).
+template <class L, int NP>
+static cudaError_t set_smem_attrs_np(int n)
+{
+    cudaError_t e;
+    if constexpr (NP >= 1) {
+        e = cudaFuncSetAttribute(k_rows_inverse<L, Cfg<L>::LPC, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem_rows<L>(n));
+        if (e != cudaSuccess)
+            return e;
+        e = cudaFuncSetAttribute(k_rows_line<L, Cfg<L>::LPC, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem_rows<L>(n));
+        if (e != cudaSuccess)
+            return e;
+    }
+    if constexpr (half_line<L>()) {
+        e = cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX, true, NP>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols_half<L>(n));
+        if (e != cudaSuccess)
+            return e;
+        if constexpr (NP >= 1) {
+            e = cudaFuncSetAttribute(k_rows_inverse_half<L, Cfg<L>::LPC, half_groups<L>(), NP>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rows_half<L>(n));
+            if (e != cudaSuccess)
+                return e;
+        }
+    }
+    e = cudaFuncSetAttribute(k_columns_boundary<L, Cfg<L>::KX, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_cols<L>(n));
+    if (e != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX, false, NP>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols<L>(n));
+}
+
 template <class L>
 static cudaError_t set_smem_attrs(int n)
 {
@@ -1035,35 +945,12 @@ static cudaError_t set_smem_attrs(int n)
                              (int)smem_rows<L>(n));
     if (e != cudaSuccess)
         return e;
-    e = cudaFuncSetAttribute(k_rows_inverse<L, Cfg<L>::LPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem_rows<L>(n));
-    if (e != cudaSuccess)
-        return e;
-    e = cudaFuncSetAttribute(k_rows_line<L, Cfg<L>::LPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem_rows<L>(n));
-    if (e != cudaSuccess)
-        return e;
-    e = cudaFuncSetAttribute(k_columns_boundary<L, Cfg<L>::KX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem_cols<L>(n));
-    if (e != cudaSuccess)
-        return e;
-    if constexpr (half_line<L>()) {
-        e = cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX, true>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols_half<L>(n));
-        if (e != cudaSuccess)
-            return e;
-        e = cudaFuncSetAttribute(k_rows_inverse_half<L, half_rows_lpc<L>(), 16 / half_rows_lpc<L>()>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem_rows_half<L, half_rows_lpc<L>()>(n));
-        if (e != cudaSuccess)
-            return e;
-        e = cudaFuncSetAttribute(k_rows_inverse_pow2<L, Cfg<L>::LPC, half_groups<L>()>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rows_half<L>(n));
+    for (int np = 0; np <= 2; ++np) {
+        e = with_poles(np, [&](auto v) { return set_smem_attrs_np<L, decltype(v)::value>(n); });
         if (e != cudaSuccess)
             return e;
     }
-    return cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX, false>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols_prop<L>(n));
+    return cudaSuccess;
 }
 
 int columns_slots(const StageParams &P)
@@ -1075,8 +962,8 @@ int columns_slots(const StageParams &P)
     const cudaError_t e = with_line(P.lNy, [&](auto line) {
         using L = decltype(line);
         constexpr int KX = Cfg<L>::KX;
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_columns_propagate<L, KX, false>, KX * L::TPL,
-                                                             smem_cols_prop<L>(line.n));
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_columns_propagate<L, KX, false, 0>,
+                                                             KX * L::TPL, smem_cols<L>(line.n));
     });
     return e == cudaSuccess ? per * sms : 0;
 }
@@ -1130,8 +1017,16 @@ cudaError_t launch_rows_line(const StageParams &P, const float2 *rowspec, const 
         using L = decltype(line);
         constexpr int LPC = Cfg<L>::LPC;
         const unsigned grid = (unsigned)((qn + rows_per_cta<LPC>() - 1) / rows_per_cta<LPC>());
-        k_rows_line<L, LPC><<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, rowspec, Tab, slab, q0, qn);
-        return cudaGetLastError();
+        return with_poles(row_poles(P), [&](auto np) {
+            constexpr int NP = decltype(np)::value;
+            if constexpr (NP >= 1) {
+                k_rows_line<L, LPC, NP>
+                    <<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, rowspec, Tab, slab, q0, qn);
+                return cudaGetLastError();
+            } else {
+                return cudaErrorInvalidValue;
+            }
+        });
     });
 }
 
