@@ -23,6 +23,7 @@ padfac 1.75 (512x512 padded FFTs), intp_order=2, output 256^3 complex64.
   apple  apple.correct of the headline reconstruction
   ri     odt_to_ri of a 256^3 volume (opt_to_ri beside it)
   bpp2d  backpropagate_2d, A=400 x 512
+  mlp    the learned-gain network alone (tcgen05 and mma.sync kernels)
 
 value   device-resident throughput (sinogram already in HBM; the prepared
         plan's kernels timed with CUDA events on their stream, L2 flushed
@@ -103,6 +104,12 @@ WORKLOADS["c5"] = dict(
     name="learned wedge filter: A=40 uniform over 120 deg, 128x128 -> 128^3, "
          "shipped network (trained on 2000 phantoms); rel-L2 to the plain "
          "A=400 full-circle reconstruction on held-out phantoms")
+# the learned-gain network alone on the wedge configuration's points
+WORKLOADS["mlp"] = dict(
+    A=40, n=128, res=3.0, nm=1.333, padfac=1.75,
+    name="learned-gain MLP 4-64-64-64-2 (SiLU, BF16 operands, FP32 "
+         "accumulation) on the 40-angle wedge configuration's filter support "
+         "of the 256x256 padded grid: inference and backward")
 # sinogram preparation of the headline sinogram (the step before the
 # reconstruction; the reference's sinogram_as_rytov)
 WORKLOADS["rytov"] = dict(
@@ -913,6 +920,69 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+def run_mlp(args):
+    """The learned-gain network on the wedge configuration's point set
+    (40 angles x the filter support of the 256^2 padded grid): inference and
+    backward (data part + weight gradients) on the tcgen05 kernels, and the
+    same network on the warp-level mma.sync kernels beside it (selected with
+    odt_mlp_select_kernels), timed with CUDA events in the same run."""
+    import torch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    from odtbrain_gb300 import build as native_build
+    native_build.build()
+    from odtbrain_gb300 import _native
+    from odtbrain_gb300._alg3d import Backprop3D
+    from odtbrain_gb300.learned import (WEDGE_CONFIG, load_learned_filter,
+                                        wedge_angles)
+    c = dict(WEDGE_CONFIG)
+    A, n = c["num_angles"], c["n"]
+    rec = Backprop3D((A, n, n), wedge_angles(A, c["span"]), c["res"], c["nm"],
+                     device=dev)
+    lf = load_learned_filter(rec)
+    g = lf.gains()
+    rng = np.random.default_rng(3)
+    dg = torch.tensor((rng.normal(size=tuple(g.shape)) + 1j *
+                       rng.normal(size=tuple(g.shape))).astype(np.complex64),
+                      device=dev)
+    points = int(A * lf.positions.numel())
+    L = _native.lib()
+    flush = torch.empty(L2_FLUSH_BYTES, device=dev, dtype=torch.uint8)
+    stream = torch.cuda.current_stream(dev)
+
+    def forward():
+        lf.mlp.gains(lf.feat, *rec.gain_shape(), out=g,
+                     positions=lf.positions)
+
+    def backward():
+        lf.mlp.grads(lf.feat, dg, positions=lf.positions)
+
+    times = {}
+    try:
+        for family, tc in (("tcgen05", 1), ("mma_sync", 0)):
+            _native.check(L.odt_mlp_select_kernels(tc))
+            for name, fn in (("forward", forward), ("backward", backward)):
+                ms, _ = _timed(fn, args.steps, args.warmup, flush, stream)
+                times["%s_%s_ms" % (family, name)] = ms
+            lf.mlp.check()
+    finally:
+        _native.check(L.odt_mlp_select_kernels(1))
+    # 2 * (4*64 + 64*64 + 64*64 + 64*2) FLOP per point through the network
+    flop = 2.0 * (4 * 64 + 64 * 64 + 64 * 64 + 64 * 2)
+    ms = times["tcgen05_forward_ms"]
+    w = WORKLOADS["mlp"]
+    line = _base_line(args, w, points / (ms / 1e3), ms, {})
+    line.update({
+        "metric": "learned-gain MLP inference points/s on 1 GB300 "
+                  "(tcgen05, BF16 operands, FP32 accumulation)",
+        "unit": "points/s", "dtype": "bf16 (fp32 accumulation)",
+        "points": points, "tflops_inference": points * flop / (ms / 1e3) / 1e12,
+        "kernels": times,
+        "gpu_launches": args.steps,  # one inference launch per timed step
+        "cpu_baseline": None})
+    print(json.dumps(line), flush=True)
+
+
 def measure_learned(args, dev, n_eval):
     """The learned wedge filter (A=40 over 120 deg, 128^2 -> 128^3): GPU
     time learned vs plain, and mean rel-L2 to the plain dense A=400
@@ -1514,6 +1584,13 @@ def main():
             run_reference_bpp2d(args)
         else:
             run_bpp2d(args)
+    elif args.config == "mlp":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "no counterpart in the reference (it has a "
+                              "fixed filter)"}))
+        else:
+            run_mlp(args)
     elif args.config in ("c4", "c5"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":

@@ -254,6 +254,13 @@ odt_status odt_mlp_gain_forward(const odt_mlp_params *params,
  * the last call (the gains of that call are then invalid). */
 odt_status odt_mlp_read_status(void *stream);
 
+/* Kernel family of odt_mlp_gain_forward and odt_mlp_gain_backward, process
+ * wide: 1 (the default) the tcgen05 kernels (BF16 operands, FP32
+ * accumulators in tensor memory), 0 the same network on warp-level
+ * mma.sync; both give the same results within BF16 rounding.  For
+ * comparisons.  No counterpart in the reference. */
+odt_status odt_mlp_select_kernels(int32_t tensor_memory);
+
 /* Device bytes of the activation store odt_mlp_gain_backward needs for
  * num_positions positions per angle. */
 odt_status odt_mlp_store_size(int32_t num_angles, int32_t num_positions,

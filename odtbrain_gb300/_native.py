@@ -44,6 +44,7 @@ EXPORTED_SYMBOLS = (
     "odt_mlp_store_size",
     "odt_mlp_gain_backward",
     "odt_mlp_read_status",
+    "odt_mlp_select_kernels",
     "odt_odt_to_ri",
     "odt_opt_to_ri",
     "odt_sino_workspace_size",
@@ -226,6 +227,7 @@ def lib():
         L.odt_mlp_gain_forward.argtypes = [ctypes.POINTER(MlpParams), i32,
                                            i32, i32, vp, vp, i32, vp, vp]
         L.odt_mlp_read_status.argtypes = [vp]
+        L.odt_mlp_select_kernels.argtypes = [i32]
         L.odt_mlp_store_size.argtypes = [i32, i32,
                                          ctypes.POINTER(ctypes.c_uint64)]
         L.odt_mlp_gain_backward.argtypes = [
@@ -239,6 +241,7 @@ def lib():
                      "odt_bpp3d_read_status", "odt_bpp3d_plan_destroy",
                      "odt_mlp_gain_forward", "odt_mlp_store_size",
                      "odt_mlp_gain_backward", "odt_mlp_read_status",
+                     "odt_mlp_select_kernels",
                      "odt_odt_to_ri",
                      "odt_opt_to_ri", "odt_sino_workspace_size",
                      "odt_sino_prepare", "odt_sino_launch_count",

@@ -33,6 +33,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 #include "../../include/odtbrain_gb300.h"
@@ -264,10 +265,11 @@ __device__ __forceinline__ void to_a(const float (&H)[NT][4], uint32_t (&A)[NT /
 // warp walks 16-point groups with a grid stride, the weights stay in shared
 // memory.
 constexpr int FWD_WARPS = 8;
-// Inference runs on tcgen05 (k_mlp_forward_tc); k_mlp_forward, the same
-// network on the legacy warp-level mma.sync path, is kept for comparison
-// (1.62 M points of the 40-angle 128^3 wedge: 0.179 ms against 0.195 ms).
-constexpr bool kMlpTensorMemory = true;
+// Inference and the data part of the backward pass run on tcgen05
+// (k_mlp_forward_tc, k_mlp_backward_data_tc) unless odt_mlp_select_kernels
+// picks the same network on the warp-level mma.sync path (k_mlp_forward,
+// k_mlp_backward_data), which is kept for comparison.
+std::atomic<int> g_mlp_tensor_memory{1};
 
 __global__ void __launch_bounds__(32 * FWD_WARPS) k_mlp_forward(MlpWeights W, MlpGrid Gd, float2 *gain)
 {
@@ -697,6 +699,10 @@ __global__ void __launch_bounds__(128, 1) k_mlp_backward_data_tc(MlpWeights W, M
         float f[4] = {0.f, 0.f, 0.f, 0.f};
         if (valid)
             point_features(Gd, p, f);
+        // The A operand changes layout here (K = 64 -> 16): the previous
+        // tile's last rows, written by every thread in the K = 64 layout,
+        // overlap other rows' K = 16 addresses, so all of them land first.
+        __syncthreads();
         const uint4 h0 = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), 0u, 0u);
         *reinterpret_cast<uint4 *>(S.a + tc::kmaj(row, 0, 2)) = h0;
         *reinterpret_cast<uint4 *>(S.a + tc::kmaj(row, 1, 2)) = make_uint4(0u, 0u, 0u, 0u);
@@ -726,6 +732,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_backward_data_tc(MlpWeights W, M
         const long long gi = valid ? gain_index(Gd, p) : -1;
         const float2 d = gi >= 0 ? dgain[gi] : make_float2(0.f, 0.f);
         const uint4 dz4 = make_uint4(pack_bf16(d.x, d.y), 0u, 0u, 0u);
+        __syncthreads();  // every H3 row (K = 64 layout) is written before the K = 16 rows
         *reinterpret_cast<uint4 *>(S.a + tc::kmaj(row, 0, 2)) = dz4;
         *reinterpret_cast<uint4 *>(S.a + tc::kmaj(row, 1, 2)) = make_uint4(0u, 0u, 0u, 0u);
         if (valid) {
@@ -922,7 +929,7 @@ odt_status odt_mlp_gain_forward(const odt_mlp_params *params, int32_t num_angles
         return st;
     if (!gain || !aligned(gain, 8))
         return err(ODT_ERR_INVALID_ARGUMENT, "gain must be non-NULL and 8-byte aligned");
-    if (kMlpTensorMemory) {
+    if (g_mlp_tensor_memory.load(std::memory_order_relaxed)) {
         static thread_local int configured_device = -1;
         int dev = 0;
         cudaError_t e = cudaGetDevice(&dev);
@@ -981,6 +988,14 @@ odt_status odt_mlp_store_size(int32_t num_angles, int32_t num_positions, uint64_
     return ODT_OK;
 }
 
+odt_status odt_mlp_select_kernels(int32_t tensor_memory)
+{
+    if (tensor_memory != 0 && tensor_memory != 1)
+        return err(ODT_ERR_INVALID_ARGUMENT, "tensor_memory must be 0 or 1");
+    g_mlp_tensor_memory.store(tensor_memory, std::memory_order_relaxed);
+    return ODT_OK;
+}
+
 odt_status odt_mlp_gain_backward(const odt_mlp_params *params, int32_t num_angles, int32_t pad_ny, int32_t pad_nx,
                                  const float *angle_features, const int32_t *positions, int32_t num_positions,
                                  const void *gain_grad, void *store, const odt_mlp_grads *grads, void *stream)
@@ -1015,7 +1030,7 @@ odt_status odt_mlp_gain_backward(const odt_mlp_params *params, int32_t num_angle
     const long long want = (groups + BWD_WARPS - 1) / BWD_WARPS;
     const long long cap = 4LL * sms;
     cudaError_t e = cudaSuccess;
-    if (kMlpTensorMemory) {
+    if (g_mlp_tensor_memory.load(std::memory_order_relaxed)) {
         static thread_local int configured_device = -1;
         int dev = 0;
         e = cudaGetDevice(&dev);
