@@ -325,6 +325,10 @@ odt_status validate(const odt_bpp3d_desc *d)
                     "FFT length must be a power of two in [64, 4096] or any length <= 1024");
     if (!d->filter || !d->kz_phase)
         return fail(ODT_ERR_INVALID_ARGUMENT, "filter and kz_phase tables are required");
+    // the resampling kernels address one angle's slab [z][x][y pitch] with
+    // 32-bit element offsets
+    if ((long long)d->nx * d->nx * odt::yaxis_slab_pitch(d->ny) >= (1ll << 31))
+        return fail(ODT_ERR_UNSUPPORTED, "one angle's coefficient slab must hold fewer than 2^31 elements");
     return ODT_OK;
 }
 

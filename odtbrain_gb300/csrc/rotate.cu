@@ -270,26 +270,32 @@ constexpr int R2_THREADS = 512;
 constexpr int R2_KAHAN = 8;     // angles summed plainly between Kahan steps
 constexpr int R2_RING = 4;      // tile records in flight (angles a..a+3)
 constexpr int R2_WMAX = 6;      // spline taps per axis, up to order 5
-// Shape of the y-axis resampling per spline order.  Orders <= 3: 16 y per
-// CTA, footprints of at most 28 x 28 positions (the tile's coordinate span,
-// at most 15 sqrt(2), plus the taps and one position of margin on each
-// side); orders 4 and 5 reach 30 x 30, so their CTAs take 8 y to keep two
-// footprint buffers in shared memory.  LPO lanes (2 y each) share an
-// output.  The parameter record of an output: 4 words (box offset, in/out
-// flag), then the z and x weights, each duplicated into a (w, w) pair for
-// packed FMAs; at least 20 words (80 bytes), so that the 16-byte stores of
-// 8 consecutive threads hit disjoint banks.
+// Shape of the y-axis resampling per spline order.  A footprint spans the
+// tap starts of the tile's outputs (their coordinates span at most
+// 15 (|cos| + |sin|) <= 15 sqrt(2), so at most 22 starts), plus the ORDER + 1
+// taps and one position of margin on each side: at most 25 + ORDER
+// positions per axis (k_rotate_y_setup checks it).  Orders <= 3: 16 y per
+// CTA; orders 4 and 5 (30 x 30) take 8 y to keep two footprint buffers in
+// shared memory.  LPO lanes (2 y each) share an output.  The parameter
+// record of an output: 4 words (box offset, in/out flag), then the z and x
+// weights, each duplicated into a (w, w) pair for packed FMAs; at least 20
+// words (80 bytes), so that the 16-byte stores of 8 consecutive threads hit
+// disjoint banks.  Where two record buffers fit next to the two footprint
+// buffers (every order but 3), the records of angle a+1 are computed while
+// angle a is interpolated (DBL), with one barrier per angle.
 template <int ORDER>
 struct RotY {
-    static constexpr int Y = ORDER >= 4 ? 8 : 16;     // y values per CTA
-    static constexpr int BOX = ORDER >= 4 ? 30 : 28;  // max footprint per axis (virtual positions)
-    static constexpr int BOXE = BOX * BOX * Y;        // float2 per footprint buffer
-    static constexpr int LPO = Y / 2;                 // lanes per output
+    static constexpr int Y = ORDER >= 4 ? 8 : 16;              // y values per CTA
+    static constexpr int BOX = ORDER >= 4 ? 30 : 25 + ORDER;   // max footprint per axis (virtual positions)
+    static constexpr int BOXE = BOX * BOX * Y;                 // float2 per footprint buffer
+    static constexpr int LPO = Y / 2;                          // lanes per output
     static constexpr int OUTW = R2_T * R2_T * LPO / R2_THREADS;  // outputs per thread
-    static constexpr int SUMS = 2 * OUTW;             // (output, y) sums per thread
+    static constexpr int SUMS = 2 * OUTW;                      // (output, y) sums per thread
     static constexpr int PW = 4 + 4 * (ORDER + 1) > 20 ? 4 + 4 * (ORDER + 1) : 20;
-    static constexpr size_t SMEM = (size_t)2 * BOXE * sizeof(float2) + (size_t)R2_T * R2_T * PW * sizeof(float) +
-                                   (size_t)R2_RING * 64 + 2 * sizeof(uint64_t);
+    static constexpr size_t PRM = (size_t)R2_T * R2_T * PW * sizeof(float);  // one record buffer
+    static constexpr size_t FIXED = (size_t)2 * BOXE * sizeof(float2) + (size_t)R2_RING * 64 + 2 * sizeof(uint64_t);
+    static constexpr bool DBL = FIXED + 2 * PRM <= 227 * 1024;
+    static constexpr size_t SMEM = FIXED + (DBL ? 2 : 1) * PRM;
 };
 
 // Footprints whose positions are all inside the slab (no mirrored
@@ -569,8 +575,9 @@ __global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const f
     constexpr int R2_Y = C::Y, R2_BOXE = C::BOXE, PW = C::PW, R2_OUT = C::SUMS, LPO = C::LPO;
     extern __shared__ __align__(1024) float4 r2_smem[];
     float2 *box = reinterpret_cast<float2 *>(r2_smem);       // [2][R2_BOXE]
-    float *prm = reinterpret_cast<float *>(box + 2 * R2_BOXE); // [256][PW]
-    TileGeo *ring = reinterpret_cast<TileGeo *>(prm + R2_T * R2_T * PW);  // [R2_RING]
+    float *prm = reinterpret_cast<float *>(box + 2 * R2_BOXE); // [DBL ? 2 : 1][256][PW]
+    constexpr int PRMN = R2_T * R2_T * PW;  // floats per record buffer
+    TileGeo *ring = reinterpret_cast<TileGeo *>(prm + (C::DBL ? 2 : 1) * PRMN);  // [R2_RING]
     uint64_t *bar = reinterpret_cast<uint64_t *>(ring + R2_RING);  // [2]: TMA copies into box[0], box[1]
     unsigned phase = 0;  // bit b: parity of the next TMA completion of box[b]
     const int tid = threadIdx.x;
@@ -624,25 +631,13 @@ __global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const f
             stage_box<R2_Y>(t, slab + (size_t)aa * aslab_stride, nz, nx, yp, y0, box + b * R2_BOXE);
         }
     };
-    TileGeo cur = load_tile(ring);
-    stage(cur, 0, 0);
-    cp_async_commit();
-    for (int a = 0; a < nb; ++a) {
-        if (a + 1 < nb)
-            stage(load_tile(ring + (a + 1) % R2_RING), a + 1, (a + 1) & 1);
-        if (a + 3 < nb && tid < 4)
-            cp_async16(reinterpret_cast<int4 *>(ring + (a + 3) % R2_RING) + tid,
-                       reinterpret_cast<const int4 *>(tiles + (size_t)(a + 3) * rec_stride + tile) + tid);
-        cp_async_commit();
-        if (tid < R2_T * R2_T)
-            output_params<ORDER>(R, cur, geo + 6 * (size_t)a, oz0, ox0, oz0 + (tid >> 4), ox0 + (tid & 15),
-                                 prm + tid * PW);
-        cp_async_wait<1>();
-        if (TMA && cur.pad > 0) {
-            // every thread waits for the copy's bytes; a copy that does not
-            // complete within the limit is reported and ends the CTA (all
-            // threads together, after a second bounded wait by thread 0 so
-            // that no copy is left writing into shared memory)
+    // every thread waits for the TMA copy of footprint a; a copy that does
+    // not complete within the limit is reported and ends the CTA (all
+    // threads together, after a second bounded wait by thread 0 so that no
+    // copy is left writing into shared memory).  The vote is the barrier
+    // that orders angle a's footprint and records before their use.
+    auto footprint_barrier = [&](int a, bool tma_copy) -> bool {
+        if (TMA && tma_copy) {
             const bool done = mbar_wait(bar + (a & 1), (phase >> (a & 1)) & 1u, kCopyWaitNs);
             phase ^= 1u << (a & 1);
             if (__syncthreads_or(!done)) {
@@ -651,10 +646,57 @@ __global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const f
                     mbar_wait(bar + (a & 1), ((phase >> (a & 1)) & 1u) ^ 1u, kCopyWaitNs);
                 }
                 __syncthreads();
-                return;
+                return false;
             }
+        } else {
+            __syncthreads();
         }
-        __syncthreads();
+        return true;
+    };
+    auto prefetch_record = [&](int a) {  // tile record of angle a into the ring
+        if (a < nb && tid < 4)
+            cp_async16(reinterpret_cast<int4 *>(ring + a % R2_RING) + tid,
+                       reinterpret_cast<const int4 *>(tiles + (size_t)a * rec_stride + tile) + tid);
+    };
+    TileGeo cur = load_tile(ring);
+    stage(cur, 0, 0);
+    cp_async_commit();
+    if constexpr (C::DBL) {
+        if (tid < R2_T * R2_T)
+            output_params<ORDER>(R, cur, geo, oz0, ox0, oz0 + (tid >> 4), ox0 + (tid & 15), prm + tid * PW);
+    }
+    for (int a = 0; a < nb; ++a) {
+        const float *prm_a = prm + ((C::DBL && (a & 1)) ? PRMN : 0);
+        if constexpr (C::DBL) {
+            // one barrier per angle: footprint a (copied during angle a-1)
+            // and its records (computed during angle a-1) are complete, and
+            // every thread is done with angle a-1's footprint and record
+            // buffers, which angle a+1 takes now; threads 0..255 compute the
+            // records of angle a+1 while the others start interpolating
+            cp_async_wait<0>();
+            if (!footprint_barrier(a, cur.pad > 0))
+                return;
+            if (a + 1 < nb) {
+                const TileGeo nxt = load_tile(ring + (a + 1) % R2_RING);
+                stage(nxt, a + 1, (a + 1) & 1);
+                prefetch_record(a + 3);
+                cp_async_commit();
+                if (tid < R2_T * R2_T)
+                    output_params<ORDER>(R, nxt, geo + 6 * (size_t)(a + 1), oz0, ox0, oz0 + (tid >> 4),
+                                         ox0 + (tid & 15), prm + ((a + 1) & 1) * PRMN + tid * PW);
+            }
+        } else {
+            if (a + 1 < nb)
+                stage(load_tile(ring + (a + 1) % R2_RING), a + 1, (a + 1) & 1);
+            prefetch_record(a + 3);
+            cp_async_commit();
+            if (tid < R2_T * R2_T)
+                output_params<ORDER>(R, cur, geo + 6 * (size_t)a, oz0, ox0, oz0 + (tid >> 4), ox0 + (tid & 15),
+                                     prm + tid * PW);
+            cp_async_wait<1>();
+            if (!footprint_barrier(a, cur.pad > 0))
+                return;
+        }
         if (cur.box_zn > 0) {
             const float2 *b = box + (a & 1) * R2_BOXE + yl;
             const int rowstride = cur.box_xn * R2_Y;
@@ -665,7 +707,7 @@ __global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const f
                 // it adds zero, and the loop over q stays straight-line code
                 // whose loads the compiler can issue ahead (measured: 13.52
                 // -> 13.28 ms for the 256^3 resampling)
-                const float *rec = prm + ((hz0 + q) * R2_T + hx) * PW;
+                const float *rec = prm_a + ((hz0 + q) * R2_T + hx) * PW;
                 const float4 h = *reinterpret_cast<const float4 *>(rec);
                 float2 w[2 * (ORDER + 1)];
 #pragma unroll
@@ -700,7 +742,8 @@ __global__ void __launch_bounds__(R2_THREADS, 1) k_rotate_y(RotParams R, const f
                 part[q] = make_float2(0.f, 0.f);
             }
         }
-        __syncthreads();
+        if constexpr (!C::DBL)
+            __syncthreads();  // footprint and record buffers free for angle a+2 / a+1
         if (a + 1 < nb)
             cur = load_tile(ring + (a + 1) % R2_RING);
     }
@@ -904,7 +947,10 @@ __global__ void __launch_bounds__(256, ORDER >= 4 ? 2 : 4) k_rotate_3d(RotParams
     const bool full = x0 + R3_X <= nx && y0 + R3_Y <= ny && z0 + R3_Z <= nz;
     const int n3[3] = {nx, ny, nz};
     const size_t aslab = (size_t)nz * nx * yp;
-    const size_t zstride = (size_t)nx * yp;
+    // element offsets within one angle's slab fit 32 bits (plan creation
+    // refuses slabs of 2^31 or more elements), so the tap addresses are
+    // 32-bit offsets from the angle's slab pointer
+    const int zstride = nx * yp;
     // frame offsets of this thread's outputs from the tile origin
     const float d0 = (float)w, d1 = (float)(-lane);
     const double o0 = (double)x, o1 = (double)(ny - 1 - y);
@@ -982,12 +1028,12 @@ __global__ void __launch_bounds__(256, ORDER >= 4 ? 2 : 4) k_rotate_3d(RotParams
                 }
                 float2 acc = part[q];
                 if (interior) {
-                    const float2 *base = sa + ((size_t)t0[2] * nx + t0[0]) * yp + (ny - 1 - t0[1]);
+                    const int off = (t0[2] * nx + t0[0]) * yp + (ny - 1 - t0[1]);
 #pragma unroll
                     for (int k2 = 0; k2 <= ORDER; ++k2) {
 #pragma unroll
                         for (int k0 = 0; k0 <= ORDER; ++k0) {
-                            const float2 *col = base + k2 * zstride + (size_t)k0 * yp;
+                            const float2 *col = sa + (off + k2 * zstride + k0 * yp);
                             float2 r = make_float2(0.f, 0.f);
 #pragma unroll
                             for (int k1 = 0; k1 <= ORDER; ++k1)
@@ -1008,11 +1054,11 @@ __global__ void __launch_bounds__(256, ORDER >= 4 ? 2 : 4) k_rotate_3d(RotParams
                     for (int k2 = 0; k2 <= ORDER; ++k2) {
 #pragma unroll
                         for (int k0 = 0; k0 <= ORDER; ++k0) {
-                            const float2 *col = sa + ((size_t)iz[k2] * nx + ix[k0]) * yp;
+                            const int col = (iz[k2] * nx + ix[k0]) * yp;
                             float2 r = make_float2(0.f, 0.f);
 #pragma unroll
                             for (int k1 = 0; k1 <= ORDER; ++k1)
-                                r = ffma2(make_float2(wt[1][k1], wt[1][k1]), __ldg(col + iy[k1]), r);
+                                r = ffma2(make_float2(wt[1][k1], wt[1][k1]), __ldg(sa + (col + iy[k1])), r);
                             const float w02 = wt[2][k2] * wt[0][k0];
                             acc = ffma2(make_float2(w02, w02), r, acc);
                         }

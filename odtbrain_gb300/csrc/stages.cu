@@ -38,6 +38,26 @@ namespace odt {
 // 24.1 ms with both).
 constexpr bool kColumnStepRegs = true;
 constexpr bool kColumnTw2 = true;
+// Planes between exact propagator anchors within a column CTA's run.
+constexpr int kReanchorPlanes = 32;
+// The half-crop column kernel's shared memory (smem_cols_half) has one
+// [n][KX] region, which holds the filtered spectrum because the steps are
+// in registers.
+static_assert(kColumnStepRegs, "smem_cols_half assumes register-held propagator steps");
+// Column CTAs that run through up to 256 planes of an angle, re-anchoring
+// the propagator every kReanchorPlanes planes: the half-crop kernel with
+// 4 columns of 64-thread lines (the 512-point planes).  256^3 workload,
+// cap on the planes per CTA against the column stage: 32 planes 24.1 ms,
+// 64 22.8, 128 22.4, 256 22.2 ms.  The other column kernels keep runs of
+// at most kReanchorPlanes planes (one exact anchor each): the 512-thread
+// CTAs of 256-point columns lost 30 % with longer runs (one wave of long
+// CTAs), and the generic kernel's extra shared memory for the re-anchoring
+// cost more than the longer runs saved.
+template <class L, int KX, bool HALF>
+constexpr bool long_runs()
+{
+    return HALF && kColumnStepRegs && KX * L::TPL <= 256;
+}
 
 // ---------------------------------------------------------------------------
 // (a) rows: pad + weight + forward FFT along x.
@@ -250,6 +270,11 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
     float2 *buf0 = smem, *buf1 = smem + KX * ls, *tw = smem + 2 * KX * ls;
     float2 *edge = tw + (TW2 ? tw_slots2(n) : tw_slots(n)); // [KX][EDGE_SLOTS]
     float2 *stp = edge + EDGE_SLOTS * KX;  // [n][KX] propagator step per element
+    // long runs: [n][KX] the filtered spectrum G X of the current angle,
+    // for the exact re-anchoring every kReanchorPlanes planes (in the step
+    // region: the steps live in registers)
+    constexpr bool REANCHOR = long_runs<L, KX, HALF>();
+    float2 *gx = stp;
     if constexpr (TW2)
         copy_twiddles2<L>(tw, P.tab.twy, n);
     else
@@ -271,27 +296,43 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
     float2 V[L::SLOTS];  // G * exp(i w z_p) for this thread's elements
     int flip = 0;
     int cur_a = -1;
+    int since = 0;  // planes advanced by the recurrence since the last exact anchor
     int a = qb / nz, p = qb % nz;
     for (int q = qb; q < qe; ++q, ++p) {
         if (p == nz) {
             p = 0;
             ++a;
         }
-        if (a != cur_a) {
-            column_spectrum<L, KX>(P, line, rowspec, a, kx, colok, c, j, buf0, buf1, tw, flip, V);
+        if (a != cur_a || (REANCHOR && since == kReanchorPlanes)) {
+            // exact anchor at the first plane of an angle, and again every
+            // kReanchorPlanes planes: the FP32 recurrence drifts by about one
+            // rounding per plane (measured on the 256^3 workload: rel-L2 to
+            // the FP64 oracle 3.5e-7 with anchors every 32 planes, 1.6e-6
+            // with one anchor per 256-plane run)
+            const bool fresh = a != cur_a;
+            if (fresh)
+                column_spectrum<L, KX>(P, line, rowspec, a, kx, colok, c, j, buf0, buf1, tw, flip, V);
             const float zp = (float)p - 0.5f * (float)nz + P.zshift;
 #pragma unroll
             for (int r = 0; r < L::SLOTS; ++r) {
                 const int ky = j + r * L::TPL;
                 if (colok && ky < n) {
                     const size_t k = (size_t)ky * lNx + kx;
+                    if (fresh) {
+                        if (REANCHOR)
+                            gx[ky * KX + c] = V[r];  // read back only by this thread
+                        if (!STEP_REGS)
+                            stp[ky * KX + c] = P.tab.step[k];
+                    } else if (REANCHOR) {
+                        V[r] = gx[ky * KX + c];
+                    }
                     V[r] = cmul(V[r], expi_phase(P.tab.wsplit[k], zp));
-                    if (!STEP_REGS)
-                        stp[ky * KX + c] = P.tab.step[k];
                 }
             }
             cur_a = a;
+            since = 0;
         }
+        ++since;
         float2 v[L::SLOTS];
 #pragma unroll
         for (int r = 0; r < L::SLOTS; ++r) {
@@ -770,9 +811,10 @@ __global__ void __launch_bounds__(256) k_columns_boundary_line(StageParams P, co
 // Planes per column-stage CTA: enough CTAs for one full wave of the
 // resident slots over the active column groups (the forward column FFT of a
 // CTA is amortised over its planes, so fewer, longer CTAs are better as long
-// as every slot is busy), within [4, 32].
+// as every slot is busy), at least 4 and at most 256 for long runs
+// (long_runs), else at most kReanchorPlanes.
 template <int KX>
-static int planes_per_cta(const StageParams &P, int qn)
+static int planes_per_cta(const StageParams &P, int qn, bool long_run)
 {
     const int groups = (P.lNx + KX - 1) / KX;
     int active = 0;
@@ -781,7 +823,7 @@ static int planes_per_cta(const StageParams &P, int qn)
             ++active;
     const int per = P.col_slots > 0 ? std::max(1, P.col_slots / std::max(1, active)) : 4;
     const int ppc = (qn + per - 1) / per;
-    return std::min(32, std::max(4, ppc));
+    return std::min(long_run ? 256 : kReanchorPlanes, std::max(4, ppc));
 }
 
 // Calls fn(std::integral_constant<int, V>) for V = v (one of 0, 1, 2), so a
@@ -853,7 +895,10 @@ static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rows
                                 cudaStream_t s)
 {
     constexpr int KX = Cfg<L>::KX;
-    const int ppc = planes_per_cta<KX>(P, qn);
+    bool half = false;
+    if constexpr (half_line<L>())
+        half = half_crop(P);
+    const int ppc = planes_per_cta<KX>(P, qn, half && long_runs<L, KX, true>());
     dim3 grid((P.lNx + KX - 1) / KX, (qn + ppc - 1) / ppc);
     return with_poles(column_poles(P), [&](auto yf) {
         constexpr int YF = decltype(yf)::value;

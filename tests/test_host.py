@@ -338,6 +338,31 @@ def test_forced_allocation_failure_raises_memory_error(native_lib):
         _native.set_table_alloc_limit(0)
 
 
+def test_slab_size_limit(native_lib):
+    """One angle's coefficient slab is addressed with 32-bit element
+    offsets: a plan whose slab would hold 2^31 elements or more is refused
+    as unsupported before any device call."""
+    keep = []
+    d = _small_desc(keep)
+    d.ny, d.nx = 1024, 2048          # 2048 * 2048 * 1024 = 2^32 elements
+    d.pad_ny, d.pad_nx = 2048, 4096
+    d.pad_y_left, d.pad_x_left = 512, 1024
+    h = ctypes.c_void_p()
+    st = native_lib.odt_bpp3d_plan_create(ctypes.byref(d), ctypes.byref(h))
+    assert st == _native.ODT_ERR_UNSUPPORTED and not h.value
+    assert b"2^31" in native_lib.odt_last_error()
+
+
+def test_mlp_kernel_selection_argument_check(native_lib):
+    """odt_mlp_select_kernels takes 0 (warp-level mma.sync) or 1 (tcgen05)
+    and refuses anything else without touching a device."""
+    assert native_lib.odt_mlp_select_kernels(2) == _native.ODT_ERR_INVALID_ARGUMENT
+    assert b"tensor_memory" in native_lib.odt_last_error()
+    assert native_lib.odt_mlp_select_kernels(-1) == _native.ODT_ERR_INVALID_ARGUMENT
+    assert native_lib.odt_mlp_select_kernels(0) == 0
+    assert native_lib.odt_mlp_select_kernels(1) == 0
+
+
 def test_status_codes_map_to_python_exceptions(native_lib):
     """Each non-OK status becomes the exception the reference's callers
     expect (ValueError / NotImplementedError / MemoryError) or OdtError."""
