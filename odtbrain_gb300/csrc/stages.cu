@@ -45,8 +45,9 @@ constexpr int kReanchorPlanes = 32;
 // in registers.
 static_assert(kColumnStepRegs, "smem_cols_half assumes register-held propagator steps");
 // Column CTAs that run through up to 256 planes of an angle, re-anchoring
-// the propagator every kReanchorPlanes planes: the half-crop kernel with
-// 4 columns of 64-thread lines (the 512-point planes).  256^3 workload,
+// the propagator every kReanchorPlanes planes: power-of-two columns of
+// 64-thread lines with the steps in registers (4 columns per CTA, the
+// 512-point planes).  256^3 workload,
 // cap on the planes per CTA against the column stage: 32 planes 24.1 ms,
 // 64 22.8, 128 22.4, 256 22.2 ms.  The other column kernels keep runs of
 // at most kReanchorPlanes planes (one exact anchor each): the 512-thread
@@ -56,7 +57,17 @@ static_assert(kColumnStepRegs, "smem_cols_half assumes register-held propagator 
 template <class L, int KX, bool HALF>
 constexpr bool long_runs()
 {
-    return HALF && kColumnStepRegs && KX * L::TPL <= 256;
+    return pow2_len<L>() > 0 && kColumnStepRegs && KX * L::TPL <= 256;
+}
+// Column kernels that hold the propagator steps in registers and read the
+// third pass's twiddles from the 64x7 table (N >= 512): the half-crop
+// kernel, and for other crops power-of-two columns in CTAs of at most 256
+// threads (with more threads per CTA, 64 registers per thread, the steps
+// spill).
+template <class L, int KX, bool HALF>
+constexpr bool column_regs()
+{
+    return kColumnStepRegs && (HALF || (pow2_len<L>() > 0 && KX * L::TPL <= 256));
 }
 
 // ---------------------------------------------------------------------------
@@ -259,11 +270,12 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
 {
     if (!group_active<KX>(P, blockIdx.x * KX))
         return;  // all-zero columns: the row stage never reads them
-    // half-crop plans: the per-element propagator step lives in registers
-    // and (N >= 512) the third radix-8 pass reads per-thread-class twiddles
-    // (for other crops both measured slower: tilted 200^3, 37.5 -> 38.1 ms)
-    constexpr bool STEP_REGS = HALF && kColumnStepRegs;
-    constexpr bool TW2 = HALF && kColumnTw2 && pow2_len<L>() >= 512;
+    // power-of-two columns: the per-element propagator step lives in
+    // registers and (N >= 512) the third radix-8 pass reads
+    // per-thread-class twiddles (with long runs, tilted 200^3 step 72.1 ->
+    // 70.6 ms; same box)
+    constexpr bool STEP_REGS = column_regs<L, KX, HALF>();
+    constexpr bool TW2 = STEP_REGS && kColumnTw2 && pow2_len<L>() >= 512;
     extern __shared__ float2 smem[];
     const int n = line.size();  // lNy
     const int ls = xslots<true>(n);
@@ -288,8 +300,8 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
     float2 St[L::SLOTS];  // STEP_REGS: exp(i w) of this thread's elements
     if constexpr (STEP_REGS) {
 #pragma unroll
-        for (int r = 0; r < L::SLOTS; ++r)
-            St[r] = P.tab.step[(size_t)(j + r * L::TPL) * lNx + kx];
+        for (int r = 0; r < L::SLOTS; ++r)  // (columns beyond lNx: never stored)
+            St[r] = colok ? P.tab.step[(size_t)(j + r * L::TPL) * lNx + kx] : make_float2(1.f, 0.f);
     }
     __syncthreads();
 
@@ -826,6 +838,15 @@ static int planes_per_cta(const StageParams &P, int qn, bool long_run)
     return std::min(long_run ? 256 : kReanchorPlanes, std::max(4, ppc));
 }
 
+// Shared memory of the generic-crop column kernel: power-of-two columns of
+// 512 or more carry the third-pass twiddle table and the filtered-spectrum
+// region as the half-crop kernel does.
+template <class L>
+static size_t smem_cols_prop(int n)
+{
+    return (column_regs<L, Cfg<L>::KX, false>() && pow2_len<L>() >= 512) ? smem_cols_half<L>(n) : smem_cols<L>(n);
+}
+
 // Calls fn(std::integral_constant<int, V>) for V = v (one of 0, 1, 2), so a
 // pole count chosen at run time selects a compile-time instantiation.
 template <class F>
@@ -898,7 +919,7 @@ static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rows
     bool half = false;
     if constexpr (half_line<L>())
         half = half_crop(P);
-    const int ppc = planes_per_cta<KX>(P, qn, half && long_runs<L, KX, true>());
+    const int ppc = planes_per_cta<KX>(P, qn, half ? long_runs<L, KX, true>() : long_runs<L, KX, false>());
     dim3 grid((P.lNx + KX - 1) / KX, (qn + ppc - 1) / ppc);
     return with_poles(column_poles(P), [&](auto yf) {
         constexpr int YF = decltype(yf)::value;
@@ -910,7 +931,7 @@ static cudaError_t columns_impl(const StageParams &P, L line, const float2 *rows
             }
         }
         k_columns_propagate<L, KX, false, YF>
-            <<<grid, KX * L::TPL, smem_cols<L>(line.n), s>>>(P, line, rowspec, T, q0, qn, ppc);
+            <<<grid, KX * L::TPL, smem_cols_prop<L>(line.n), s>>>(P, line, rowspec, T, q0, qn, ppc);
         return cudaGetLastError();
     });
 }
@@ -977,7 +998,7 @@ static cudaError_t set_smem_attrs_np(int n)
     if (e != cudaSuccess)
         return e;
     return cudaFuncSetAttribute(k_columns_propagate<L, Cfg<L>::KX, false, NP>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols<L>(n));
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cols_prop<L>(n));
 }
 
 template <class L>
@@ -1008,7 +1029,7 @@ int columns_slots(const StageParams &P)
         using L = decltype(line);
         constexpr int KX = Cfg<L>::KX;
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_columns_propagate<L, KX, false, 0>,
-                                                             KX * L::TPL, smem_cols<L>(line.n));
+                                                             KX * L::TPL, smem_cols_prop<L>(line.n));
     });
     return e == cudaSuccess ? per * sms : 0;
 }
