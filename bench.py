@@ -722,7 +722,12 @@ def public_e2e(w, host, angles, U, args, world, dev, barrier):
         api = odt.backpropagate_3d_tilted
         kw["tilted_axis"] = w["axis"]
     host_np = host.numpy()
-    out = api(host_np, angles, w["res"], w["nm"], **kw)
+    # the same warm-up as the device timing: the returned volumes live in
+    # pinned host blocks of torch's caching allocator, and the first calls
+    # allocate the blocks the later ones reuse (a result is still alive
+    # while the next call runs)
+    for _ in range(max(args.warmup, 3)):
+        out = api(host_np, angles, w["res"], w["nm"], **kw)
     e2e_t = []
     barrier()
     for _ in range(e2e_steps):
