@@ -96,7 +96,11 @@ typedef struct odt_bpp3d_desc {
 typedef struct odt_bpp3d_plan odt_bpp3d_plan;
 
 /* Build a plan (device tables for the filter, the propagator and the FFT
- * twiddles).  Replaces the per-call setup of _alg3d_bpp.py:237-487. */
+ * twiddles).  Replaces the per-call setup of _alg3d_bpp.py:237-487.
+ * ODT_ERR_UNSUPPORTED for FFT lengths other than powers of two in
+ * [64, 4096] or lengths <= 1024, for spline orders 4 and 5 on lines of
+ * fewer than 4 samples, and when one angle's coefficient slab
+ * (nx * nx * ny rounded up to 32) would hold 2^31 elements or more. */
 odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc,
                                  odt_bpp3d_plan **plan);
 
