@@ -213,7 +213,7 @@ struct odt_bpp3d_plan {
     int batch;       // angles per batch
     int jobs;        // (angle, plane) jobs per column/row launch
     size_t off_rowspec, off_T, off_T2, off_Tab, off_slab, off_comp, off_rot, ws_bytes;
-    size_t off_Qg, off_W, off_Pg, adj_ws_bytes;  // adjoint-only regions after ws_bytes
+    size_t off_Qg, off_W, off_Pg, off_vT, adj_ws_bytes;  // adjoint-only regions after ws_bytes
     double bx_ca, bx_cb, by_ca, by_cb;  // one-pole solve in the adjoint's form
     int npoles;                         // prefilter poles: 0, 1 or 2
     float kx_solve[16], ky_solve[16];   // boundary_matrix of x and y lines
@@ -616,6 +616,8 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
         p->off_Qg = w; w = align_up(w + spec_b);
         p->off_W = w; w = align_up(w + spec_b);
         p->off_Pg = w; w = align_up(w + spec_b);
+        // the volume gradient in the [z][x][y] order (y-axis adjoint)
+        p->off_vT = w; w = align_up(w + (size_t)nz * d.ny * d.nx * 8);
         p->adj_ws_bytes = w;
     }
 
@@ -905,6 +907,14 @@ odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const
     const size_t spec = (size_t)d.pad_ny * d.pad_nx;
     const int nbatches = (d.num_angles + plan->batch - 1) / plan->batch;
     cudaError_t e;
+    const float2 *vg = (const float2 *)vol_grad;
+    if (!tilted) {
+        float2 *vT = (float2 *)(ws + plan->off_vT);
+        e = odt::launch_volume_zxy(vg, vT, plan->nz, d.ny, d.nx, s);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "volume transpose launch");
+        vg = vT;
+    }
     if (gain_grad) {
         e = cudaMemsetAsync(gain_grad, 0, spec * sizeof(float), s);
         if (e != cudaSuccess)
@@ -924,7 +934,7 @@ odt_status odt_bpp3d_adjoint(const odt_bpp3d_plan *plan, const void *sino, const
         R.last_pass = 1;
         R.onlyreal = 0;
         R.status = plan->d_status;
-        e = odt::launch_rotate_adjoint(R, d.intp_order, tilted ? 1 : 0, (const float2 *)vol_grad,
+        e = odt::launch_rotate_adjoint(R, d.intp_order, tilted ? 1 : 0, vg,
                                        geometry + (size_t)a0 * geo_stride, slab, ws + plan->off_rot, s);
         if (e != cudaSuccess)
             return cuda_fail(e, "rotate_adjoint launch");

@@ -123,9 +123,14 @@ cudaError_t configure_rotate_kernels();
 // Adjoint (adjoint.cu, rotate.cu).
 cudaError_t configure_adjoint_kernels(const StageParams &P);
 // Scratch: rotate_scratch_bytes(batch, ...) (one 64-byte record per angle and
-// 16 x 16 tile, like the forward).
+// 16 x 16 tile, like the forward).  vol_grad: the volume gradient in the
+// [z][x][y] order (launch_volume_zxy) for the y axis, [z][y][x] for the
+// tilted geometry.
 cudaError_t launch_rotate_adjoint(const RotParams &R, int order, int tilted, const float2 *vol_grad,
                                   const double *geo, float2 *slab_grad, void *scratch, cudaStream_t s);
+// The volume gradient [z][y][x] in the [z][x][y] order that the y-axis
+// resampling transpose reads (y innermost, one contiguous run per output).
+cudaError_t launch_volume_zxy(const float2 *vol, float2 *vol_zxy, int nz, int ny, int nx, cudaStream_t s);
 cudaError_t configure_rotate_adjoint_kernels();
 cudaError_t launch_adj_rows(const StageParams &P, const float2 *sgrad, float2 *Tg, int q0, int qn, cudaStream_t s);
 cudaError_t launch_adj_columns(const StageParams &P, const float2 *Tg, float2 *Qg, int q0, int qn, cudaStream_t s);

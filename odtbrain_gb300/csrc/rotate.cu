@@ -1319,14 +1319,18 @@ __global__ void k_rotate_y_adj_setup(RotParams R, const double *__restrict__ geo
 }
 
 template <int ORDER>
-__global__ void __launch_bounds__(RA_THREADS, 1) k_rotate_y_adjoint(RotParams R, const float2 *__restrict__ vgrad,
+__global__ void __launch_bounds__(RA_THREADS, 2) k_rotate_y_adjoint(RotParams R, const float2 *__restrict__ vgrad,
                                                                     const double *__restrict__ geo,
                                                                     const AdjTileGeo *__restrict__ tiles,
                                                                     float2 *__restrict__ sgrad)
 {
     extern __shared__ float4 ra_smem[];
-    float2 *acc = reinterpret_cast<float2 *>(ra_smem);              // [16 z][16 x][RA_YP]
-    float4 *rec = reinterpret_cast<float4 *>(acc + RA_T * RA_T * RA_YP);  // [box][2]
+    // accumulators [16 z][16 x][RA_YP], real and imaginary parts in separate
+    // planes (the 16 lanes of an output add into 16 consecutive words, so the
+    // two outputs of a warp do not meet on the same even banks)
+    float *acc_re = reinterpret_cast<float *>(ra_smem);
+    float *acc_im = acc_re + RA_T * RA_T * RA_YP;
+    float4 *rec = reinterpret_cast<float4 *>(acc_im + RA_T * RA_T * RA_YP);  // [box][2]
     const int tid = threadIdx.x, hw = tid >> 4, yl = tid & 15;
     const int nx = R.nx, nz = R.nz, ny = R.ny;
     const int ntx = (nx + RA_T - 1) / RA_T, ntz = (nz + RA_T - 1) / RA_T;
@@ -1336,12 +1340,16 @@ __global__ void __launch_bounds__(RA_THREADS, 1) k_rotate_y_adjoint(RotParams R,
     const bool yok = y < ny;
     for (int a = 0; a < R.nbatch_angles; ++a) {
         const AdjTileGeo tg = tiles[(size_t)a * ntz * ntx + tile];
-        for (int i = tid; i < RA_T * RA_T * RA_YP; i += RA_THREADS)
-            acc[i] = make_float2(0.f, 0.f);
+        for (int i = tid; i < RA_T * RA_T * RA_YP; i += RA_THREADS) {
+            acc_re[i] = 0.f;
+            acc_im[i] = 0.f;
+        }
         const int nbox = tg.ozn * tg.oxn;
         const double *g = geo + 6 * (size_t)a;
-        // parameter records: (tz0, tx0, wz0, wz1) (wz2, wx0, wx1, wx2), or
-        // tz0 = INT_MIN when the output is outside or cannot reach the tile
+        // parameter records: (pz, px, wz0, wz1) (wz2, wx0, wx1, wx2), where
+        // byte i of pz (px) is the tile-relative position of z (x) tap i
+        // after mirroring, 0xFF for a tap outside the tile; pz = -1 when the
+        // output is outside the domain or none of its taps lands in the tile
         for (int o = tid; o < nbox; o += RA_THREADS) {
             const int dz = o / tg.oxn, dx = o - dz * tg.oxn;
             const int oz = tg.oz0 + dz, ox = tg.ox0 + dx;
@@ -1356,7 +1364,7 @@ __global__ void __launch_bounds__(RA_THREADS, 1) k_rotate_y_adjoint(RotParams R,
                 return __dadd_rn(__dadd_rn(__ldg(g + 5), __dmul_rn(__ldg(g + 2), (double)oz)),
                                  __dmul_rn(__ldg(g + 3), (double)ox));
             });
-            int tz0 = INT_MIN, tx0 = 0;
+            int pz = -1, px = -1;
             float wz[4] = {0.f, 0.f, 0.f, 0.f}, wx[4] = {0.f, 0.f, 0.f, 0.f};
             if (in) {
                 int sz, sx;
@@ -1381,11 +1389,23 @@ __global__ void __launch_bounds__(RA_THREADS, 1) k_rotate_y_adjoint(RotParams R,
                         wx[k] = w[k];
                 }
                 if (sz + ORDER >= tg.vz0 && sz <= tg.vz1 && sx + ORDER >= tg.vx0 && sx <= tg.vx1) {
-                    tz0 = sz;
-                    tx0 = sx;
+                    bool anyz = false, anyx = false;
+                    unsigned uz = 0xFFFFFFFFu, ux = 0xFFFFFFFFu;
+#pragma unroll
+                    for (int i = 0; i <= ORDER; ++i) {
+                        const int zz = mirror_idx(sz + i, nz) - cz0, xx = mirror_idx(sx + i, nx) - cx0;
+                        const bool zin = zz >= 0 && zz < RA_T, xin = xx >= 0 && xx < RA_T;
+                        const unsigned sh = 8u * (unsigned)i;
+                        uz = (uz & ~(0xFFu << sh)) | ((zin ? (unsigned)zz : 0xFFu) << sh);
+                        ux = (ux & ~(0xFFu << sh)) | ((xin ? (unsigned)xx : 0xFFu) << sh);
+                        anyz = anyz || zin;
+                        anyx = anyx || xin;
+                    }
+                    pz = (anyz && anyx) ? (int)uz : -1;
+                    px = (int)ux;
                 }
             }
-            rec[2 * o] = make_float4(__int_as_float(tz0), __int_as_float(tx0), wz[0], wz[1]);
+            rec[2 * o] = make_float4(__int_as_float(pz), __int_as_float(px), wz[0], wz[1]);
             rec[2 * o + 1] = make_float4(wz[2], wx[0], wx[1], wx[2]);
             if (ORDER == 3) {
                 // order 3 needs wz[3], wx[3]: the box holds at most
@@ -1399,11 +1419,11 @@ __global__ void __launch_bounds__(RA_THREADS, 1) k_rotate_y_adjoint(RotParams R,
         // push: half-warp hw takes outputs hw, hw + 32, ...
         for (int o = hw; o < nbox; o += RA_THREADS / 16) {
             const float4 r0 = rec[2 * o];
-            const int tz0 = __float_as_int(r0.x);
-            if (tz0 == INT_MIN)
+            const int pz = __float_as_int(r0.x);
+            if (pz == -1)
                 continue;
             const float4 r1 = rec[2 * o + 1];
-            const int tx0 = __float_as_int(r0.y);
+            const unsigned upz = (unsigned)pz, upx = (unsigned)__float_as_int(r0.y);
             float wz[4] = {r0.z, r0.w, r1.x, 0.f}, wx[4] = {r1.y, r1.z, r1.w, 0.f};
             if (ORDER == 3) {
                 const float2 w4 = reinterpret_cast<const float2 *>(rec + 2 * RA_OBOX * RA_OBOX)[o];
@@ -1412,21 +1432,23 @@ __global__ void __launch_bounds__(RA_THREADS, 1) k_rotate_y_adjoint(RotParams R,
             }
             const int dz = o / tg.oxn, dx = o - dz * tg.oxn;
             const int oz = tg.oz0 + dz, ox = tg.ox0 + dx;
-            const float2 gv = yok ? __ldg(vgrad + ((size_t)oz * ny + y) * nx + ox) : make_float2(0.f, 0.f);
+            // vgrad is the volume gradient in the [z][x][y] order: the 16
+            // lanes (consecutive y) of an output read one 128-byte run
+            const float2 gv = yok ? __ldg(vgrad + ((size_t)oz * nx + ox) * ny + y) : make_float2(0.f, 0.f);
 #pragma unroll
             for (int i = 0; i <= ORDER; ++i) {
-                const int zz = mirror_idx(tz0 + i, nz) - cz0;
-                if (zz < 0 || zz >= RA_T)
+                const int zz = (int)((upz >> (8 * i)) & 0xFFu);
+                if (zz == 0xFF)
                     continue;
 #pragma unroll
                 for (int k = 0; k <= ORDER; ++k) {
-                    const int xx = mirror_idx(tx0 + k, nx) - cx0;
-                    if (xx < 0 || xx >= RA_T)
+                    const int xx = (int)((upx >> (8 * k)) & 0xFFu);
+                    if (xx == 0xFF)
                         continue;
                     const float w = wz[i] * wx[k];
-                    float2 *dst = acc + (zz * RA_T + xx) * RA_YP + yl;
-                    atomicAdd(&dst->x, w * gv.x);
-                    atomicAdd(&dst->y, w * gv.y);
+                    const int idx = (zz * RA_T + xx) * RA_YP + yl;
+                    atomicAdd(acc_re + idx, w * gv.x);
+                    atomicAdd(acc_im + idx, w * gv.y);
                 }
             }
         }
@@ -1435,8 +1457,9 @@ __global__ void __launch_bounds__(RA_THREADS, 1) k_rotate_y_adjoint(RotParams R,
         for (int e = tid; e < RA_T * RA_T * RA_Y; e += RA_THREADS) {
             const int xx = e & 15, zz = (e >> 4) & 15, yy = e >> 8;
             const int z = cz0 + zz, x = cx0 + xx, yv = y0 + yy;
+            const int idx = (zz * RA_T + xx) * RA_YP + yy;
             if (z < nz && x < nx && yv < ny)
-                sgrad[(((size_t)a * ny + yv) * nz + z) * nx + x] = acc[(zz * RA_T + xx) * RA_YP + yy];
+                sgrad[(((size_t)a * ny + yv) * nz + z) * nx + x] = make_float2(acc_re[idx], acc_im[idx]);
         }
         __syncthreads();
     }
@@ -1608,6 +1631,34 @@ cudaError_t launch_rotate_adjoint(const RotParams &R, int order, int tilted, con
     default:
         return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+// [z][y][x] -> [z][x][y], 32 x 32 tiles of one z plane through shared
+// memory (coalesced reads along x, writes along y).
+__global__ void __launch_bounds__(256) k_volume_zxy(const float2 *__restrict__ src, float2 *__restrict__ dst, int ny,
+                                                    int nx)
+{
+    __shared__ float2 t[32][33];
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32, z = blockIdx.z;
+    const size_t plane = (size_t)z * ny * nx;
+    for (int i = threadIdx.y; i < 32; i += 8) {
+        const int y = y0 + i, x = x0 + threadIdx.x;
+        if (y < ny && x < nx)
+            t[i][threadIdx.x] = src[plane + (size_t)y * nx + x];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += 8) {
+        const int x = x0 + i, y = y0 + threadIdx.x;
+        if (x < nx && y < ny)
+            dst[plane + (size_t)x * ny + y] = t[threadIdx.x][i];
+    }
+}
+
+cudaError_t launch_volume_zxy(const float2 *vol, float2 *vol_zxy, int nz, int ny, int nx, cudaStream_t s)
+{
+    dim3 grid((nx + 31) / 32, (ny + 31) / 32, nz);
+    k_volume_zxy<<<grid, dim3(32, 8), 0, s>>>(vol, vol_zxy, ny, nx);
     return cudaGetLastError();
 }
 
