@@ -393,6 +393,44 @@ odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real,
                              size_t workspace_bytes, int32_t *iterations,
                              void *stream);
 
+/* One spatial constraint in place, replacing constraint_nn / constraint_sh
+ * (odtbrain/apple.py:56-72, :75-110) called on their own.  Uses n0, n1, n2
+ * (any 3D shape) and method (ODT_APPLE_NN or ODT_APPLE_SH) of the
+ * descriptor.
+ *   data      device, n0*n1*n2 values of real_bits (32 or 64) bits, or
+ *             interleaved (re, im) pairs when is_complex: the real part is
+ *             constrained, the imaginary part set to 0; arithmetic in the
+ *             data's own precision like the reference's NumPy code
+ *   mask      device bytes (nonzero = honour the voxel) or NULL
+ *   bg_shell  device bytes (nonzero = known background) or NULL
+ *   workspace odt_apple_constrain_workspace_size bytes, 256-byte aligned
+ * Synchronous for ODT_APPLE_SH (the histogram's counts come to the host),
+ * stream-ordered for ODT_APPLE_NN. */
+odt_status odt_apple_constrain_workspace_size(const odt_apple_desc *desc,
+                                              size_t *bytes);
+odt_status odt_apple_constrain(const odt_apple_desc *desc, int32_t real_bits,
+                               int32_t is_complex, void *data,
+                               const uint8_t *mask, const uint8_t *bg_shell,
+                               void *workspace, size_t workspace_bytes,
+                               void *stream);
+
+/* The Gaussian-blurred Fourier-amplitude envelope, replacing envelope_gauss
+ * (odtbrain/apple.py:289-350) called on its own.  Uses n0, n1, n2 (n0 ==
+ * n2), gauss_radius and gauss_weights of the descriptor.
+ *   ftdata    device, n0*n1*n2 complex values (interleaved pairs of
+ *             real_bits = 32 or 64 bits): the spectrum in FFT order
+ *   core      device bytes, bit 0 set inside the apple core
+ *   envelope  device, n0*n1*n2 values of real_bits bits (the type of the
+ *             reference's |ftdata|)
+ *   workspace odt_apple_envelope_workspace_size bytes, 256-byte aligned
+ * Synchronous (a count decides whether the nearest-neighbour fill runs). */
+odt_status odt_apple_envelope_workspace_size(const odt_apple_desc *desc,
+                                             size_t *bytes);
+odt_status odt_apple_envelope(const odt_apple_desc *desc, int32_t real_bits,
+                              const void *ftdata, const uint8_t *core,
+                              void *envelope, void *workspace,
+                              size_t workspace_bytes, void *stream);
+
 /* Wait for `stream`, then return ODT_ERR_DEVICE_CHECK if any kernel of this
  * plan recorded a failed internal check since the last call (the status word
  * is cleared). */

@@ -55,6 +55,10 @@ EXPORTED_SYMBOLS = (
     "odt_apple_correct",
     "odt_apple_flags",
     "odt_apple_flags_workspace_size",
+    "odt_apple_constrain_workspace_size",
+    "odt_apple_constrain",
+    "odt_apple_envelope_workspace_size",
+    "odt_apple_envelope",
     "odt_debug_inject_status",
     "odt_debug_set_table_alloc_limit",
     "odt_status_string",
@@ -224,6 +228,14 @@ def lib():
         L.odt_apple_flags_workspace_size.argtypes = [
             ad, ctypes.POINTER(ctypes.c_uint64)]
         i32 = ctypes.c_int32
+        L.odt_apple_constrain_workspace_size.argtypes = [
+            ad, ctypes.POINTER(ctypes.c_uint64)]
+        L.odt_apple_constrain.argtypes = [ad, i32, i32, vp, vp, vp, vp,
+                                          ctypes.c_uint64, vp]
+        L.odt_apple_envelope_workspace_size.argtypes = [
+            ad, ctypes.POINTER(ctypes.c_uint64)]
+        L.odt_apple_envelope.argtypes = [ad, i32, vp, vp, vp, vp,
+                                         ctypes.c_uint64, vp]
         L.odt_mlp_gain_forward.argtypes = [ctypes.POINTER(MlpParams), i32,
                                            i32, i32, vp, vp, i32, vp, vp]
         L.odt_mlp_read_status.argtypes = [vp]
@@ -248,6 +260,10 @@ def lib():
                      "odt_sino_read_status", "odt_apple_workspace_size",
                      "odt_apple_correct", "odt_apple_flags",
                      "odt_apple_flags_workspace_size",
+                     "odt_apple_constrain_workspace_size",
+                     "odt_apple_constrain",
+                     "odt_apple_envelope_workspace_size",
+                     "odt_apple_envelope",
                      "odt_debug_inject_status",
                      "odt_debug_set_table_alloc_limit"):
             getattr(L, name).restype = ctypes.c_int

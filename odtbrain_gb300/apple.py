@@ -7,7 +7,10 @@ pyFFTW plans, the constraints, the envelope suppression and the spectrum
 restore are fused into the FFT passes, and the stopping test is evaluated
 on the device in float32 like the reference's NumPy scalars.  The masks
 ``apple_core_3d``, ``spillover_region`` and ``ellipsoid_shell`` come from
-the same GPU kernel (``odt_apple_flags``).
+the same GPU kernel (``odt_apple_flags``).  ``constraint_nn``,
+``constraint_sh`` (apple.py:56-110) and ``envelope_gauss`` (:289-350)
+called on their own run on the GPU too (``odt_apple_constrain``,
+``odt_apple_envelope``), with the kernels ``correct`` uses.
 
 NumPy input gives NumPy output; torch tensors give CUDA tensors.  There is
 no CPU fallback.
@@ -95,6 +98,144 @@ def spillover_region(shape, shell=0):
 def ellipsoid_shell(shape, width=20):
     """Background ellipsoid shell (odtbrain/apple.py:281-286)."""
     return (_flags(shape, bg_shell_width=width) & 4).astype(bool)
+
+
+def _voxel_bytes(m, shape, dev):
+    """A boolean array (NumPy or torch, broadcast to `shape`) as device
+    bytes, 1 where it is nonzero."""
+    torch = _torch()
+    if _is_tensor(m):
+        return (m.to(dev) != 0).expand(shape).to(torch.uint8).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(
+        np.broadcast_to(np.asarray(m) != 0, shape), dtype=np.uint8)).to(dev)
+
+
+def _real_bits(dtype):
+    """32 or 64 for a float / complex NumPy or torch dtype, else None."""
+    torch = _torch()
+    if isinstance(dtype, torch.dtype):
+        return {torch.float32: 32, torch.complex64: 32, torch.float64: 64,
+                torch.complex128: 64}.get(dtype)
+    return {np.dtype(np.float32): 32, np.dtype(np.complex64): 32,
+            np.dtype(np.float64): 64,
+            np.dtype(np.complex128): 64}.get(np.dtype(dtype))
+
+
+def _constrain(data, mask, bg_shell, method):
+    """One constraint of apple.py:56-110 in place on the GPU
+    (``odt_apple_constrain``): NumPy arrays are copied to the device and
+    back, CUDA tensors are changed where they lie."""
+    torch = _torch()
+    shape = tuple(data.shape)
+    if len(shape) != 3:
+        raise ValueError("`data` must be a 3D array")
+    bits = _real_bits(data.dtype)
+    if bits is None:
+        raise TypeError("`data` must be float32, float64, complex64 or "
+                        "complex128, not {}".format(data.dtype))
+    is_t = _is_tensor(data)
+    dev = _device_for(data)
+    d = _native.AppleDesc()
+    d.n0, d.n1, d.n2 = (int(v) for v in shape)
+    d.method = method
+    L = _native.lib()
+    with torch.cuda.device(dev):
+        if is_t and data.is_cuda and data.is_contiguous():
+            t = data
+        elif is_t:
+            t = data.to(dev).contiguous()
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(data)).to(dev)
+        mk = _voxel_bytes(mask, shape, dev) if mask is not None else None
+        sh = _voxel_bytes(bg_shell, shape, dev) if bg_shell is not None \
+            else None
+        nb = ctypes.c_uint64()
+        _native.check(L.odt_apple_constrain_workspace_size(ctypes.byref(d),
+                                                           ctypes.byref(nb)))
+        ws = torch.empty(nb.value, dtype=torch.uint8, device=dev)
+        stream = torch.cuda.current_stream(dev)
+        _native.check(L.odt_apple_constrain(
+            ctypes.byref(d), bits, int(t.is_complex()),
+            ctypes.c_void_p(t.data_ptr()),
+            ctypes.c_void_p(mk.data_ptr() if mk is not None else 0),
+            ctypes.c_void_p(sh.data_ptr() if sh is not None else 0),
+            ctypes.c_void_p(ws.data_ptr()), nb.value,
+            ctypes.c_void_p(stream.cuda_stream)))
+        if t is data:
+            return
+        if is_t:
+            data.copy_(t)
+        else:
+            data[...] = _to_host(t)
+
+
+def constraint_nn(data, mask=None, bg_shell=None):
+    """Non-negativity constraint, in place (drop-in for
+    ``odtbrain.apple.constraint_nn``, odtbrain/apple.py:56-72): the
+    imaginary part set to 0; the real part set to 0 in ``bg_shell``,
+    outside the inscribed ellipsoid and where it is negative (where
+    ``mask`` is set, if given)."""
+    _constrain(data, mask, bg_shell, _native.ODT_APPLE_NN)
+
+
+def constraint_sh(data, mask=None, bg_shell=None):
+    """Symmetric-histogram background constraint, in place (drop-in for
+    ``odtbrain.apple.constraint_sh``, odtbrain/apple.py:75-110): the real
+    values outside the half-maximum band of the histogram over
+    [min, max] of the background region halved (where ``mask`` is set, if
+    given), ``bg_shell`` halved, the imaginary part set to 0.  Histogram
+    arithmetic in the data's precision like the reference's NumPy code."""
+    _constrain(data, mask, bg_shell, _native.ODT_APPLE_SH)
+
+
+def envelope_gauss(ftdata, core):
+    """Gaussian-filtered envelope of the Fourier amplitude without the
+    apple core (drop-in for ``odtbrain.apple.envelope_gauss``,
+    odtbrain/apple.py:289-350), on the GPU (``odt_apple_envelope``).
+
+    ``ftdata``: spectrum in FFT order, shape (N, M, N); ``core``: boolean
+    mask of the same shape.  The result has the real type of ``ftdata``
+    (float32 for complex64 / float32 input, float64 otherwise), NumPy for
+    NumPy input and a CUDA tensor for a tensor."""
+    torch = _torch()
+    shape = tuple(ftdata.shape)
+    if len(shape) != 3:
+        raise ValueError("`ftdata` must be a 3D array")
+    if shape[0] != shape[2]:
+        raise ValueError("`shape[0]` and `shape[2]` must be identical!")
+    is_t = _is_tensor(ftdata)
+    dev = _device_for(ftdata)
+    bits = _real_bits(ftdata.dtype) or 64
+    cdt = torch.complex64 if bits == 32 else torch.complex128
+    d = _native.AppleDesc()
+    d.n0, d.n1, d.n2 = (int(v) for v in shape)
+    w, r = _gauss_weights(shape)
+    d.gauss_radius = r
+    d.gauss_weights = w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    L = _native.lib()
+    with torch.cuda.device(dev):
+        if is_t:
+            t = ftdata.to(dev)
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(ftdata)).to(dev)
+        t = t.to(cdt).contiguous()
+        cb = _voxel_bytes(core, shape, dev)
+        out = torch.empty(shape, device=dev,
+                          dtype=torch.float32 if bits == 32
+                          else torch.float64)
+        nb = ctypes.c_uint64()
+        _native.check(L.odt_apple_envelope_workspace_size(ctypes.byref(d),
+                                                          ctypes.byref(nb)))
+        ws = torch.empty(nb.value, dtype=torch.uint8, device=dev)
+        stream = torch.cuda.current_stream(dev)
+        _native.check(L.odt_apple_envelope(
+            ctypes.byref(d), bits, ctypes.c_void_p(t.data_ptr()),
+            ctypes.c_void_p(cb.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+            ctypes.c_void_p(ws.data_ptr()), nb.value,
+            ctypes.c_void_p(stream.cuda_stream)))
+    if is_t:
+        return out
+    return _to_host(out)
 
 
 def count_to_half(array):

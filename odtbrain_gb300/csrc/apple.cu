@@ -32,6 +32,11 @@
 // scipy.ndimage.distance_transform_edt implements: k_edt_*), and scipy's
 // gaussian_filter (FP64 sums in its order, float32 after each axis,
 // k_env_gauss).
+//
+// The same kernels serve constraint_nn / constraint_sh and envelope_gauss
+// called on their own (odt_apple_constrain, odt_apple_envelope), for
+// float32 or float64 data: k_sh_minmax / k_sh_hist / k_constrain and the
+// envelope pipeline, templated on the data's type.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -91,35 +96,44 @@ __device__ __forceinline__ bool ran_out(const AP &P, int it)
     return s != 0 && s <= it;
 }
 
+// The real part after one spatial constraint (the imaginary part becomes 0):
+// method 0 constraint_nn (apple.py:56-72), 1 constraint_sh (apple.py:75-110)
+// with the thresholds fmin, fmax (over the spillover region and shell) and
+// lo, hi (the histogram's half-maximum bin centres).  Halving is exact.
+template <typename T>
+__device__ __forceinline__ T constrain_re(int method, bool has_mask, T re, uint8_t fl, T fmin, T fmax, T lo, T hi)
+{
+    if (method == 0) {
+        if (fl & F_SHELL)
+            re = T(0);
+        if (fl & F_SPOV)
+            re = T(0);
+        bool low = re < T(0);
+        if (has_mask)
+            low = low && (fl & F_MASK);
+        if (low)
+            re = T(0);
+    } else {
+        const bool below = re > fmin && re < lo;
+        const bool above = re > hi && re < fmax;
+        bool out = below || above;
+        if (has_mask)
+            out = out && (fl & F_MASK);
+        if (out)
+            re = re * T(0.5);
+        if (fl & F_SHELL)
+            re = re * T(0.5);
+    }
+    return re;
+}
+
 // Spatial constraint of the reference's loop on one voxel value.
 __device__ __forceinline__ float2 constrain(const AP &P, float2 d, uint8_t fl, float fmin, float fmax, float lo,
                                             float hi)
 {
     if (P.method == 2)  // neither constraint (apple.py:222-227 with another method)
         return d;
-    float re = d.x;
-    if (P.method == 0) {  // constraint_nn, apple.py:56-72
-        if (fl & F_SHELL)
-            re = 0.f;
-        if (fl & F_SPOV)
-            re = 0.f;
-        bool low = re < 0.f;
-        if (P.has_mask)
-            low = low && (fl & F_MASK);
-        if (low)
-            re = 0.f;
-    } else {  // constraint_sh, apple.py:75-110
-        const bool below = re > fmin && re < lo;
-        const bool above = re > hi && re < fmax;
-        bool out = below || above;
-        if (P.has_mask)
-            out = out && (fl & F_MASK);
-        if (out)
-            re = __fmul_rn(re, 0.5f);
-        if (fl & F_SHELL)
-            re = __fmul_rn(re, 0.5f);
-    }
-    return make_float2(re, 0.f);
+    return make_float2(constrain_re<float>(P.method, P.has_mask, d.x, fl, fmin, fmax, lo, hi), 0.f);
 }
 
 // ---- axis 2 (contiguous lines) --------------------------------------------
@@ -375,7 +389,7 @@ __global__ void k_apple_tables(int n0, int n1, int n2, double km, double shell_w
 }
 
 __global__ void k_apple_flags(int n0, int n1, int n2, double km, int use_shell, FlagTables T, const uint8_t *mask,
-                              uint8_t *flags)
+                              const uint8_t *shell, uint8_t *flags)
 {
     // grid (ceil(n2/32), ceil(n1/8), n0), blocks of 32 x 8
     const double twopi = 6.283185307179586;
@@ -396,6 +410,8 @@ __global__ void k_apple_flags(int n0, int n1, int n2, double km, int use_shell, 
             f |= F_SPOV;
         if (use_shell && outer != (__dadd_rn(__dadd_rn(T.ei[0][i0], T.ei[1][i1]), T.ei[2][i2]) > 1.0))
             f |= F_SHELL;
+        if (shell && shell[v])
+            f |= F_SHELL;
         if (mask && mask[v])
             f |= F_MASK;
         flags[v] = f;
@@ -403,13 +419,15 @@ __global__ void k_apple_flags(int n0, int n1, int n2, double km, int use_shell, 
 }
 
 // Tables in a scratch block of flag_table_bytes() bytes; then the flags.
+// `shell` (device bytes, nonzero = background shell, or NULL) adds a shell
+// given voxel by voxel to the computed one.
 size_t flag_table_bytes(int n0, int n1, int n2)
 {
     return (size_t)(3 * (n0 + n1 + n2) + n1 + (long long)n0 * n2 + 8) * 8;
 }
 
 cudaError_t compute_flags(int n0, int n1, int n2, double km, int use_shell, double shell_width, const uint8_t *mask,
-                          uint8_t *flags, double *tab, cudaStream_t s)
+                          const uint8_t *shell, uint8_t *flags, double *tab, cudaStream_t s)
 {
     FlagTables T;
     double *p = tab;
@@ -430,7 +448,7 @@ cudaError_t compute_flags(int n0, int n1, int n2, double km, int use_shell, doub
     const unsigned tg = (unsigned)std::max<long long>((mx + 255) / 256, std::min<long long>((q + 255) / 256, 1024));
     k_apple_tables<<<tg, 256, 0, s>>>(n0, n1, n2, km, shell_width, T);
     const dim3 fg((unsigned)((n2 + 31) / 32), (unsigned)((n1 + 7) / 8), (unsigned)n0), fb(32, 8);
-    k_apple_flags<<<fg, fb, 0, s>>>(n0, n1, n2, km, use_shell, T, mask, flags);
+    k_apple_flags<<<fg, fb, 0, s>>>(n0, n1, n2, km, use_shell, T, mask, shell, flags);
     return cudaGetLastError();
 }
 
@@ -442,9 +460,15 @@ struct EnvGeom {
 
 __device__ __forceinline__ int wrapi(int i, int n) { return ((i % n) + n) % n; }
 
+__device__ __forceinline__ double magnitude(float2 o) { return (double)hypotf(o.x, o.y); }
+__device__ __forceinline__ double magnitude(double2 o) { return hypot(o.x, o.y); }
+
 // hull_pad = fftshift(|orig|, core -> NaN) inside the slice, 0 outside;
-// cpad = fftshift(core) inside the slice
-__global__ void k_env_pad(EnvGeom G, const float2 *orig, const uint8_t *flags, double *hp, uint8_t *cpad)
+// cpad = fftshift(core) inside the slice.  C2 = float2 (complex64 spectrum,
+// float32 hull) or double2 (complex128, float64 hull); the core is bit 0 of
+// flags[v].
+template <typename C2>
+__global__ void k_env_pad(EnvGeom G, const C2 *orig, const uint8_t *flags, double *hp, uint8_t *cpad)
 {
     // grid (ceil(msh/32), ceil(msh/8), msh), blocks of 32 x 8
     {
@@ -464,8 +488,7 @@ __global__ void k_env_pad(EnvGeom G, const float2 *orig, const uint8_t *flags, d
                 h = __longlong_as_double(0x7ff8000000000000ll);
                 cp = 1;
             } else {
-                const float2 o = orig[v];
-                h = (double)hypotf(o.x, o.y);
+                h = magnitude(orig[v]);
             }
         }
         hp[p] = h;
@@ -601,7 +624,7 @@ __global__ void k_edt_gather(long long M, const int *ft, const double *in, doubl
 
 // scipy.ndimage.gaussian_filter (mode constant 0): per axis in order 0, 1,
 // 2, acc = x[i] w0 + sum_{j = r..1} (x[i+j] + x[i-j]) w_j in FP64, rounded
-// to float32 after each axis.  Axis 0 reads the padded cube's slice (the
+// to the hull's type T (float32 or float64) after each axis.  Axis 0 reads the padded cube's slice (the
 // fftshifted hull); the last axis writes ifftshift(result) (the envelope in
 // FFT order).  A 32 x 8 block stages its inputs as doubles in shared memory
 // (one conversion per input): for axes 0 and 1 the block covers 32 x2
@@ -609,7 +632,8 @@ __global__ void k_edt_gather(long long M, const int *ft, const double *in, doubl
 // 32 consecutive x2 positions (the filtered axis) and 8 x1 rows.
 constexpr int GAUSS_RMAX = 64;  // radius limit (sigma <= 15.9, volumes <= 1590)
 
-__global__ void __launch_bounds__(256) k_env_gauss(EnvGeom G, int axis, const double *hp, const float *in, float *out,
+template <typename T>
+__global__ void __launch_bounds__(256) k_env_gauss(EnvGeom G, int axis, const double *hp, const T *in, T *out,
                                                    const double *w, int r)
 {
     extern __shared__ double gx[];  // the staged inputs with halo
@@ -620,7 +644,7 @@ __global__ void __launch_bounds__(256) k_env_gauss(EnvGeom G, int axis, const do
         if (a0 < 0 || a0 >= G.n0 || a1 < 0 || a1 >= G.n1 || a2 < 0 || a2 >= G.n2)
             return 0.0;
         if (axis == 0)
-            return (double)(float)hp[((long long)(a0 + G.off0) * G.msh + (a1 + G.off1)) * G.msh + (a2 + G.off2)];
+            return (double)(T)hp[((long long)(a0 + G.off0) * G.msh + (a1 + G.off1)) * G.msh + (a2 + G.off2)];
         return (double)in[((long long)a0 * G.n1 + a1) * G.n2 + a2];
     };
     double acc;
@@ -671,38 +695,167 @@ __global__ void __launch_bounds__(256) k_env_gauss(EnvGeom G, int axis, const do
                   s2 = wrapi(ii[2] - G.n2 / 2, G.n2);
         o = ((long long)s0 * G.n1 + s1) * G.n2 + s2;
     }
-    out[o] = (float)acc;
+    out[o] = (T)acc;
+}
+
+// envelope_gauss (apple.py:289-350) of the spectrum `orig` (n0 == n2; C2 =
+// float2 for complex64, double2 for complex128) with the core in bit 0 of
+// flags, written to `out` (type T of the hull: float or double) in FFT
+// order.  Scratch: hp0, hp1 (msh^3 doubles, msh = max(n0, n1)), cpad (msh^3
+// bytes), ft (msh^3 ints), scratch (2 msh^3 ints), g0, g1 (n0 n1 n2 values
+// of T), the Gaussian's 2 gr + 1 weights on the device and a NaN counter
+// that is 0.  Synchronous: the NaN count decides whether the feature
+// transform runs.
+struct EnvWork {
+    double *hp0, *hp1;
+    uint8_t *cpad;
+    int *ft, *scratch;
+    void *g0, *g1;
+    const double *gw;
+    unsigned int *nan_count;
+};
+
+template <typename C2, typename T>
+cudaError_t run_envelope(int n0, int n1, int n2, int gr, const C2 *orig, const uint8_t *flags, T *out,
+                         const EnvWork &W, cudaStream_t s)
+{
+    cudaError_t e;
+    EnvGeom G{};
+    G.n0 = n0;
+    G.n1 = n1;
+    G.n2 = n2;
+    G.msh = std::max(n0, n1);
+    const int dsh = std::abs(n1 - n0) / 2;
+    if (n0 > n1) {
+        G.off0 = 0;
+        G.off1 = dsh;
+        G.off2 = 0;
+    } else {
+        G.off0 = dsh;
+        G.off1 = 0;
+        G.off2 = dsh;
+    }
+    const long long M = (long long)G.msh * G.msh * G.msh;
+    const unsigned mg = (unsigned)std::min<long long>((M + 255) / 256, 152ll * 16);
+    const dim3 cg((unsigned)((G.msh + 31) / 32), (unsigned)((G.msh + 7) / 8), (unsigned)G.msh), cb(32, 8);
+    k_env_pad<C2><<<cg, cb, 0, s>>>(G, orig, flags, W.hp0, W.cpad);
+    k_env_swap<<<cg, cb, 0, s>>>(G, W.hp0, W.cpad, W.hp1, W.nan_count);
+    unsigned int nans = 0;
+    if ((e = cudaMemcpyAsync(&nans, W.nan_count, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+        return e;
+    const double *hp = W.hp1;
+    if (nans) {
+        k_edt_init<<<mg, 256, 0, s>>>(M, W.hp1, W.ft);
+        const long long nl = (long long)G.msh * G.msh;
+        for (int ax = 0; ax < 3; ++ax)
+            k_edt_pass<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(G.msh, ax, W.ft, W.scratch);
+        k_edt_gather<<<mg, 256, 0, s>>>(M, W.ft, W.hp1, W.hp0);
+        hp = W.hp0;
+    }
+    T *g0 = (T *)W.g0, *g1 = (T *)W.g1;
+    const dim3 vb(32, 8);
+    const dim3 g0g((unsigned)((n2 + 31) / 32), (unsigned)((n0 + 7) / 8), (unsigned)n1);
+    const dim3 g1g((unsigned)((n2 + 31) / 32), (unsigned)((n1 + 7) / 8), (unsigned)n0);
+    const size_t sm01 = (size_t)(8 + 2 * gr) * 32 * 8, sm2 = (size_t)8 * (32 + 2 * gr) * 8;
+    const size_t smx = std::max(sm01, sm2);
+    if (smx > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(k_env_gauss<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx)))
+        return e;
+    k_env_gauss<T><<<g0g, vb, sm01, s>>>(G, 0, hp, nullptr, g0, W.gw, gr);
+    k_env_gauss<T><<<g1g, vb, sm01, s>>>(G, 1, hp, g0, g1, W.gw, gr);
+    k_env_gauss<T><<<g1g, vb, sm2, s>>>(G, 2, hp, g1, out, W.gw, gr);
+    return cudaGetLastError();
 }
 
 // ---- method "sh": min / max over the spillover (and shell) voxels and the
-// histogram of all values in [fmin, fmax] -----------------------------------
-__device__ __forceinline__ unsigned long long fkey(float f)
-{
-    const unsigned int b = __float_as_uint(f);
-    return (b >> 31) ? (unsigned long long)(~b) : (unsigned long long)(b | 0x80000000u);
-}
-__host__ __device__ __forceinline__ float fkey_val(unsigned long long k)
-{
-    const unsigned int u = (unsigned int)k;
+// histogram of all values in [fmin, fmax], for float32 or float64 data ------
+// Order-preserving keys of the values (min / max by integer atomics).
+template <typename T>
+struct OrdKey;
+template <>
+struct OrdKey<float> {
+    __device__ static unsigned long long of(float f)
+    {
+        const unsigned int b = __float_as_uint(f);
+        return (b >> 31) ? (unsigned long long)(~b) : (unsigned long long)(b | 0x80000000u);
+    }
+    __host__ __device__ static float val(unsigned long long k)
+    {
+        const unsigned int u = (unsigned int)k;
+        const unsigned int b = (u >> 31) ? (u & 0x7fffffffu) : ~u;
 #ifdef __CUDA_ARCH__
-    return __uint_as_float((u >> 31) ? (u & 0x7fffffffu) : ~u);
+        return __uint_as_float(b);
 #else
-    const unsigned int b = (u >> 31) ? (u & 0x7fffffffu) : ~u;
-    float f;
-    memcpy(&f, &b, 4);
-    return f;
+        float f;
+        memcpy(&f, &b, 4);
+        return f;
 #endif
+    }
+};
+template <>
+struct OrdKey<double> {
+    __device__ static unsigned long long of(double f)
+    {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(f);
+        return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+    }
+    __host__ __device__ static double val(unsigned long long k)
+    {
+        const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+#ifdef __CUDA_ARCH__
+        return __longlong_as_double((long long)b);
+#else
+        double f;
+        memcpy(&f, &b, 8);
+        return f;
+#endif
+    }
+};
+
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+
+// One spatial constraint's arguments: the real parts at data[v * stride]
+// (stride 2 for complex data), the voxel flags, and the "sh" state.
+template <typename T>
+struct ConsArgs {
+    T *data;
+    long long N;
+    int stride;
+    const uint8_t *flags;
+    int method;  // 0 nn, 1 sh
+    int has_mask;
+    unsigned long long *keys;  // [2] min, max keys (method "sh")
+    unsigned int *hist;        // [HIST_BINS]
+    const T *edges;            // [HIST_BINS + 1]
+    const T *th;               // lo, hi, fmin, fmax
+    const int *stop;           // with `it`: skip iterations after the stop (NULL: never)
+    int it;
+};
+
+template <typename T>
+__device__ __forceinline__ bool cons_skip(const ConsArgs<T> &C)
+{
+    if (!C.stop)
+        return false;
+    const int s = *(volatile const int *)C.stop;
+    return s != 0 && s <= C.it;
 }
 
-__global__ void k_sh_minmax(AP P, int it)
+template <typename T>
+__global__ void k_sh_minmax(ConsArgs<T> C)
 {
-    if (ran_out(P, it))
+    if (cons_skip(C))
         return;
     unsigned long long mn = ~0ull, mx = 0;
-    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < P.N;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < C.N;
          v += (long long)gridDim.x * blockDim.x) {
-        if (P.flags[v] & (F_SPOV | F_SHELL)) {
-            const unsigned long long k = fkey(P.data[v].x);
+        if (C.flags[v] & (F_SPOV | F_SHELL)) {
+            const unsigned long long k = OrdKey<T>::of(C.data[v * C.stride]);
             mn = min(mn, k);
             mx = max(mx, k);
         }
@@ -712,36 +865,37 @@ __global__ void k_sh_minmax(AP P, int it)
         mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, s));
     }
     if ((threadIdx.x & 31) == 0) {
-        atomicMin(&P.ctl->minkey, mn);
-        atomicMax(&P.ctl->maxkey, mx);
+        atomicMin(&C.keys[0], mn);
+        atomicMax(&C.keys[1], mx);
     }
 }
 
-// numpy.histogram's bin of x for equal bins (float32 arithmetic): index =
-// int(((x - first) / (last - first)) * bins), the last edge in the last bin,
-// then one-step corrections against the float32 edges.
-__global__ void k_sh_hist(AP P, int it)
+// numpy.histogram's bin of x for equal bins (arithmetic in the data's type):
+// index = int(((x - first) / (last - first)) * bins), the last edge in the
+// last bin, then one-step corrections against the edges.
+template <typename T>
+__global__ void k_sh_hist(ConsArgs<T> C)
 {
-    if (ran_out(P, it))
+    if (cons_skip(C))
         return;
     __shared__ unsigned int h[HIST_BINS];
     for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x)
         h[i] = 0;
     __syncthreads();
-    const float first = P.edges[0], last = P.edges[HIST_BINS];
-    const float denom = __fsub_rn(last, first);
-    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < P.N;
+    const T first = C.edges[0], last = C.edges[HIST_BINS];
+    const T denom = rn_sub(last, first);
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < C.N;
          v += (long long)gridDim.x * blockDim.x) {
-        const float x = P.data[v].x;
+        const T x = C.data[v * C.stride];
         if (!(x >= first && x <= last))
             continue;
-        int idx = (int)__fmul_rn(__fdiv_rn(__fsub_rn(x, first), denom), (float)HIST_BINS);
+        int idx = (int)rn_mul(rn_div(rn_sub(x, first), denom), (T)HIST_BINS);
         idx = min(max(idx, 0), HIST_BINS);  // (a zero-width range gives no NaN index)
         if (idx == HIST_BINS)
             idx -= 1;
-        if (idx > 0 && x < P.edges[idx])
+        if (idx > 0 && x < C.edges[idx])
             idx -= 1;
-        if (x >= P.edges[idx + 1] && idx != HIST_BINS - 1)
+        if (x >= C.edges[idx + 1] && idx != HIST_BINS - 1)
             idx += 1;
         idx = min(max(idx, 0), HIST_BINS - 1);
         atomicAdd(&h[idx], 1u);
@@ -749,7 +903,124 @@ __global__ void k_sh_hist(AP P, int it)
     __syncthreads();
     for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x)
         if (h[i])
-            atomicAdd(&P.hist[i], h[i]);
+            atomicAdd(&C.hist[i], h[i]);
+}
+
+// The constraint applied in place (constraint_nn / constraint_sh called on
+// their own): the real part constrained, the imaginary part zeroed.
+template <typename T>
+__global__ void k_constrain(ConsArgs<T> C)
+{
+    T lo = T(0), hi = T(0), fmin = T(0), fmax = T(0);
+    if (C.method == 1) {
+        lo = C.th[0];
+        hi = C.th[1];
+        fmin = C.th[2];
+        fmax = C.th[3];
+    }
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < C.N;
+         v += (long long)gridDim.x * blockDim.x) {
+        T *p = C.data + v * C.stride;
+        p[0] = constrain_re<T>(C.method, C.has_mask, p[0], C.flags[v], fmin, fmax, lo, hi);
+        if (C.stride == 2)
+            p[1] = T(0);
+    }
+}
+
+// numpy.linspace(first, last, 101) in the data's type (numpy.histogram's
+// edges; first == last widened by 0.5 each way first), as numpy evaluates
+// it: k * step + first, the last edge set to `last`.
+template <typename T>
+void hist_edges(T fmin, T fmax, T *edges)
+{
+    T first = fmin, last = fmax;
+    if (first == last) {
+        first = first - T(0.5);
+        last = last + T(0.5);
+    }
+    const T delta = last - first;
+    const T step = delta / (T)HIST_BINS;
+    for (int k = 0; k <= HIST_BINS; ++k) {
+        volatile T y = (T)k * step;  // no contraction into a fused multiply-add
+        edges[k] = y + first;
+    }
+    edges[HIST_BINS] = last;
+}
+
+// count_to_half of apple.py:266-278 on counts a[0..len)
+int count_to_half(const unsigned int *a, int len, int step)
+{
+    int num = 0;
+    for (int i = 1; i < len; ++i) {
+        if ((double)a[i * step] < (double)a[0] / 2.0)
+            break;
+        ++num;
+    }
+    return num;
+}
+
+// constraint_sh's thresholds from the 100 counts (apple.py:91-103): the
+// histogram's peak, the bins down to half its count either side, the bin
+// centres edge[k + 1] - de / 2; th = lo, hi, fmin, fmax.
+template <typename T>
+void sh_thresholds(const unsigned int *hist, const T *edges, T fmin, T fmax, T *th)
+{
+    int idx_c = 0;
+    for (int k = 1; k < HIST_BINS; ++k)
+        if (hist[k] > hist[idx_c])
+            idx_c = k;
+    const int idx_start = idx_c - (idx_c > 0 ? count_to_half(hist + idx_c - 1, idx_c, -1) : 0);
+    const int idx_end = idx_c + count_to_half(hist + idx_c, HIST_BINS - idx_c, 1);
+    const T de = edges[1] - edges[0];
+    const T half = de / T(2);
+    th[0] = edges[idx_start + 1] - half;
+    th[1] = edges[idx_end + 1] - half;
+    th[2] = fmin;
+    th[3] = fmax;
+}
+
+// The "sh" thresholds of the values C.data (synchronous: the min / max keys
+// and the counts come to the host).  C.keys, C.hist and C.edges point into
+// the device workspace; the thresholds are copied to C.th.  *stopped is set
+// when the iteration `C.it` lies after the loop's stop (nothing computed).
+template <typename T>
+cudaError_t sh_prepare(ConsArgs<T> C, unsigned eg, cudaStream_t s, bool *stopped)
+{
+    cudaError_t e;
+    const unsigned long long k0[2] = {~0ull, 0ull};
+    *stopped = false;
+    if ((e = cudaMemcpyAsync(C.keys, k0, 16, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemsetAsync(C.hist, 0, HIST_BINS * 4, s)))
+        return e;
+    k_sh_minmax<T><<<eg, 256, 0, s>>>(C);
+    unsigned long long keys[2];
+    int stop = 0;
+    if ((e = cudaMemcpyAsync(keys, C.keys, 16, cudaMemcpyDeviceToHost, s)))
+        return e;
+    if (C.stop && (e = cudaMemcpyAsync(&stop, C.stop, 4, cudaMemcpyDeviceToHost, s)))
+        return e;
+    if ((e = cudaStreamSynchronize(s)))
+        return e;
+    if (stop != 0 && stop <= C.it) {
+        *stopped = true;
+        return cudaSuccess;
+    }
+    const T fmin = OrdKey<T>::val(keys[0]), fmax = OrdKey<T>::val(keys[1]);
+    T edges[HIST_BINS + 1];
+    hist_edges<T>(fmin, fmax, edges);
+    if ((e = cudaMemcpyAsync((void *)C.edges, edges, sizeof(edges), cudaMemcpyHostToDevice, s)))
+        return e;
+    k_sh_hist<T><<<eg, 256, 0, s>>>(C);
+    unsigned int hist[HIST_BINS];
+    if ((e = cudaMemcpyAsync(hist, C.hist, sizeof(hist), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+        return e;
+    T th[4];
+    sh_thresholds<T>(hist, edges, fmin, fmax, th);
+    if ((e = cudaMemcpyAsync((void *)C.th, th, sizeof(th), cudaMemcpyHostToDevice, s)))
+        return e;
+    // the host arrays live until the copy ran
+    return cudaStreamSynchronize(s);
 }
 
 // ---------------------------------------------------------------------------
@@ -876,16 +1147,123 @@ std::vector<float2> twiddles(int n)
     return t;
 }
 
-// count_to_half of apple.py:266-278 on counts a[0..len)
-int count_to_half(const unsigned int *a, int len, int step)
+// ---- constraint_nn / constraint_sh / envelope_gauss called on their own --
+odt_status check_helper(const odt_apple_desc *d, int32_t real_bits)
 {
-    int num = 0;
-    for (int i = 1; i < len; ++i) {
-        if ((double)a[i * step] < (double)a[0] / 2.0)
-            break;
-        ++num;
+    if (!d)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL descriptor");
+    if (d->n0 < 1 || d->n1 < 1 || d->n2 < 1)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "volume sizes must be positive");
+    if ((long long)d->n0 * d->n1 * d->n2 >= (1ll << 31))
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "volume too large (2^31 voxels or more)");
+    if (real_bits != 32 && real_bits != 64)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "real_bits must be 32 or 64");
+    return ODT_OK;
+}
+
+odt_status check_envelope(const odt_apple_desc *d)
+{
+    if (d->n0 != d->n2)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "`shape[0]` and `shape[2]` must be identical!");
+    if (d->gauss_radius < 0 || !d->gauss_weights)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "envelope needs the Gaussian weights");
+    if (d->gauss_radius > GAUSS_RMAX)
+        return (odt_status)set_error(ODT_ERR_UNSUPPORTED, "envelope Gaussian radius above 64 (volume axes above 1590)");
+    const long long msh = std::max(d->n0, d->n1);
+    if (msh * msh * msh >= (1ll << 31))
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "volume too large (max(n0, n1)^3 of 2^31 or more)");
+    return ODT_OK;
+}
+
+struct HelperLayout {
+    size_t ctl, hist, edges, ftab, flags, gw, hp0, hp1, cpad, ft, scratch, g0, g1, total;
+};
+
+// envelope == false: the constraint's workspace; true: the envelope's
+HelperLayout helper_layout(const odt_apple_desc &d, bool envelope)
+{
+    const long long N = (long long)d.n0 * d.n1 * d.n2;
+    HelperLayout L{};
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o += (bytes + 255) / 256 * 256;
+        return at;
+    };
+    L.ctl = take(64);  // min / max keys, thresholds (or the NaN counter)
+    if (!envelope) {
+        L.hist = take(HIST_BINS * 4);
+        L.edges = take((HIST_BINS + 1) * 8);
+        L.ftab = take(flag_table_bytes(d.n0, d.n1, d.n2));
+        L.flags = take((size_t)N);
+    } else {
+        const long long msh = std::max(d.n0, d.n1);
+        const long long M = msh * msh * msh;
+        L.gw = take((size_t)(2 * std::max(d.gauss_radius, 0) + 1) * 8);
+        L.hp0 = take((size_t)M * 8);
+        L.hp1 = take((size_t)M * 8);
+        L.cpad = take((size_t)M);
+        L.ft = take((size_t)M * 4);
+        L.scratch = take((size_t)msh * msh * 2 * msh * 4);
+        L.g0 = take((size_t)N * 8);
+        L.g1 = take((size_t)N * 8);
     }
-    return num;
+    L.total = o;
+    return L;
+}
+
+template <typename T>
+cudaError_t constrain_impl(const odt_apple_desc &d, int is_complex, T *data, const uint8_t *mask,
+                           const uint8_t *bg_shell, char *ws, const HelperLayout &L, cudaStream_t s)
+{
+    cudaError_t e;
+    const long long N = (long long)d.n0 * d.n1 * d.n2;
+    uint8_t *flags = (uint8_t *)(ws + L.flags);
+    // spillover region (shell 0), the given shell and mask
+    if ((e = compute_flags(d.n0, d.n1, d.n2, 1.0, 0, 0.0, mask, bg_shell, flags, (double *)(ws + L.ftab), s)))
+        return e;
+    ConsArgs<T> C{};
+    C.data = data;
+    C.N = N;
+    C.stride = is_complex ? 2 : 1;
+    C.flags = flags;
+    C.method = d.method == ODT_APPLE_SH ? 1 : 0;
+    C.has_mask = mask != nullptr;
+    C.keys = (unsigned long long *)(ws + L.ctl);
+    C.th = (const T *)(ws + L.ctl + 16);
+    C.hist = (unsigned int *)(ws + L.hist);
+    C.edges = (const T *)(ws + L.edges);
+    const unsigned eg = (unsigned)std::min<long long>((N + 255) / 256, 152ll * 16);
+    if (C.method == 1) {
+        bool stopped;
+        if ((e = sh_prepare<T>(C, eg, s, &stopped)))
+            return e;
+    }
+    k_constrain<T><<<eg, 256, 0, s>>>(C);
+    return cudaGetLastError();
+}
+
+template <typename C2, typename T>
+cudaError_t envelope_impl(const odt_apple_desc &d, const C2 *ftdata, const uint8_t *core, T *out, char *ws,
+                          const HelperLayout &L, cudaStream_t s)
+{
+    cudaError_t e;
+    EnvWork W{};
+    W.hp0 = (double *)(ws + L.hp0);
+    W.hp1 = (double *)(ws + L.hp1);
+    W.cpad = (uint8_t *)(ws + L.cpad);
+    W.ft = (int *)(ws + L.ft);
+    W.scratch = (int *)(ws + L.scratch);
+    W.g0 = ws + L.g0;
+    W.g1 = ws + L.g1;
+    W.gw = (const double *)(ws + L.gw);
+    W.nan_count = (unsigned int *)(ws + L.ctl);
+    // (the weights are read on the host until run_envelope's first wait)
+    if ((e = cudaMemcpyAsync(ws + L.gw, d.gauss_weights, (size_t)(2 * d.gauss_radius + 1) * 8,
+                             cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemsetAsync(W.nan_count, 0, 4, s)))
+        return e;
+    return run_envelope<C2, T>(d.n0, d.n1, d.n2, d.gauss_radius, ftdata, core, out, W, s);
 }
 
 }  // namespace
@@ -918,7 +1296,8 @@ odt_status odt_apple_flags(const odt_apple_desc *desc, const uint8_t *mask, uint
         return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "misaligned pointer");
     const odt_apple_desc &d = *desc;
     const cudaError_t e = compute_flags(d.n0, d.n1, d.n2, (2.0 * M_PI * d.nm) / d.res, d.use_bg_shell,
-                                        d.bg_shell_width, mask, flags, (double *)workspace, (cudaStream_t)stream);
+                                        d.bg_shell_width, mask, nullptr, flags, (double *)workspace,
+                                        (cudaStream_t)stream);
     return e == cudaSuccess ? ODT_OK : cuda_fail("apple flags", e);
 }
 
@@ -995,63 +1374,26 @@ odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real, co
     }
     const unsigned eg = (unsigned)std::min<long long>((N + 255) / 256, 152ll * 16);
     const double km = (2.0 * M_PI * d.nm) / d.res;
-    if ((e = compute_flags(d.n0, d.n1, d.n2, km, d.use_bg_shell, d.bg_shell_width, mask, (uint8_t *)(ws + L.flags),
-                           (double *)(ws + L.ftab), s)))
+    if ((e = compute_flags(d.n0, d.n1, d.n2, km, d.use_bg_shell, d.bg_shell_width, mask, nullptr,
+                           (uint8_t *)(ws + L.flags), (double *)(ws + L.ftab), s)))
         return cuda_fail("apple flags", e);
     // original spectrum: axis 2, 1 from f.real into buf, axis 0 into orig
     if ((e = launch_x(P, 0, -1, s)) || (e = launch_s(P, 1, 0, -1, s)) || (e = launch_s(P, 0, 2, -1, s)))
         return cuda_fail("apple spectrum", e);
     k_apple_dec<<<1, 1, 0, s>>>(P, -1);
     if (P.evlp) {
-        EnvGeom G{};
-        G.n0 = d.n0;
-        G.n1 = d.n1;
-        G.n2 = d.n2;
-        G.msh = std::max(d.n0, d.n1);
-        const int dsh = std::abs(d.n1 - d.n0) / 2;
-        if (d.n0 > d.n1) {
-            G.off0 = 0;
-            G.off1 = dsh;
-            G.off2 = 0;
-        } else {
-            G.off0 = dsh;
-            G.off1 = 0;
-            G.off2 = dsh;
-        }
-        const long long M = (long long)G.msh * G.msh * G.msh;
-        const unsigned mg = (unsigned)std::min<long long>((M + 255) / 256, 152ll * 16);
-        double *hp0 = (double *)(ws + L.hp0), *hp1 = (double *)(ws + L.hp1);
-        const dim3 cg((unsigned)((G.msh + 31) / 32), (unsigned)((G.msh + 7) / 8), (unsigned)G.msh), cb(32, 8);
-        k_env_pad<<<cg, cb, 0, s>>>(G, P.orig, P.flags, hp0, (uint8_t *)(ws + L.cpad));
-        k_env_swap<<<cg, cb, 0, s>>>(G, hp0, (const uint8_t *)(ws + L.cpad), hp1, &P.ctl->nan_count);
-        unsigned int nans = 0;
-        if ((e = cudaMemcpyAsync(&nans, &P.ctl->nan_count, 4, cudaMemcpyDeviceToHost, s)) ||
-            (e = cudaStreamSynchronize(s)))
-            return cuda_fail("apple envelope", e);
-        const double *hp = hp1;
-        if (nans) {
-            int *ft = (int *)(ws + L.ft);
-            k_edt_init<<<mg, 256, 0, s>>>(M, hp1, ft);
-            const long long nl = (long long)G.msh * G.msh;
-            for (int ax = 0; ax < 3; ++ax)
-                k_edt_pass<<<(unsigned)((nl + 127) / 128), 128, 0, s>>>(G.msh, ax, ft, (int *)(ws + L.scratch));
-            k_edt_gather<<<mg, 256, 0, s>>>(M, ft, hp1, hp0);
-            hp = hp0;
-        }
-        float *g0 = (float *)(ws + L.g0), *g1 = (float *)(ws + L.g1);
-        const double *gw = (const double *)(ws + L.gw);
-        const int gr = d.gauss_radius;
-        const dim3 vb(32, 8);
-        const dim3 g0g((unsigned)((d.n2 + 31) / 32), (unsigned)((d.n0 + 7) / 8), (unsigned)d.n1);
-        const dim3 g1g((unsigned)((d.n2 + 31) / 32), (unsigned)((d.n1 + 7) / 8), (unsigned)d.n0);
-        const size_t sm01 = (size_t)(8 + 2 * gr) * 32 * 8, sm2 = (size_t)8 * (32 + 2 * gr) * 8;
-        const size_t smx = std::max(sm01, sm2);
-        if (smx > 48 * 1024)
-            cudaFuncSetAttribute(k_env_gauss, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
-        k_env_gauss<<<g0g, vb, sm01, s>>>(G, 0, hp, nullptr, g0, gw, gr);
-        k_env_gauss<<<g1g, vb, sm01, s>>>(G, 1, hp, g0, g1, gw, gr);
-        k_env_gauss<<<g1g, vb, sm2, s>>>(G, 2, hp, g1, (float *)(ws + L.evlp), gw, gr);
-        if ((e = cudaGetLastError()))
+        EnvWork W{};
+        W.hp0 = (double *)(ws + L.hp0);
+        W.hp1 = (double *)(ws + L.hp1);
+        W.cpad = (uint8_t *)(ws + L.cpad);
+        W.ft = (int *)(ws + L.ft);
+        W.scratch = (int *)(ws + L.scratch);
+        W.g0 = ws + L.g0;
+        W.g1 = ws + L.g1;
+        W.gw = (const double *)(ws + L.gw);
+        W.nan_count = &P.ctl->nan_count;
+        if ((e = run_envelope<float2, float>(d.n0, d.n1, d.n2, d.gauss_radius, P.orig, P.flags,
+                                             (float *)(ws + L.evlp), W, s)))
             return cuda_fail("apple envelope", e);
     }
     if (d.max_iter == 0 || d.method == ODT_APPLE_SH)
@@ -1067,63 +1409,25 @@ odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real, co
             } else {
                 // constraint_sh: min / max over the spillover region, the
                 // histogram, and the thresholds (host, from 100 counts)
-                AppleCtl c0{};
-                c0.minkey = ~0ull;
-                c0.maxkey = 0;
-                if ((e = cudaMemcpyAsync(&P.ctl->minkey, &c0.minkey, 16, cudaMemcpyHostToDevice, s)) ||
-                    (e = cudaMemsetAsync(P.hist, 0, HIST_BINS * 4, s)))
+                ConsArgs<float> C{};
+                C.data = (float *)P.data;
+                C.N = N;
+                C.stride = 2;
+                C.flags = P.flags;
+                C.method = 1;
+                C.keys = &P.ctl->minkey;
+                C.hist = P.hist;
+                C.edges = P.edges;
+                C.th = &P.ctl->lo;
+                C.stop = &P.ctl->stop;
+                C.it = it;
+                bool stopped = false;
+                if ((e = sh_prepare<float>(C, eg, s, &stopped)))
                     return cuda_fail("apple sh", e);
-                k_sh_minmax<<<eg, 256, 0, s>>>(P, it);
-                unsigned long long keys[2];
-                int stop = 0;
-                if ((e = cudaMemcpyAsync(keys, &P.ctl->minkey, 16, cudaMemcpyDeviceToHost, s)) ||
-                    (e = cudaMemcpyAsync(&stop, &P.ctl->stop, 4, cudaMemcpyDeviceToHost, s)) ||
-                    (e = cudaStreamSynchronize(s)))
-                    return cuda_fail("apple sh", e);
-                if (stop != 0 && stop <= it)
+                if (stopped)
                     break;
-                float fmin = fkey_val(keys[0]), fmax = fkey_val(keys[1]);
-                float first = fmin, last = fmax;
-                if (first == last) {
-                    first = first - 0.5f;
-                    last = last + 0.5f;
-                }
-                // numpy.linspace(first, last, 101) in float32
-                float edges[HIST_BINS + 1];
-                const float delta = last - first;
-                const float step = delta / (float)HIST_BINS;
-                for (int k = 0; k <= HIST_BINS; ++k) {
-                    volatile float y = (float)k * step;
-                    edges[k] = y + first;
-                }
-                edges[HIST_BINS] = last;
-                if ((e = cudaMemcpyAsync(ws + L.edges, edges, sizeof(edges), cudaMemcpyHostToDevice, s)))
-                    return cuda_fail("apple sh", e);
-                k_sh_hist<<<eg, 256, 0, s>>>(P, it);
-                unsigned int hist[HIST_BINS];
-                if ((e = cudaMemcpyAsync(hist, P.hist, sizeof(hist), cudaMemcpyDeviceToHost, s)) ||
-                    (e = cudaStreamSynchronize(s)))
-                    return cuda_fail("apple sh", e);
-                int idx_c = 0;
-                for (int k = 1; k < HIST_BINS; ++k)
-                    if (hist[k] > hist[idx_c])
-                        idx_c = k;
-                const int idx_start = idx_c - (idx_c > 0 ? count_to_half(hist + idx_c - 1, idx_c, -1) : 0);
-                const int idx_end = idx_c + count_to_half(hist + idx_c, HIST_BINS - idx_c, 1);
-                const float de = edges[1] - edges[0];
-                const float half = de / 2.0f;
-                float th[4];
-                th[0] = edges[idx_start + 1] - half;  // lo
-                th[1] = edges[idx_end + 1] - half;    // hi
-                th[2] = fmin;
-                th[3] = fmax;
-                if ((e = cudaMemcpyAsync(&P.ctl->lo, th, 16, cudaMemcpyHostToDevice, s)))
-                    return cuda_fail("apple sh", e);
                 if ((e = launch_x(P, 3, it, s)))
                     return cuda_fail("apple iteration", e);
-                // keep the host arrays alive until the copies ran
-                if ((e = cudaStreamSynchronize(s)))
-                    return cuda_fail("apple sh", e);
             }
             if ((e = launch_s(P, 1, 0, it, s)) || (e = launch_s(P, 0, 3, it, s)))
                 return cuda_fail("apple iteration", e);
@@ -1143,6 +1447,81 @@ odt_status odt_apple_correct(const odt_apple_desc *desc, const float *f_real, co
     if (iterations)
         *iterations = done;
     return ODT_OK;
+}
+
+odt_status odt_apple_constrain_workspace_size(const odt_apple_desc *desc, size_t *bytes)
+{
+    const odt_status st = check_helper(desc, 32);
+    if (st != ODT_OK)
+        return st;
+    if (!bytes)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL output pointer");
+    *bytes = helper_layout(*desc, false).total;
+    return ODT_OK;
+}
+
+odt_status odt_apple_constrain(const odt_apple_desc *desc, int32_t real_bits, int32_t is_complex, void *data,
+                               const uint8_t *mask, const uint8_t *bg_shell, void *workspace, size_t workspace_bytes,
+                               void *stream)
+{
+    const odt_status st = check_helper(desc, real_bits);
+    if (st != ODT_OK)
+        return st;
+    if (desc->method != ODT_APPLE_NN && desc->method != ODT_APPLE_SH)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "constraint method must be nn or sh");
+    if (is_complex != 0 && is_complex != 1)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "is_complex must be 0 or 1");
+    if (!data || !workspace)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL device pointer");
+    const HelperLayout L = helper_layout(*desc, false);
+    if (workspace_bytes < L.total)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "workspace too small");
+    if ((uintptr_t)workspace % 256 || (uintptr_t)data % (real_bits / 8))
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "misaligned pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    const cudaError_t e =
+        real_bits == 32
+            ? constrain_impl<float>(*desc, is_complex, (float *)data, mask, bg_shell, (char *)workspace, L, s)
+            : constrain_impl<double>(*desc, is_complex, (double *)data, mask, bg_shell, (char *)workspace, L, s);
+    return e == cudaSuccess ? ODT_OK : cuda_fail("apple constraint", e);
+}
+
+odt_status odt_apple_envelope_workspace_size(const odt_apple_desc *desc, size_t *bytes)
+{
+    odt_status st = check_helper(desc, 32);
+    if (st == ODT_OK)
+        st = check_envelope(desc);
+    if (st != ODT_OK)
+        return st;
+    if (!bytes)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL output pointer");
+    *bytes = helper_layout(*desc, true).total;
+    return ODT_OK;
+}
+
+odt_status odt_apple_envelope(const odt_apple_desc *desc, int32_t real_bits, const void *ftdata, const uint8_t *core,
+                              void *envelope, void *workspace, size_t workspace_bytes, void *stream)
+{
+    odt_status st = check_helper(desc, real_bits);
+    if (st == ODT_OK)
+        st = check_envelope(desc);
+    if (st != ODT_OK)
+        return st;
+    if (!ftdata || !core || !envelope || !workspace)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "NULL device pointer");
+    const HelperLayout L = helper_layout(*desc, true);
+    if (workspace_bytes < L.total)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "workspace too small");
+    const size_t rb = (size_t)real_bits / 8;
+    if ((uintptr_t)workspace % 256 || (uintptr_t)ftdata % (2 * rb) || (uintptr_t)envelope % rb)
+        return (odt_status)set_error(ODT_ERR_INVALID_ARGUMENT, "misaligned pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    const cudaError_t e =
+        real_bits == 32 ? envelope_impl<float2, float>(*desc, (const float2 *)ftdata, core, (float *)envelope,
+                                                       (char *)workspace, L, s)
+                        : envelope_impl<double2, double>(*desc, (const double2 *)ftdata, core, (double *)envelope,
+                                                         (char *)workspace, L, s);
+    return e == cudaSuccess ? ODT_OK : cuda_fail("apple envelope", e);
 }
 
 }  // extern "C"

@@ -26,13 +26,16 @@ Writes
                        sinogram_as_rytov / sinogram_as_radon
 
   reference_apple.npz  inputs and outputs of the reference's apple.correct
+  reference_apple_helpers.npz  inputs and outputs of the reference's
+                       constraint_nn, constraint_sh and envelope_gauss
+                       called on their own
   reference_c1.npz     the reference's backpropagate_3d of the whole
                        60-angle, 64x64 -> 64^3 ellipsoid-phantom workload
                        (FP64 run, stored as float32 real/imaginary parts),
                        with a checksum of the regenerated input
 
-Parts can be chosen on the command line (backprop, sino, apple, c1);
-default all.
+Parts can be chosen on the command line (backprop, sino, apple,
+apple_helpers, c1); default all.
 The input sinogram generator below restates the reference's test helper
 (tests/common_methods.py:63-184) so that the GPU tests can regenerate the
 same inputs without the reference tree.
@@ -67,6 +70,8 @@ def main(parts):
         make_sino(odt)
     if "apple" in parts:
         make_apple(odt)
+    if "apple_helpers" in parts:
+        make_apple_helpers(odt)
     if "c1" in parts:
         make_c1(odt)
     print("wrote fixtures to", HERE)
@@ -319,5 +324,81 @@ def make_apple(odt):
     np.savez_compressed(os.path.join(HERE, "reference_apple.npz"), **out)
 
 
+def make_apple_helpers(odt):
+    """reference_apple_helpers.npz: inputs and outputs of the reference's
+    constraint_nn / constraint_sh (odtbrain/apple.py:56-110, in place) and
+    envelope_gauss (:289-350), run unmodified on small volumes of float32,
+    float64, complex64 and complex128 data."""
+    out = {}
+    rng = np.random.default_rng(47)
+
+    def volume(A, nx, ny, seed):
+        s, a = gauss_sino_3d(A=A, Nx=nx, Ny=ny, max_phase=2.5,
+                             ampl_range=(0.9, 1.0))
+        s = s * np.exp(0.05j * np.random.default_rng(seed).standard_normal(
+            s.shape))
+        return odt.backpropagate_3d(np.log(s), a, res=2.5, nm=1.333,
+                                    padval=0, dtype=float)
+
+    cube = volume(12, 20, 20, 1)
+    rect = volume(10, 18, 12, 2)
+    out["in_cube"] = cube
+    out["in_rect"] = rect
+
+    def cons(name, fn, src, dtype, mask=None, shell=None):
+        # the input is in_<src> cast to dtype (its real part for a real type)
+        base = {"cube": cube, "rect": rect}[src]
+        if np.issubdtype(dtype, np.complexfloating):
+            data = base.astype(dtype)
+        else:
+            data = np.ascontiguousarray(base.real.astype(dtype))
+        kw = {}
+        if mask is not None:
+            kw["mask"] = mask
+            out[name + "__mask"] = mask
+        if shell is not None:
+            kw["bg_shell"] = shell
+            out[name + "__shell"] = shell
+        getattr(odt.apple, fn)(data=data, **kw)
+        out[name + "__src"] = np.array(src)
+        out[name + "__fn"] = np.array(fn)
+        out[name + "__out"] = data
+
+    mask_c = rng.random(cube.shape) > 0.3
+    mask_r = rng.random(rect.shape) > 0.5
+    shell_c = odt.apple.ellipsoid_shell(cube.shape, width=3)
+    shell_r = odt.apple.ellipsoid_shell(rect.shape, width=2)
+    cons("nn_c64", "constraint_nn", "cube", np.complex64)
+    cons("nn_c64_mask_shell", "constraint_nn", "cube", np.complex64,
+         mask_c, shell_c)
+    cons("nn_f64_shell", "constraint_nn", "cube", np.float64, None, shell_c)
+    cons("nn_c128_rect_mask", "constraint_nn", "rect", np.complex128, mask_r)
+    cons("sh_c64", "constraint_sh", "cube", np.complex64)
+    cons("sh_c64_mask_shell", "constraint_sh", "cube", np.complex64,
+         mask_c, shell_c)
+    cons("sh_c128", "constraint_sh", "cube", np.complex128)
+    cons("sh_f32_rect_shell", "constraint_sh", "rect", np.float32, None,
+         shell_r)
+    cons("sh_f64_rect_mask", "constraint_sh", "rect", np.float64, mask_r)
+
+    def env(name, src, dtype, res=2.5, nm=1.333):
+        ft = np.fft.fftn(src).astype(dtype)
+        core = odt.apple.apple_core_3d(shape=src.shape, res=res, nm=nm)
+        out[name + "__ft"] = ft
+        out[name + "__core"] = core
+        out[name + "__out"] = odt.apple.envelope_gauss(ftdata=ft.copy(),
+                                                       core=core)
+
+    env("env_c64_cube", cube, np.complex64)
+    env("env_c128_cube", cube, np.complex128)
+    env("env_c64_rect", rect, np.complex64)  # shape[0] > shape[1]
+    tall = np.ascontiguousarray(cube[4:16, :, 4:16])  # shape[0] < shape[1]
+    env("env_c64_tall", tall, np.complex64, res=1.5)
+    env("env_c128_tall", tall, np.complex128, res=1.5)
+    np.savez_compressed(os.path.join(HERE, "reference_apple_helpers.npz"),
+                        **out)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1:] or ["backprop", "sino", "apple", "c1"])
+    main(sys.argv[1:] or ["backprop", "sino", "apple", "apple_helpers",
+                          "c1"])

@@ -19,6 +19,7 @@ import os
 import numpy as np
 import pytest
 
+import apple_helper_cases
 from oracle import apple_oracle as ao
 from oracle import odt_oracle, unwrap_oracle
 from sino_gen import cutout, gauss_sino_3d
@@ -212,3 +213,74 @@ def test_well_conditioned_cases_are_tight(odt, apple_fix):
         assert tolerance(f, **kw) == REL, n
         close(odt.apple.correct(f=f.copy(), **kw), apple_fix[n + "__out"],
               REL, n)
+
+
+@pytest.fixture(scope="module")
+def helper_fix():
+    return apple_helper_cases.load()
+
+
+def test_constraints_match_reference(odt, helper_fix):
+    """constraint_nn / constraint_sh called on their own
+    (odtbrain/apple.py:56-110), in place on float32, float64, complex64 and
+    complex128 NumPy arrays with and without mask and background shell:
+    bit-identical to the reference's results (zeroing and exact halving,
+    with the histogram thresholds computed as NumPy does)."""
+    n = 0
+    for name, fn, data, kw, ref in apple_helper_cases.constraint_cases(helper_fix):
+        assert getattr(odt.apple, fn)(data, **kw) is None
+        assert data.dtype == ref.dtype
+        np.testing.assert_array_equal(data, ref, err_msg=name)
+        n += 1
+    assert n == 9
+
+
+def test_constraints_tensor_and_view_inputs(odt, helper_fix):
+    """A CUDA tensor is constrained where it lies, a CPU tensor and a
+    non-contiguous NumPy array are written back in place."""
+    import torch
+    cases = {c[0]: c for c in apple_helper_cases.constraint_cases(helper_fix)}
+    _, fn, data, kw, ref = cases["sh_c64_mask_shell"]
+    t = torch.from_numpy(data.copy()).cuda()
+    ptr = t.data_ptr()
+    getattr(odt.apple, fn)(t, mask=torch.from_numpy(kw["mask"]).cuda(),
+                           bg_shell=kw["bg_shell"])
+    assert t.data_ptr() == ptr
+    np.testing.assert_array_equal(t.cpu().numpy(), ref)
+    _, fn, data, kw, ref = cases["nn_c128_rect_mask"]
+    c = torch.from_numpy(data.copy())
+    getattr(odt.apple, fn)(c, **kw)
+    np.testing.assert_array_equal(c.numpy(), ref)
+    f = np.asfortranarray(data)
+    getattr(odt.apple, fn)(f, **kw)
+    assert f.flags.f_contiguous
+    np.testing.assert_array_equal(f, ref)
+
+
+def test_envelope_matches_reference(odt, helper_fix):
+    """envelope_gauss called on its own (odtbrain/apple.py:289-350): cubic
+    and both non-cubic paddings, complex64 and complex128 spectra.  The
+    magnitudes are the one rounding that may differ (CUDA's hypot against
+    the C library's, within an ulp); the Gaussian's FP64 sums run in
+    scipy's order.  Bound: 2e-6 (float32) and 1e-13 (float64) of the
+    largest value."""
+    n = 0
+    for name, ft, core, ref in apple_helper_cases.envelope_cases(helper_fix):
+        got = odt.apple.envelope_gauss(ft, core)
+        assert got.dtype == ref.dtype and got.shape == ref.shape
+        close(got, ref, rel=2e-6 if ref.dtype == np.float32 else 1e-13,
+              name=name)
+        n += 1
+    assert n == 5
+
+
+def test_envelope_gauss_shape(odt):
+    """tests/test_apple.py:90-97 of the reference: a non-cubic volume, here
+    also compared with the oracle."""
+    shape = (60, 50, 60)
+    ftdata = np.ones(shape)
+    core = odt.apple.apple_core_3d(shape=shape, res=.1, nm=1)
+    envlp = odt.apple.envelope_gauss(ftdata=ftdata, core=core)
+    assert envlp.shape == shape
+    close(envlp, ao.envelope_gauss(ftdata, core), rel=1e-13,
+          name="ones_60_50_60")

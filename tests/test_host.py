@@ -266,6 +266,63 @@ def test_apple_descriptor_checks(native_lib):
     assert ws(ctypes.byref(d), ctypes.byref(nb)) == _native.ODT_OK
 
 
+def test_apple_helper_argument_checks(native_lib):
+    """odt_apple_constrain / odt_apple_envelope check their arguments on the
+    host before anything is launched (no device pointer is touched)."""
+    from odtbrain_gb300 import apple
+    nb = ctypes.c_uint64()
+    d = _native.AppleDesc()
+    d.n0, d.n1, d.n2 = 12, 20, 9  # any 3D shape for a constraint
+    d.method = _native.ODT_APPLE_SH
+    assert native_lib.odt_apple_constrain_workspace_size(
+        ctypes.byref(d), ctypes.byref(nb)) == _native.ODT_OK
+    assert nb.value >= 12 * 20 * 9
+    bad = _native.ODT_ERR_INVALID_ARGUMENT
+    fake = ctypes.c_void_p(4096)  # never dereferenced: the checks fail first
+    con = native_lib.odt_apple_constrain
+    assert con(ctypes.byref(d), 16, 1, fake, None, None, fake, nb.value,
+               None) == bad  # real_bits
+    assert con(ctypes.byref(d), 32, 2, fake, None, None, fake, nb.value,
+               None) == bad  # is_complex
+    assert con(ctypes.byref(d), 32, 1, None, None, None, fake, nb.value,
+               None) == bad  # data
+    assert con(ctypes.byref(d), 32, 1, fake, None, None, fake, nb.value - 1,
+               None) == bad  # workspace size
+    assert con(ctypes.byref(d), 64, 0, ctypes.c_void_p(4100), None, None,
+               fake, nb.value, None) == bad  # alignment
+    d.method = _native.ODT_APPLE_NONE
+    assert con(ctypes.byref(d), 32, 1, fake, None, None, fake, nb.value,
+               None) == bad  # method
+    e = apple._desc((16, 12, 16), 2.1, 1.333)
+    assert native_lib.odt_apple_envelope_workspace_size(
+        ctypes.byref(e), ctypes.byref(nb)) == _native.ODT_OK
+    env = native_lib.odt_apple_envelope
+    assert env(ctypes.byref(e), 32, fake, None, fake, fake, nb.value,
+               None) == bad  # core
+    assert env(ctypes.byref(e), 64, ctypes.c_void_p(4104), fake, fake, fake,
+               nb.value, None) == bad  # complex128 alignment
+    e = apple._desc((16, 12, 15), 2.1, 1.333)
+    assert native_lib.odt_apple_envelope_workspace_size(
+        ctypes.byref(e), ctypes.byref(nb)) == bad  # n0 != n2
+    e = apple._desc((16, 12, 16), 2.1, 1.333)
+    e.gauss_radius = 65
+    assert native_lib.odt_apple_envelope_workspace_size(
+        ctypes.byref(e), ctypes.byref(nb)) == _native.ODT_ERR_UNSUPPORTED
+
+
+def test_apple_helper_dtype_errors():
+    """The Python drop-ins refuse what the kernels do not compute, before
+    touching a device."""
+    from odtbrain_gb300 import apple
+    with pytest.raises(TypeError):
+        apple.constraint_nn(np.zeros((4, 4, 4), dtype=np.int32))
+    with pytest.raises(ValueError):
+        apple.constraint_sh(np.zeros((4, 4), dtype=np.float32))
+    with pytest.raises(ValueError):
+        apple.envelope_gauss(np.zeros((4, 5, 6), dtype=np.complex64),
+                             np.zeros((4, 5, 6), dtype=bool))
+
+
 def test_apple_gauss_weights_match_scipy():
     """The 1D Gaussian handed to the envelope kernel is scipy's."""
     import scipy.ndimage as ndi
@@ -289,7 +346,8 @@ def test_public_names_match_the_reference():
                  "util", "warn", "__version__"):
         assert hasattr(odt, name), name
     for name in ("apple_core_3d", "correct", "spillover_region",
-                 "ellipsoid_shell", "count_to_half"):
+                 "ellipsoid_shell", "count_to_half", "constraint_nn",
+                 "constraint_sh", "envelope_gauss"):
         assert callable(getattr(odt.apple, name)), name
     assert callable(odt.util.compute_angle_weights_1d)
     assert issubclass(odt.warn.DataUndersampledWarning, UserWarning)
