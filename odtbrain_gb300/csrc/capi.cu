@@ -212,6 +212,7 @@ struct odt_bpp3d_plan {
     int nz;
     int batch;       // angles per batch
     int jobs;        // (angle, plane) jobs per column/row launch
+    int ydefer;      // the row stage adds the y-prefilter terms (StageParams::ydefer)
     size_t off_rowspec, off_T, off_T2, off_Tab, off_slab, off_comp, off_rot, ws_bytes;
     size_t off_Qg, off_W, off_Pg, off_vT, adj_ws_bytes;  // adjoint-only regions after ws_bytes
     double bx_ca, bx_cb, by_ca, by_cb;  // one-pole solve in the adjoint's form
@@ -294,6 +295,8 @@ StageParams stage_params(const odt_bpp3d_plan *p)
     P.gain = nullptr;
     P.again = nullptr;
     P.status = p->d_status;
+    P.ydefer = p->ydefer;
+    P.yedge_off = p->ydefer ? (long long)p->jobs * d.ny * d.pad_nx : 0;
     return P;
 }
 
@@ -543,7 +546,17 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
 
     // ---- batching: the largest angle batch (and column-stage chunk) whose
     // workspace fits the limit
+    // tilted path, order >= 2, crops other than the centred half: the
+    // column stage leaves the y-prefilter terms to the row stage and stores
+    // each job's raw edge samples (4 np rows) after the chunk's jobs
+    p->jobs = 0;
+    p->ydefer = 0;
+    {
+        const StageParams G = stage_params(p);
+        p->ydefer = (tilted && pf && !odt::half_crop(G) && !odt::single_row_plan(G)) ? 1 : 0;
+    }
     const size_t plane_row_bytes = (size_t)d.ny * lNx * 8;           // one job's column-stage output
+    const size_t edge_row_bytes = p->ydefer ? (size_t)4 * np * lNx * 8 : 0;  // its y-prefilter edge samples
     // one angle's coefficient slab [z][x][ypitch] (the adjoint's slab
     // gradients [y][z][x] fit too)
     const size_t slab_bytes = (size_t)nz * odt::yaxis_slab_pitch(d.ny) * d.nx * 8;
@@ -561,8 +574,8 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
         const int nbatches = (d.num_angles + batch - 1) / batch;
         size_t w = 0;
         const size_t o_rowspec = w; w = align_up(w + (size_t)batch * rowspec_bytes);
-        const size_t o_T = w; w = align_up(w + jobs * plane_row_bytes);
-        const size_t o_T2 = w; w = align_up(w + jobs * plane_row_bytes);
+        const size_t o_T = w; w = align_up(w + jobs * (plane_row_bytes + edge_row_bytes));
+        const size_t o_T2 = w; w = align_up(w + jobs * (plane_row_bytes + edge_row_bytes));
         const size_t o_Tab = w; w = align_up(w + (size_t)batch * tab_bytes);
         const size_t o_slab = w; w = align_up(w + (size_t)batch * slab_bytes);
         const size_t o_comp = w; w = align_up(w + (nbatches > 1 ? vol_bytes : 0));

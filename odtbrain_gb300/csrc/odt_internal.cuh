@@ -74,6 +74,13 @@ struct StageParams {
     const float2 *again; // optional complex per-angle gain [A][lNy*lNx], this
                          // batch's first angle at again (NULL: 1)
     int *status;
+    // Tilted path, order >= 2, crops other than the centred half (ydefer =
+    // 1): the column stage leaves the y-prefilter boundary terms to the row
+    // stage and stores the raw y-line samples around the crop's ends, 4
+    // npoles rows of lNx per job (edge_row order), at T + yedge_off + (q -
+    // q0) * 4 npoles * lNx of the job chunk's buffer T.
+    int ydefer;
+    long long yedge_off;
 };
 
 // y pitch of the slab layout [a][z][x][y]

@@ -92,6 +92,12 @@ __host__ __device__ constexpr bool edge_used(int slot, int np)
 {
     return ((slot & 3) >> 1) < np;
 }
+// Row of a used edge slot among the 4 np rows of the deferred y-prefilter's
+// edge samples (the slots at the crop's start, then those at its end).
+__host__ __device__ constexpr int edge_row(int slot, int np)
+{
+    return slot < 4 ? slot : 2 * np + (slot - 4);
+}
 
 // Coefficients of an NP-pole prefilter (NP = 1: orders 2, 3; NP = 2:
 // orders 4, 5) from the edge slots: c[i] = A_(i+1), c[NP + i] = B_(i+1).

@@ -144,20 +144,67 @@ __device__ __forceinline__ void column_spectrum(const StageParams &P, const L &l
     }
 }
 
+// The edge samples of the y-prefilter solve that thread j holds after a
+// column's backward transform: bit 8 r + e is set when slot r holds the
+// sample of edge slot e (the same for every plane of the CTA, so it is
+// computed once).  Power-of-two lines (8 slots).
+template <class L, int NP>
+__device__ __forceinline__ unsigned long long edge_holdings(const StageParams &P, int n, int j)
+{
+    unsigned long long m = 0;
+#pragma unroll
+    for (int e = 0; e < EDGE_SLOTS; ++e) {
+        if (edge_used(e, NP)) {
+            const int pos = (P.padyl + edge_offset(e, P.ny) + 2 * n) % n;
+            if (pos % L::TPL == j)
+                m |= 1ull << (8 * (pos / L::TPL) + e);
+        }
+    }
+    return m;
+}
+
 // Backward FFT along y of v, then the y-prefilter boundary terms (YF > 0:
 // tilted path, order >= 2, YF poles) and the cropped store dst[yy * lNx]
-// for yy < ny.
-template <class L, int KX, int YF, bool TW2 = false>
+// for yy < ny.  DEFER (P.ydefer): the terms' coefficients need the line's
+// edge samples, held by a few other threads, so adding them here costs a
+// barrier per line; instead the raw edge samples go to yedge[row * lNx]
+// (rows edge_row(e)), the crop is stored raw, and the row stage adds the
+// terms.  `eheld`: edge_holdings of this thread (power-of-two lines).
+template <class L, int KX, int YF, bool TW2 = false, bool DEFER = false>
 __device__ __forceinline__ void column_inverse_store(const StageParams &P, const L &line, float2 (&v)[L::SLOTS],
                                                      int c, int j, bool colok, float2 *buf0, float2 *buf1,
-                                                     const float2 *tw, float2 *edge, int &flip, float2 *dst)
+                                                     const float2 *tw, float2 *edge, int &flip, float2 *dst,
+                                                     float2 *yedge = nullptr, unsigned long long eheld = 0)
 {
     const int n = line.size();
     const int ny = P.ny, padyl = P.padyl;
     line.template run<1, true, TW2>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
-    constexpr bool yfix = YF > 0;
+    constexpr bool yfix = YF > 0 && !DEFER;
     constexpr int NPY = YF > 0 ? YF : 1;
     float2 cf[2 * NPY];
+    if constexpr (YF > 0 && DEFER) {
+        if constexpr (L::SLOTS <= 8) {
+            if (eheld && colok) {
+#pragma unroll
+                for (int r = 0; r < L::SLOTS; ++r) {
+                    const unsigned m = (unsigned)(eheld >> (8 * r)) & 0xffu;
+                    if (m) {
+#pragma unroll
+                        for (int e = 0; e < EDGE_SLOTS; ++e)
+                            if (edge_used(e, NPY) && (m & (1u << e)))
+                                yedge[(size_t)edge_row(e, NPY) * P.lNx] = v[r];
+                    }
+                }
+            }
+        } else if (colok) {
+#pragma unroll
+            for (int e = 0; e < EDGE_SLOTS; ++e) {
+                float2 t;
+                if (edge_used(e, NPY) && held<L>(v, j, (padyl + edge_offset(e, ny) + 2 * n) % n, t))
+                    yedge[(size_t)edge_row(e, NPY) * P.lNx] = t;
+            }
+        }
+    }
     if constexpr (yfix) {
         // u around the crop's ends (periodic over the padded height)
 #pragma unroll
@@ -307,6 +354,10 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
 
     float2 V[L::SLOTS];  // G * exp(i w z_p) for this thread's elements
     int flip = 0;
+    // tilted generic crops: the edge samples this thread holds (fixed)
+    unsigned long long eheld = 0;
+    if constexpr (!HALF && YF > 0 && L::SLOTS <= 8)
+        eheld = edge_holdings<L, YF>(P, n, j);
     int cur_a = -1;
     int since = 0;  // planes advanced by the recurrence since the last exact anchor
     int a = qb / nz, p = qb % nz;
@@ -358,6 +409,10 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
         if constexpr (HALF)
             column_inverse_store_half<L, KX, YF, TW2>(P, line, v, c, j, buf0, buf1, tw, edge, flip,
                                                   T + (size_t)(q - q0) * (L::N / 2) * L::N + kx);
+        else if constexpr (YF > 0)  // (tilted: the y-prefilter terms go to the row stage)
+            column_inverse_store<L, KX, YF, TW2, true>(
+                P, line, v, c, j, colok, buf0, buf1, tw, edge, flip, T + (size_t)(q - q0) * ny * lNx + kx,
+                T + P.yedge_off + (size_t)(q - q0) * 4 * YF * lNx + kx, eheld);
         else
             column_inverse_store<L, KX, YF, TW2>(P, line, v, c, j, colok, buf0, buf1, tw, edge, flip,
                                              T + (size_t)(q - q0) * ny * lNx + kx);
@@ -382,7 +437,23 @@ constexpr int rows_per_cta()
     return LPC >= 8 ? LPC : 8;
 }
 
-template <class L, int LPC, int NP>
+// YD (P.ydefer): the column stage left the tilted path's y-prefilter
+// boundary terms to this stage.  A CTA with rows within ZPOW_N of either end
+// of the crop solves each column's coefficients once, from the job's raw
+// edge samples, into shared memory (lines of up to 2048; longer lines solve
+// them per row), and those rows add the terms before the z-boundary rows:
+// the same values in the same order as in the column stage.
+template <class L>
+constexpr bool ycoef_smem()
+{
+    return pow2_len<L>() == 0 || pow2_len<L>() <= 2048;
+}
+template <class L, int NP, bool YD>
+constexpr size_t smem_rows_y(int n)
+{
+    return (YD && ycoef_smem<L>()) ? (size_t)2 * NP * n * sizeof(float2) : 0;
+}
+template <class L, int LPC, int NP, bool YD>
 __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     k_rows_inverse(StageParams P, L line, const float2 *T, const float2 *Tab, float2 *slab, int q0, int qn)
 {
@@ -428,15 +499,64 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
             v[r] = (valid && column_active(P, x)) ? __ldcs(src + x) : make_float2(0.f, 0.f);
         }
     };
+    // YD: the y-prefilter coefficient rows of this job, [2 NP][n] after the
+    // row buffers (CTAs with boundary rows)
+    float2 *ycs = smem + (2 * LPC * ls + tw_slots(n) + EDGE_SLOTS * LPC);
+    const float2 *yed = T + P.yedge_off + (size_t)qrel * 4 * NP * n;
+    if constexpr (YD && ycoef_smem<L>()) {
+        if (ybase < ZPOW_N || min(ybase + RG, ny) - 1 >= ny - ZPOW_N) {
+            for (int x = threadIdx.x; x < n; x += LPC * L::TPL) {
+                float2 cy[2 * NP];
+                if (column_active(P, x)) {
+                    float2 ed[EDGE_SLOTS];
+#pragma unroll
+                    for (int e = 0; e < EDGE_SLOTS; ++e)
+                        ed[e] = edge_used(e, NP) ? yed[(size_t)edge_row(e, NP) * n + x] : make_float2(0.f, 0.f);
+                    pf_coefs<NP>(P.kys, ed, cy);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 2 * NP; ++i)
+                        cy[i] = make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int i = 0; i < 2 * NP; ++i)
+                    ycs[i * n + x] = cy[i];
+            }
+        }
+    }
     float2 v[L::SLOTS], vn[L::SLOTS];
     load_row(ybase + l, v);
-    __syncthreads();  // twiddles
+    __syncthreads();  // twiddles (and the coefficient rows)
 #pragma unroll 1
     for (int g = 0; g < GV; ++g) {
         const int y = ybase + g * LPC + l;
         const bool valid = y < ny;
         if (g + 1 < GV)
             load_row(y + LPC, vn);
+        if constexpr (YD) {
+            if (valid && (y < ZPOW_N || ny - 1 - y < ZPOW_N)) {
+#pragma unroll
+                for (int r = 0; r < L::SLOTS; ++r) {
+                    const int x = j + r * L::TPL;
+                    if (column_active(P, x)) {
+                        float2 cy[2 * NP];
+                        if constexpr (ycoef_smem<L>()) {
+#pragma unroll
+                            for (int i = 0; i < 2 * NP; ++i)
+                                cy[i] = ycs[i * n + x];
+                        } else {
+                            float2 ed[EDGE_SLOTS];
+#pragma unroll
+                            for (int e = 0; e < EDGE_SLOTS; ++e)
+                                ed[e] = edge_used(e, NP) ? yed[(size_t)edge_row(e, NP) * n + x]
+                                                         : make_float2(0.f, 0.f);
+                            pf_coefs<NP>(P.kys, ed, cy);
+                        }
+                        v[r] = pf_apply<NP>(P, cy, y, ny, v[r]);
+                    }
+                }
+            }
+        }
         if (valid && zb_any) {
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
@@ -955,8 +1075,13 @@ static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 
             }
             const unsigned grid =
                 (unsigned)((long long)qn * ((P.ny + rows_per_cta<LPC>() - 1) / rows_per_cta<LPC>()));
-            k_rows_inverse<L, LPC, NP>
-                <<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, Tab, slab, q0, qn);
+            if (P.ydefer)
+                k_rows_inverse<L, LPC, NP, true>
+                    <<<grid, LPC * L::TPL, smem_rows<L>(line.n) + smem_rows_y<L, NP, true>(line.n), s>>>(
+                        P, line, T, Tab, slab, q0, qn);
+            else
+                k_rows_inverse<L, LPC, NP, false>
+                    <<<grid, LPC * L::TPL, smem_rows<L>(line.n), s>>>(P, line, T, Tab, slab, q0, qn);
             return cudaGetLastError();
         } else {
             return cudaErrorInvalidValue;
@@ -972,8 +1097,13 @@ static cudaError_t set_smem_attrs_np(int n)
 {
     cudaError_t e;
     if constexpr (NP >= 1) {
-        e = cudaFuncSetAttribute(k_rows_inverse<L, Cfg<L>::LPC, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem_rows<L>(n));
+        e = cudaFuncSetAttribute(k_rows_inverse<L, Cfg<L>::LPC, NP, false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rows<L>(n));
+        if (e != cudaSuccess)
+            return e;
+        e = cudaFuncSetAttribute(k_rows_inverse<L, Cfg<L>::LPC, NP, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(smem_rows<L>(n) + smem_rows_y<L, NP, true>(n)));
         if (e != cudaSuccess)
             return e;
         e = cudaFuncSetAttribute(k_rows_line<L, Cfg<L>::LPC, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
