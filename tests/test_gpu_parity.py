@@ -144,6 +144,29 @@ def test_padding_and_sizes(odt, shape, padding, padval):
     assert_close(got, ref, what=str(shape))
 
 
+@pytest.mark.parametrize("order", [2, 4])
+@pytest.mark.parametrize("shape,padding", [
+    ((5, 30, 24), (False, False)),   # generic DFT columns
+    ((5, 64, 64), (False, False)),   # 64-point Stockham columns, no crop
+    ((4, 70, 40), (True, True)),     # 128-point columns cropped to 70
+])
+def test_tilted_sizes_and_orders(odt, shape, padding, order):
+    """Tilted plans whose y crop is not the centred half: the column stage
+    stores the crop raw with the y-line samples around its ends, and the
+    row stage adds the y-prefilter boundary terms (one pole at order 2, two
+    at order 4), for every column line type."""
+    rng = np.random.default_rng(sum(shape) + order)
+    A = shape[0]
+    sino = np.exp(1j * rng.normal(0, .4, shape) + rng.normal(0, .05, shape))
+    angles = np.sort(rng.uniform(0, 2 * np.pi, A))
+    ax = [0.15, 1.0, -0.2]
+    kw = dict(res=2.5, nm=1.335, lD=1.5, padding=padding, padval="edge",
+              intp_order=order)
+    ref = O.backpropagate_3d_tilted(sino, angles, tilted_axis=ax, **kw)
+    got = odt.backpropagate_3d_tilted(sino, angles, tilted_axis=ax, **kw)
+    assert_close(got, ref, what="%s order %d" % (shape, order))
+
+
 def test_onlyreal_matches_real_part(odt):
     """test_alg3d_bpp.py:77-98."""
     sino, angles = gauss_sino_3d(Nx=10, Ny=10)
