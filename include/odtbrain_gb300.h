@@ -9,7 +9,8 @@
  * (also backpropagate_2d through a ny = 1 plan), and of the steps either
  * side of it, declared further down: odt_to_ri / opt_to_ri, the sinogram
  * preparation sinogram_as_rytov / sinogram_as_radon, and the
- * missing-apple-core correction apple.correct.
+ * missing-apple-core correction apple.correct with its helpers
+ * constraint_nn / constraint_sh / envelope_gauss.
  *
  * The reference is pure Python (NumPy + pyFFTW + numexpr + scipy.ndimage +
  * multiprocessing); it has no foreign-function interface of its own.  The
@@ -26,7 +27,8 @@
  * All functions return an odt_status; none of them throws.  Device pointers
  * are raw CUDA device addresses; `stream` is a cudaStream_t passed as void*.
  * Execution is stream-ordered and does not synchronise the host, except
- * odt_bpp3d_read_status which waits for the stream.
+ * where a declaration says it is synchronous (the read_status calls, the
+ * apple correction and envelope, the "sh" constraint).
  */
 #ifndef ODTBRAIN_GB300_H
 #define ODTBRAIN_GB300_H
