@@ -1027,7 +1027,18 @@ __global__ void __launch_bounds__(256, ORDER >= 4 ? 2 : 4) k_rotate_3d(RotParams
                         t0[i] = Ib[i] + Spline<ORDER>::weights(l[i], wt[i]);
                 }
                 float2 acc = part[q];
-                if (interior) {
+                // every tap of this output inside the slab (all of them in an
+                // interior tile; elsewhere most outputs away from the slab's
+                // faces): plain addressing, the same loads in the same order
+                // as the mirrored path below
+                bool direct = interior;
+                if (!interior) {
+                    direct = true;
+#pragma unroll
+                    for (int i = 0; i < 3; ++i)
+                        direct = direct && t0[i] >= 0 && t0[i] + ORDER <= n3[i] - 1;
+                }
+                if (direct) {
                     const int off = (t0[2] * nx + t0[0]) * yp + (ny - 1 - t0[1]);
 #pragma unroll
                     for (int k2 = 0; k2 <= ORDER; ++k2) {
