@@ -546,14 +546,14 @@ odt_status odt_bpp3d_plan_create(const odt_bpp3d_desc *desc, odt_bpp3d_plan **ou
 
     // ---- batching: the largest angle batch (and column-stage chunk) whose
     // workspace fits the limit
-    // tilted path, order >= 2, crops other than the centred half: the
-    // column stage leaves the y-prefilter terms to the row stage and stores
-    // each job's raw edge samples (4 np rows) after the chunk's jobs
+    // tilted path, order >= 2: the column stage leaves the y-prefilter
+    // terms to the row stage and stores each job's raw edge samples (4 np
+    // rows) after the chunk's jobs
     p->jobs = 0;
     p->ydefer = 0;
     {
         const StageParams G = stage_params(p);
-        p->ydefer = (tilted && pf && !odt::half_crop(G) && !odt::single_row_plan(G)) ? 1 : 0;
+        p->ydefer = (tilted && pf && !odt::single_row_plan(G)) ? 1 : 0;
     }
     const size_t plane_row_bytes = (size_t)d.ny * lNx * 8;           // one job's column-stage output
     const size_t edge_row_bytes = p->ydefer ? (size_t)4 * np * lNx * 8 : 0;  // its y-prefilter edge samples

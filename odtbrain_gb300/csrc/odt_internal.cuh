@@ -74,9 +74,8 @@ struct StageParams {
     const float2 *again; // optional complex per-angle gain [A][lNy*lNx], this
                          // batch's first angle at again (NULL: 1)
     int *status;
-    // Tilted path, order >= 2, crops other than the centred half (ydefer =
-    // 1): the column stage leaves the y-prefilter boundary terms to the row
-    // stage and stores the raw y-line samples around the crop's ends, 4
+    // Tilted path, order >= 2 (ydefer = 1): the column stage leaves the
+    // y-prefilter boundary terms to the row stage and stores the raw y-line samples around the crop's ends, 4
     // npoles rows of lNx per job (edge_row order), at T + yedge_off + (q -
     // q0) * 4 npoles * lNx of the job chunk's buffer T.
     int ydefer;

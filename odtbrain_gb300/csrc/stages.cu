@@ -236,14 +236,27 @@ __device__ __forceinline__ void column_inverse_store(const StageParams &P, const
 // of the y-prefilter solve at compile-time slots, so the crop needs no
 // predicates and the stores use constant offsets from one row pointer.
 // dst points at row 0 of the job's T block, column kx (row stride N).
-template <class L, int KX, int YF, bool TW2>
+// DEFER (P.ydefer): as in column_inverse_store, the raw edge samples go to
+// yedge[row * N] (their holders and slots are compile-time here) and the
+// row stage adds the y-prefilter terms.
+template <class L, int KX, int YF, bool TW2, bool DEFER = false>
 __device__ __forceinline__ void column_inverse_store_half(const StageParams &P, const L &line, float2 (&v)[L::SLOTS],
                                                           int c, int j, float2 *buf0, float2 *buf1,
-                                                          const float2 *tw, float2 *edge, int &flip, float2 *dst)
+                                                          const float2 *tw, float2 *edge, int &flip, float2 *dst,
+                                                          float2 *yedge = nullptr)
 {
     constexpr int N = L::N, TPL = L::TPL, NY = N / 2, PAD = N / 4;
     line.template run<1, true, TW2>(v, j, buf0 + c, buf1 + c, KX, tw, flip);
-    if constexpr (YF > 0) {
+    if constexpr (YF > 0 && DEFER) {
+#pragma unroll
+        for (int e = 0; e < EDGE_SLOTS; ++e) {
+            if (edge_used(e, YF)) {
+                const int pos = PAD + edge_offset(e, NY);
+                if (j == pos % TPL)
+                    yedge[(size_t)edge_row(e, YF) * N] = v[pos / TPL];
+            }
+        }
+    } else if constexpr (YF > 0) {
         // y-prefilter boundary terms from u around the crop's ends
         // (compile-time positions)
 #pragma unroll
@@ -406,9 +419,10 @@ __global__ void __launch_bounds__(KX * L::TPL, (KX * L::TPL <= 256) ? 3 : ((KX *
             else if (HALF || ky < n)  // half-crop plans: a power-of-two line, ky < n
                 V[r] = cmul(V[r], stp[ky * KX + c]);
         }
-        if constexpr (HALF)
-            column_inverse_store_half<L, KX, YF, TW2>(P, line, v, c, j, buf0, buf1, tw, edge, flip,
-                                                  T + (size_t)(q - q0) * (L::N / 2) * L::N + kx);
+        if constexpr (HALF)  // (tilted: the y-prefilter terms go to the row stage)
+            column_inverse_store_half<L, KX, YF, TW2, (YF > 0)>(
+                P, line, v, c, j, buf0, buf1, tw, edge, flip, T + (size_t)(q - q0) * (L::N / 2) * L::N + kx,
+                T + P.yedge_off + (size_t)(q - q0) * 4 * (YF > 0 ? YF : 1) * L::N + kx);
         else if constexpr (YF > 0)  // (tilted: the y-prefilter terms go to the row stage)
             column_inverse_store<L, KX, YF, TW2, true>(
                 P, line, v, c, j, colok, buf0, buf1, tw, edge, flip, T + (size_t)(q - q0) * ny * lNx + kx,
@@ -640,7 +654,9 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
 // predicates.  The all-zero spectrum columns (outside the |k| < km disc,
 // not written by the column stage) are a per-thread slot mask computed
 // once.  A CTA owns LPC*G consecutive rows of one job, LPC lines at a time.
-template <class L, int LPC, int G, int NP>
+// YD (P.ydefer): the tilted path's y-prefilter terms, added as in
+// k_rows_inverse.
+template <class L, int LPC, int G, int NP, bool YD>
 __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
     k_rows_inverse_half(StageParams P, L line, const float2 *T, const float2 *Tab, float2 *slab, int q0)
 {
@@ -696,14 +712,63 @@ __global__ void __launch_bounds__(LPC * L::TPL, (LPC * L::TPL <= 256) ? 4 : 1)
         for (int r = 0; r < L::SLOTS; ++r)
             v[r] = (zmask >> r) & 1u ? make_float2(0.f, 0.f) : __ldcs(src + r * TPL);
     };
+    // YD: the y-prefilter coefficient rows of this job, [2 NP][N] after the
+    // edge slots (CTAs with boundary rows)
+    float2 *ycs = edge + EDGE_SLOTS * LPC;
+    const float2 *yed = T + P.yedge_off + (size_t)qrel * 4 * NP * N;
+    if constexpr (YD && ycoef_smem<L>()) {
+        if (ybase < ZPOW_N || ybase + RG - 1 >= NX - ZPOW_N) {
+            for (int x = threadIdx.x; x < N; x += LPC * TPL) {
+                float2 cy[2 * NP];
+                if (!(x >= P.kx_zero_lo && x < P.kx_zero_hi)) {
+                    float2 ed[EDGE_SLOTS];
+#pragma unroll
+                    for (int e = 0; e < EDGE_SLOTS; ++e)
+                        ed[e] = edge_used(e, NP) ? yed[(size_t)edge_row(e, NP) * N + x] : make_float2(0.f, 0.f);
+                    pf_coefs<NP>(P.kys, ed, cy);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 2 * NP; ++i)
+                        cy[i] = make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int i = 0; i < 2 * NP; ++i)
+                    ycs[i * N + x] = cy[i];
+            }
+        }
+    }
     float2 v[L::SLOTS], vn[L::SLOTS];
     load_row(ybase + l, v);
-    __syncthreads();  // twiddles
+    __syncthreads();  // twiddles (and the coefficient rows)
 #pragma unroll 1
     for (int g = 0; g < G; ++g) {
         const int y = ybase + g * LPC + l;
         if (g + 1 < G)
             load_row(y + LPC, vn);
+        if constexpr (YD) {
+            if (y < ZPOW_N || NX - 1 - y < ZPOW_N) {
+#pragma unroll
+                for (int r = 0; r < L::SLOTS; ++r) {
+                    if (!((zmask >> r) & 1u)) {
+                        const int x = j + r * TPL;
+                        float2 cy[2 * NP];
+                        if constexpr (ycoef_smem<L>()) {
+#pragma unroll
+                            for (int i = 0; i < 2 * NP; ++i)
+                                cy[i] = ycs[i * N + x];
+                        } else {
+                            float2 ed[EDGE_SLOTS];
+#pragma unroll
+                            for (int e = 0; e < EDGE_SLOTS; ++e)
+                                ed[e] = edge_used(e, NP) ? yed[(size_t)edge_row(e, NP) * N + x]
+                                                         : make_float2(0.f, 0.f);
+                            pf_coefs<NP>(P.kys, ed, cy);
+                        }
+                        v[r] = pf_apply<NP>(P, cy, y, NX, v[r]);
+                    }
+                }
+            }
+        }
         if (zb_any) {
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
@@ -1068,8 +1133,13 @@ static cudaError_t rows_inverse_impl(const StageParams &P, L line, const float2 
                 if (half_crop(P)) {
                     constexpr int G = half_groups<L>();
                     const unsigned grid = (unsigned)((long long)qn * (L::N / 2 / (LPC * G)));
-                    k_rows_inverse_half<L, LPC, G, NP>
-                        <<<grid, LPC * L::TPL, smem_rows_half<L>(line.n), s>>>(P, line, T, Tab, slab, q0);
+                    if (P.ydefer)
+                        k_rows_inverse_half<L, LPC, G, NP, true>
+                            <<<grid, LPC * L::TPL, smem_rows_half<L>(line.n) + smem_rows_y<L, NP, true>(line.n),
+                               s>>>(P, line, T, Tab, slab, q0);
+                    else
+                        k_rows_inverse_half<L, LPC, G, NP, false>
+                            <<<grid, LPC * L::TPL, smem_rows_half<L>(line.n), s>>>(P, line, T, Tab, slab, q0);
                     return cudaGetLastError();
                 }
             }
@@ -1117,8 +1187,13 @@ static cudaError_t set_smem_attrs_np(int n)
         if (e != cudaSuccess)
             return e;
         if constexpr (NP >= 1) {
-            e = cudaFuncSetAttribute(k_rows_inverse_half<L, Cfg<L>::LPC, half_groups<L>(), NP>,
+            e = cudaFuncSetAttribute(k_rows_inverse_half<L, Cfg<L>::LPC, half_groups<L>(), NP, false>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_rows_half<L>(n));
+            if (e != cudaSuccess)
+                return e;
+            e = cudaFuncSetAttribute(k_rows_inverse_half<L, Cfg<L>::LPC, half_groups<L>(), NP, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(smem_rows_half<L>(n) + smem_rows_y<L, NP, true>(n)));
             if (e != cudaSuccess)
                 return e;
         }
